@@ -1,0 +1,173 @@
+"""ctypes binding of the CPU restatement (oracle/liboracle.so).
+
+TEST INFRASTRUCTURE: imported only by tests/, by __graft_entry__.smoke() and
+by bench.py's CPU-baseline / reference leg, always as the checker or the timed
+CPU baseline, never as part of the product path. `python -c "import
+__graft_entry__ as g; g.build()"` compiles the library.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+RANKING = {"full": 0, "high": 1, "prefix": 2}
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: run __graft_entry__.build() first")
+        _lib = C.CDLL(LIB_PATH)
+        P, U32, I32, D = C.c_void_p, C.c_uint32, C.c_int, C.c_double
+        _lib.oracle_last_error.restype = C.c_char_p
+        _lib.oracle_load.argtypes = [C.c_char_p, U32]
+        _lib.oracle_load.restype = P
+        _lib.oracle_free.argtypes = [P]
+        _lib.oracle_search.argtypes = [P, P, U32, U32, U32, I32, U32, P, P]
+        _lib.oracle_info.argtypes = [P, P, P]
+        _lib.oracle_list_offsets.argtypes = [P, P]
+        _lib.oracle_codes.argtypes = [P, P, P, P, P, P, P]
+        _lib.oracle_centroid_codes.argtypes = [P, P, P, P]
+        _lib.oracle_rotate.argtypes = [P, P, U32, P]
+        _lib.oracle_rotate_with.argtypes = [P, U32, U32, P, P]
+        _lib.oracle_quantize.argtypes = [P, P, U32, P, P, P, P, P]
+        _lib.oracle_coarse.argtypes = [P, P, P, P, U32, U32, P]
+        _lib.oracle_sq16_l2.argtypes = [P, P, P, P, P, P, D, U32, U32, U32, P]
+        _lib.oracle_sq16_high_l2.argtypes = [P, P, P, P, D, U32, U32, U32, U32, P]
+        _lib.oracle_to_dist.argtypes = [C.c_int64, D]
+        _lib.oracle_to_dist.restype = C.c_float
+        _lib.oracle_set_threads.argtypes = [I32]
+        _lib.oracle_max_threads.restype = I32
+    return _lib
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def set_threads(n: int) -> None:
+    lib().oracle_set_threads(n)
+
+
+def max_threads() -> int:
+    return lib().oracle_max_threads()
+
+
+class OracleIndex:
+    """The restated reference index: codes, norms and search on the CPU."""
+
+    def __init__(self, prefix: str, prefix_dims: int = 0):
+        self.h = lib().oracle_load(prefix.encode(), prefix_dims)
+        if not self.h:
+            raise RuntimeError(lib().oracle_last_error().decode())
+        info = np.zeros(8, np.uint32)
+        scale = np.zeros(4, np.float64)
+        lib().oracle_info(self.h, _p(info), _p(scale))
+        (self.dim, self.nlist, self.npts, self.dc, self.head_dims, rot, norm, dimc) = map(int, info)
+        self.rotated, self.normalized, self.has_dimc = bool(rot), bool(norm), bool(dimc)
+        self.lo, self.inv_step, self.step, self.step_sq = map(float, scale)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().oracle_free(self.h)
+            self.h = None
+
+    def search(self, q, k=10, nprobe=64, ranking="prefix", survivors=32):
+        q = np.ascontiguousarray(q, dtype=np.float32)
+        nq = q.shape[0]
+        ids = np.zeros((nq, k), np.uint32)
+        dists = np.zeros((nq, k), np.float32)
+        rc = lib().oracle_search(self.h, _p(q), nq, k, nprobe, RANKING[ranking], survivors,
+                                 _p(ids), _p(dists))
+        if rc:
+            raise ValueError(f"oracle error {rc}: {lib().oracle_last_error().decode()}")
+        return ids, dists
+
+    def list_offsets(self) -> np.ndarray:
+        off = np.zeros(self.nlist + 1, np.uint32)
+        lib().oracle_list_offsets(self.h, _p(off))
+        return off
+
+    def codes(self) -> dict:
+        n, dc = self.npts, self.dc
+        out = dict(hi=np.zeros((n, dc), np.uint8), lo=np.zeros((n, dc), np.uint8),
+                   norm=np.zeros(n, np.int64), hinorm=np.zeros(n, np.int64),
+                   headnorm=np.zeros(n, np.int64), ids=np.zeros(n, np.uint32))
+        lib().oracle_codes(self.h, _p(out["hi"]), _p(out["lo"]), _p(out["norm"]),
+                           _p(out["hinorm"]), _p(out["headnorm"]), _p(out["ids"]))
+        return out
+
+    def centroid_codes(self) -> dict:
+        out = dict(hi=np.zeros((self.nlist, self.dc), np.uint8),
+                   lo=np.zeros((self.nlist, self.dc), np.uint8),
+                   norm=np.zeros(self.nlist, np.int64))
+        lib().oracle_centroid_codes(self.h, _p(out["hi"]), _p(out["lo"]), _p(out["norm"]))
+        return out
+
+    def rotate(self, x) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        out = np.zeros_like(x)
+        lib().oracle_rotate(self.h, _p(x), x.shape[0], _p(out))
+        return out
+
+    def quantize(self, fq) -> dict:
+        fq = np.ascontiguousarray(fq, dtype=np.float32)
+        nq = fq.shape[0]
+        out = dict(hi=np.zeros((nq, self.dc), np.uint8), lo=np.zeros((nq, self.dc), np.uint8),
+                   norm=np.zeros(nq, np.int64), hinorm=np.zeros(nq, np.int64),
+                   h0norm=np.zeros(nq, np.int64))
+        lib().oracle_quantize(self.h, _p(fq), nq, _p(out["hi"]), _p(out["lo"]), _p(out["norm"]),
+                              _p(out["hinorm"]), _p(out["h0norm"]))
+        return out
+
+    def coarse(self, qhi, qlo, qnorm, nprobe: int) -> np.ndarray:
+        nq = qhi.shape[0]
+        probed = np.zeros((nq, nprobe), np.uint32)
+        rc = lib().oracle_coarse(self.h, _p(np.ascontiguousarray(qhi)), _p(np.ascontiguousarray(qlo)),
+                                 _p(np.ascontiguousarray(qnorm, dtype=np.int64)), nq, nprobe,
+                                 _p(probed))
+        if rc:
+            raise ValueError(lib().oracle_last_error().decode())
+        return probed
+
+
+def rotate_with(x: np.ndarray, rot: np.ndarray) -> np.ndarray:
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    rot = np.ascontiguousarray(rot, dtype=np.float32)
+    out = np.zeros_like(x)
+    lib().oracle_rotate_with(_p(x), x.shape[0], x.shape[1], _p(rot), _p(out))
+    return out
+
+
+def sq16_l2(qh, ql, xh, xl, qn, xn, step_sq):
+    m, dims = qh.shape
+    n = xh.shape[0]
+    out = np.zeros((m, n), np.float32)
+    lib().oracle_sq16_l2(_p(np.ascontiguousarray(qh)), _p(np.ascontiguousarray(ql)),
+                         _p(np.ascontiguousarray(xh)), _p(np.ascontiguousarray(xl)),
+                         _p(np.ascontiguousarray(qn, dtype=np.int64)),
+                         _p(np.ascontiguousarray(xn, dtype=np.int64)), step_sq, m, n, dims, _p(out))
+    return out
+
+
+def sq16_high_l2(qh, xh, qn, xn, step_sq, dims=None):
+    m = qh.shape[0]
+    n, plane_dim = xh.shape
+    dims = dims or qh.shape[1]
+    out = np.zeros((m, n), np.float32)
+    lib().oracle_sq16_high_l2(_p(np.ascontiguousarray(qh)), _p(np.ascontiguousarray(xh)),
+                              _p(np.ascontiguousarray(qn, dtype=np.int64)),
+                              _p(np.ascontiguousarray(xn, dtype=np.int64)), step_sq, m, n, dims,
+                              plane_dim, _p(out))
+    return out
+
+
+def to_dist(l2: int, step_sq: float) -> float:
+    return float(lib().oracle_to_dist(int(l2), step_sq))
