@@ -1,0 +1,153 @@
+/* C ABI of libkatoann_gpu.so: the sm_103a kernels of KatoANN's batched IVF
+ * search over 16-bit split-byte codes.
+ *
+ * Plain pointers and sizes only. Every pointer named d_* is device memory;
+ * every call is asynchronous on the given stream (0 = the legacy default
+ * stream) unless it says otherwise. Calls return 0 on success or a negative
+ * status and never throw:
+ *   KATO_EINVAL  bad argument       (the reference throws std::invalid_argument)
+ *   KATO_ERUNTIME CUDA/runtime error (std::runtime_error)
+ *   KATO_ELOGIC  call out of order   (std::logic_error)
+ *   KATO_ENOMEM  workspace too small or allocation failed
+ * katoann_gpu_last_error() gives the message of the calling thread's last
+ * failure.
+ *
+ * Codes are stored row-major, one row per database vector, lists concatenated
+ * in list order (list c owns rows [list_off[c], list_off[c+1])). The high
+ * bytes and the low bytes of the 16-bit codes are two planes of dc bytes per
+ * row (dc = dim rounded up to 64, padding bytes zero). The reference packs the
+ * same bytes in AMX tile order (src/kernels.cpp:263-275); row-major rows are
+ * what TMA and coalesced loads want on the GPU. */
+#ifndef KATOANN_GPU_H_
+#define KATOANN_GPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *katoann_stream_t; /* = cudaStream_t */
+
+enum {
+  KATO_OK = 0,
+  KATO_EINVAL = -1,
+  KATO_ERUNTIME = -2,
+  KATO_ELOGIC = -3,
+  KATO_ENOMEM = -4
+};
+
+/* Ranking of SearchParams (include/katoann/index.h:45-49 of the reference). */
+enum { KATO_RANK_FULL = 0, KATO_RANK_HIGH = 1, KATO_RANK_PREFIX = 2 };
+
+/* A device-resident index, as the host library uploads it. All arrays are
+ * owned by the caller (the host Index). */
+typedef struct {
+  uint32_t dim, dc, nlist, npts;
+  uint32_t head_dims;    /* prefix dims of the ranking pass, 0 if none */
+  uint32_t rotated;      /* queries are rotated by d_rotation first */
+  uint32_t max_list;     /* largest list size */
+  uint32_t reserved;
+  float lo;              /* global minimum of the rotated list values */
+  float pad;
+  double inv_step;       /* 65535 / (hi - lo) */
+  double step_sq;        /* ((hi - lo) / 65535)^2 */
+  const float *d_rotation;   /* dim x dim, row j = basis j; NULL if !rotated */
+  const uint8_t *d_hi;       /* npts x dc */
+  const uint8_t *d_lo;       /* npts x dc */
+  const int64_t *d_norm;     /* npts: sum of code^2 */
+  const int64_t *d_hinorm;   /* npts: sum of high byte^2 over dc */
+  const int64_t *d_headnorm; /* npts: sum of high byte^2 over head_dims; NULL if none */
+  const uint32_t *d_ids;     /* npts */
+  const uint32_t *d_list_off;/* nlist + 1 */
+  const uint8_t *d_chi;      /* nlist x dc, centroids coded with the database scale */
+  const uint8_t *d_clo;      /* nlist x dc */
+  const int64_t *d_cnorm;    /* nlist */
+} katoann_gpu_index;
+
+const char *katoann_gpu_last_error(void);
+int katoann_gpu_version(void);
+
+/* out[i][j] = <in_i, rot_j> with the reference's float arithmetic
+ * (rotate_rows, src/index.cpp:214-270, and rotate_rows_serial, :139-180,
+ * which give identical bits), nrows x d row-major in and out. */
+int katoann_gpu_rotate_rows(const float *d_in, uint32_t nrows, uint32_t d, const float *d_rot,
+                            float *d_out, katoann_stream_t stream);
+
+/* Global minimum and maximum of n floats, written to h_out[0..1] (host);
+ * d_scratch is 8 bytes of device memory. Synchronous. Replaces the reduction
+ * of quantize_sq16_ (src/index.cpp:634-645). */
+int katoann_gpu_minmax(const float *d_x, size_t n, uint32_t *d_scratch, float *h_out,
+                       katoann_stream_t stream);
+
+/* 16-bit codes of nrows x d floats: v = clamp(lround((x - lo) * inv_step)),
+ * high/low byte planes nrows x dc (padding zero), and the squared norms of
+ * the codes (norm), of the high bytes (hinorm) and of the high bytes of the
+ * leading head_dims dimensions (headnorm, skipped when NULL). Follows
+ * src/index.cpp:632-689 (lists), :717-750 (centroids), :917-943 (queries). */
+int katoann_gpu_quantize_rows(const float *d_x, uint32_t nrows, uint32_t d, uint32_t dc, float lo,
+                              double inv_step, uint32_t head_dims, uint8_t *d_hi, uint8_t *d_lo,
+                              int64_t *d_norm, int64_t *d_hinorm, int64_t *d_headnorm,
+                              katoann_stream_t stream);
+
+/* The reference's sq16_l2 (include/katoann/kernels.h:187-193) on row-major
+ * device planes: out[m][n] = float(double(qn + xn - 2 q.x) * step_sq), exact. */
+int katoann_gpu_sq16_l2(const uint8_t *d_qhi, const uint8_t *d_qlo, const uint8_t *d_xhi,
+                        const uint8_t *d_xlo, const int64_t *d_qnorm, const int64_t *d_xnorm,
+                        double step_sq, uint32_t m, uint32_t n, uint32_t dims, float *d_out,
+                        katoann_stream_t stream);
+
+/* The reference's sq16_high_l2 (include/katoann/kernels.h:195-205): high bytes
+ * only, over the leading `dims` of rows that are plane_dim bytes apart. */
+int katoann_gpu_sq16_high_l2(const uint8_t *d_qhi, const uint8_t *d_xhi, const int64_t *d_qnorm,
+                             const int64_t *d_xnorm, double step_sq, uint32_t m, uint32_t n,
+                             uint32_t dims, uint32_t plane_dim, float *d_out,
+                             katoann_stream_t stream);
+
+/* Coarse step of the batched search (coarse_batched_sq16_,
+ * src/index.cpp:846-877): exact SQ16 distances of nq quantized queries to the
+ * centroid planes and the nprobe nearest lists per query, ascending by
+ * (distance, list), into d_probed (nq x nprobe). d_dists (nq x nlist floats)
+ * is caller scratch that receives the distances. */
+int katoann_gpu_coarse(const katoann_gpu_index *index, const uint8_t *d_qhi, const uint8_t *d_qlo,
+                       const int64_t *d_qnorm, uint32_t nq, uint32_t nprobe, float *d_dists,
+                       uint32_t *d_probed, katoann_stream_t stream);
+
+/* Bytes of device workspace that katoann_gpu_search needs for up to
+ * max_batch queries per pass with these parameters. */
+size_t katoann_gpu_search_workspace(const katoann_gpu_index *index, uint32_t max_batch,
+                                    uint32_t k, uint32_t nprobe, int ranking, uint32_t survivors);
+
+/* Index::search on the device (src/index.cpp:879-1219): rotation and
+ * quantization of the queries, coarse product and top-nprobe, inversion of
+ * the probe lists, ranking pass with per-query top-S (S = max(survivors, k)),
+ * exact refinement and top-k (ranking PREFIX or HIGH), or the exact scan with
+ * top-k (FULL). d_queries is nq x dim; d_ids / d_dists are nq x k, nearest
+ * first, padded with UINT32_MAX / FLT_MAX. Queries are processed max_batch at
+ * a time through the workspace (d_ws, ws_bytes from
+ * katoann_gpu_search_workspace). Selection is by (distance, id), which is the
+ * reference's Selection::kLocal result and its kThreshold result wherever the
+ * latter has no tie on the survivor boundary. */
+int katoann_gpu_search(const katoann_gpu_index *index, const float *d_queries, uint32_t nq,
+                       uint32_t k, uint32_t nprobe, int ranking, uint32_t survivors,
+                       uint32_t max_batch, void *d_ws, size_t ws_bytes, uint32_t *d_ids,
+                       float *d_dists, katoann_stream_t stream);
+
+/* Diagnostics that katoann_gpu_search left in its workspace, copied to the
+ * host (synchronous on `stream`): [0] queries whose nprobe-th coarse distance
+ * was tied with a list outside the probe set, [1] queries whose survivor
+ * boundary (S-th ranking distance) was tied, [2] queries searched. */
+int katoann_gpu_workspace_stats(const void *d_ws, uint64_t *h_stats, uint32_t n,
+                                katoann_stream_t stream);
+
+/* float(double(l2) * step_sq) for n int64 values on the device (test hook of
+ * the exact conversion every kernel uses). */
+int katoann_gpu_dist_values(const int64_t *d_l2, uint32_t n, double step_sq, float *d_out,
+                            katoann_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KATOANN_GPU_H_ */

@@ -1,0 +1,135 @@
+// extern "C" entry points of libkatoann_gpu.so (declared in
+// include/katoann_gpu.h). Argument checks mirror the reference's exceptions
+// (src/index.cpp:882-892) as status codes; nothing throws across the ABI.
+#include <cstdio>
+#include <string>
+
+#include "kcommon.cuh"
+
+namespace kato {
+
+namespace {
+thread_local std::string g_error;
+}
+
+void set_error(const std::string &msg) { g_error = msg; }
+
+int cuda_status(cudaError_t e, const char *what) {
+  g_error = std::string(what) + ": " + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? KATO_ENOMEM : KATO_ERUNTIME;
+}
+
+int rotate_rows(const float *in, uint32_t nrows, uint32_t d, const float *rot, float *out,
+                cudaStream_t st);
+int minmax(const float *x, size_t n, uint32_t *d_keys, float *h_out, cudaStream_t st);
+int quantize_rows(const float *x, uint32_t nrows, uint32_t d, uint32_t dc, float lo,
+                  double inv_step, uint32_t head, uint8_t *hi, uint8_t *lop, int64_t *norm,
+                  int64_t *hinorm, int64_t *headnorm, cudaStream_t st);
+int sq16_tiles(const uint8_t *qhi, const uint8_t *qlo, const uint8_t *xhi, const uint8_t *xlo,
+               const int64_t *qn, const int64_t *xn, double step_sq, uint32_t m, uint32_t n,
+               uint32_t dims, uint32_t qstride, uint32_t xstride, float *out, bool full,
+               cudaStream_t st);
+int select_topp(const float *dists, uint32_t nq, uint32_t n, uint32_t p, uint32_t *probed,
+                unsigned long long *tie_count, cudaStream_t st);
+int dist_values(const int64_t *l2, uint32_t n, double step_sq, float *out, cudaStream_t st);
+int search(const katoann_gpu_index *ix, const float *queries, uint32_t nq, uint32_t k, uint32_t p,
+           int ranking, uint32_t survivors, uint32_t max_batch, void *ws, size_t ws_bytes,
+           uint32_t *out_ids, float *out_dists, cudaStream_t st);
+size_t search_workspace(const katoann_gpu_index *ix, uint32_t max_batch, uint32_t k, uint32_t p,
+                        int ranking, uint32_t survivors);
+
+}  // namespace kato
+
+using kato::as_stream;
+
+extern "C" {
+
+const char *katoann_gpu_last_error(void) { return kato::g_error.c_str(); }
+
+int katoann_gpu_version(void) { return 1; }
+
+int katoann_gpu_rotate_rows(const float *d_in, uint32_t nrows, uint32_t d, const float *d_rot,
+                            float *d_out, katoann_stream_t stream) {
+  if (d == 0 || d > 4096) return kato::invalid("dimension must be 1 to 4096");
+  return kato::rotate_rows(d_in, nrows, d, d_rot, d_out, as_stream(stream));
+}
+
+int katoann_gpu_minmax(const float *d_x, size_t n, uint32_t *d_scratch, float *h_out,
+                       katoann_stream_t stream) {
+  return kato::minmax(d_x, n, d_scratch, h_out, as_stream(stream));
+}
+
+int katoann_gpu_quantize_rows(const float *d_x, uint32_t nrows, uint32_t d, uint32_t dc, float lo,
+                              double inv_step, uint32_t head_dims, uint8_t *d_hi, uint8_t *d_lo,
+                              int64_t *d_norm, int64_t *d_hinorm, int64_t *d_headnorm,
+                              katoann_stream_t stream) {
+  if (dc < d || dc % 64) return kato::invalid("padded dimension must be a multiple of 64 >= dim");
+  if (head_dims > dc) return kato::invalid("prefix_dims must be a multiple of 64 within the dimension");
+  return kato::quantize_rows(d_x, nrows, d, dc, lo, inv_step, d_headnorm ? head_dims : 0, d_hi,
+                             d_lo, d_norm, d_hinorm, d_headnorm, as_stream(stream));
+}
+
+int katoann_gpu_sq16_l2(const uint8_t *d_qhi, const uint8_t *d_qlo, const uint8_t *d_xhi,
+                        const uint8_t *d_xlo, const int64_t *d_qnorm, const int64_t *d_xnorm,
+                        double step_sq, uint32_t m, uint32_t n, uint32_t dims, float *d_out,
+                        katoann_stream_t stream) {
+  return kato::sq16_tiles(d_qhi, d_qlo, d_xhi, d_xlo, d_qnorm, d_xnorm, step_sq, m, n, dims, dims,
+                          dims, d_out, true, as_stream(stream));
+}
+
+int katoann_gpu_sq16_high_l2(const uint8_t *d_qhi, const uint8_t *d_xhi, const int64_t *d_qnorm,
+                             const int64_t *d_xnorm, double step_sq, uint32_t m, uint32_t n,
+                             uint32_t dims, uint32_t plane_dim, float *d_out,
+                             katoann_stream_t stream) {
+  if (plane_dim == 0) plane_dim = dims;
+  if (plane_dim < dims || plane_dim % 64)  // src/kernels.cpp:301-303
+    return kato::invalid("plane_dim must be a multiple of 64 and at least padded_dim");
+  return kato::sq16_tiles(d_qhi, nullptr, d_xhi, nullptr, d_qnorm, d_xnorm, step_sq, m, n, dims,
+                          dims, plane_dim, d_out, false, as_stream(stream));
+}
+
+int katoann_gpu_coarse(const katoann_gpu_index *ix, const uint8_t *d_qhi, const uint8_t *d_qlo,
+                       const int64_t *d_qnorm, uint32_t nq, uint32_t nprobe, float *d_dists,
+                       uint32_t *d_probed, katoann_stream_t stream) {
+  if (!ix) return kato::invalid("null index");
+  if (nprobe == 0 || nprobe > ix->nlist) return kato::invalid("need k >= 1 and 1 <= nprobe <= nlist");
+  int rc = kato::sq16_tiles(d_qhi, d_qlo, ix->d_chi, ix->d_clo, d_qnorm, ix->d_cnorm, ix->step_sq,
+                            nq, ix->nlist, ix->dc, ix->dc, ix->dc, d_dists, true, as_stream(stream));
+  if (rc) return rc;
+  return kato::select_topp(d_dists, nq, ix->nlist, nprobe, d_probed, nullptr, as_stream(stream));
+}
+
+size_t katoann_gpu_search_workspace(const katoann_gpu_index *ix, uint32_t max_batch, uint32_t k,
+                                    uint32_t nprobe, int ranking, uint32_t survivors) {
+  if (!ix) return 0;
+  return kato::search_workspace(ix, max_batch, k, nprobe, ranking, survivors);
+}
+
+int katoann_gpu_search(const katoann_gpu_index *ix, const float *d_queries, uint32_t nq,
+                       uint32_t k, uint32_t nprobe, int ranking, uint32_t survivors,
+                       uint32_t max_batch, void *d_ws, size_t ws_bytes, uint32_t *d_ids,
+                       float *d_dists, katoann_stream_t stream) {
+  if (!ix) return kato::invalid("null index");
+  if (ix->nlist == 0) {
+    kato::set_error("search before load");
+    return KATO_ELOGIC;
+  }
+  return kato::search(ix, d_queries, nq, k, nprobe, ranking, survivors, max_batch, d_ws, ws_bytes,
+                      d_ids, d_dists, as_stream(stream));
+}
+
+int katoann_gpu_workspace_stats(const void *d_ws, uint64_t *h_stats, uint32_t n,
+                                katoann_stream_t stream) {
+  if (n > 8) return kato::invalid("at most 8 statistics");
+  KATO_CUDA(cudaMemcpyAsync(h_stats, d_ws, n * sizeof(uint64_t), cudaMemcpyDeviceToHost,
+                            as_stream(stream)));
+  KATO_CUDA(cudaStreamSynchronize(as_stream(stream)));
+  return KATO_OK;
+}
+
+int katoann_gpu_dist_values(const int64_t *d_l2, uint32_t n, double step_sq, float *d_out,
+                            katoann_stream_t stream) {
+  return kato::dist_values(d_l2, n, step_sq, d_out, as_stream(stream));
+}
+
+}  // extern "C"

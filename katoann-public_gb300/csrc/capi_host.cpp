@@ -1,0 +1,166 @@
+// extern "C" surface of libkatoann.so (include/katoann_c.h).
+#include <stdexcept>
+#include <string>
+
+#include "dist_value.h"
+#include "katoann/index.h"
+#include "katoann_c.h"
+
+namespace {
+
+thread_local std::string g_error;
+
+template <class F>
+int guarded(F &&f) {
+  try {
+    f();
+    return 0;
+  } catch (const std::invalid_argument &e) {
+    g_error = e.what();
+    return -1;
+  } catch (const std::logic_error &e) {
+    g_error = e.what();
+    return -3;
+  } catch (const std::exception &e) {
+    g_error = e.what();
+    return -2;
+  }
+}
+
+katoann::Index *I(void *p) { return static_cast<katoann::Index *>(p); }
+
+katoann::SearchParams params(uint32_t k, uint32_t nprobe, int ranking, uint32_t survivors,
+                             int selection) {
+  katoann::SearchParams p;
+  p.k = k;
+  p.nprobe = nprobe;
+  p.ranking = ranking == 0 ? katoann::Ranking::kFull
+              : ranking == 1 ? katoann::Ranking::kHighBytes
+                             : katoann::Ranking::kPrefix;
+  p.survivors = survivors;
+  p.selection = selection == 1 ? katoann::Selection::kLocal : katoann::Selection::kThreshold;
+  return p;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *katoann_last_error(void) { return g_error.c_str(); }
+
+int katoann_amx_available(void) { return katoann::amx_available() ? 1 : 0; }
+
+int katoann_build(const float *data, uint32_t n, uint32_t dim, uint32_t nlist, uint32_t train_size,
+                  uint32_t kmeans_iters, uint64_t seed, int normalized, uint32_t rotation_sample,
+                  uint32_t jacobi_sweeps, const char *prefix) {
+  return guarded([&] {
+    katoann::BuildOptions o;
+    o.nlist = nlist;
+    o.train_size = train_size;
+    o.kmeans_iters = kmeans_iters;
+    o.seed = seed;
+    o.normalized = normalized != 0;
+    o.rotation_sample = rotation_sample;
+    o.jacobi_sweeps = jacobi_sweeps;
+    katoann::Index::build(data, n, dim, o, prefix);
+  });
+}
+
+void *katoann_index_new(void) { return new katoann::Index(); }
+void katoann_index_free(void *index) { delete I(index); }
+
+int katoann_index_load(void *index, const char *prefix, int precision, int use_amx,
+                       uint32_t prefix_dims, int batched_coarse, uint32_t max_batch) {
+  return guarded([&] {
+    katoann::LoadOptions o;
+    o.precision = precision == 1 ? katoann::Precision::kBf16 : katoann::Precision::kSq16;
+    o.use_amx = use_amx != 0;
+    o.prefix_dims = prefix_dims;
+    o.batched_coarse = batched_coarse != 0;
+    if (max_batch) o.max_batch = max_batch;
+    I(index)->load(prefix, o);
+  });
+}
+
+int katoann_index_load_arrays(void *index, uint32_t dim, uint32_t nlist, uint32_t npts,
+                              int normalized, const float *centroids, const uint32_t *list_sizes,
+                              const uint32_t *ids, const float *vectors, const float *rotation,
+                              int has_dimc, uint32_t head_dims, int on_device,
+                              uint32_t prefix_dims, uint32_t max_batch) {
+  return guarded([&] {
+    katoann::IndexArrays a;
+    a.dim = dim;
+    a.nlist = nlist;
+    a.npts = npts;
+    a.normalized = normalized != 0;
+    a.centroids = centroids;
+    a.list_sizes = list_sizes;
+    a.ids = ids;
+    a.vectors = vectors;
+    a.rotation = rotation;
+    a.has_dimc = has_dimc != 0;
+    a.head_dims = head_dims;
+    a.on_device = on_device != 0;
+    katoann::LoadOptions o;
+    o.prefix_dims = prefix_dims;
+    if (max_batch) o.max_batch = max_batch;
+    I(index)->load_arrays(a, o);
+  });
+}
+
+int katoann_index_search(void *index, const float *queries, uint32_t nq, uint32_t k,
+                         uint32_t nprobe, int ranking, uint32_t survivors, int selection,
+                         uint32_t *ids, float *dists) {
+  return guarded([&] {
+    I(index)->search(queries, nq, params(k, nprobe, ranking, survivors, selection), ids, dists);
+  });
+}
+
+int katoann_index_search_device(void *index, const float *d_queries, uint32_t nq, uint32_t k,
+                                uint32_t nprobe, int ranking, uint32_t survivors, int selection,
+                                uint32_t *d_ids, float *d_dists, void *stream) {
+  return guarded([&] {
+    I(index)->search_device(d_queries, nq, params(k, nprobe, ranking, survivors, selection), d_ids,
+                            d_dists, stream);
+  });
+}
+
+int katoann_index_info(void *index, uint32_t *info) {
+  const katoann::Index &x = *I(index);
+  info[0] = x.dim();
+  info[1] = x.nlist();
+  info[2] = x.size();
+  info[3] = x.prefix_dims();
+  info[4] = x.rotated() ? 1 : 0;
+  info[5] = x.normalized() ? 1 : 0;
+  info[6] = x.batched_coarse() ? 1 : 0;
+  info[7] = 2;
+  return 0;
+}
+
+size_t katoann_index_memory_bytes(void *index) { return I(index)->memory_bytes(); }
+
+int katoann_index_list_sizes(void *index, uint32_t *sizes) {
+  const auto v = I(index)->list_sizes();
+  for (size_t i = 0; i < v.size(); ++i) sizes[i] = v[i];
+  return 0;
+}
+
+int katoann_index_stats(void *index, uint64_t *stats, uint32_t n) {
+  return guarded([&] {
+    const auto v = I(index)->last_search_stats();
+    for (uint32_t i = 0; i < n && i < v.size(); ++i) stats[i] = v[i];
+  });
+}
+
+const void *katoann_index_device_view(void *index) { return I(index)->device_view(); }
+
+void katoann_normalize_rows(float *rows, size_t n, uint32_t dim) {
+  katoann::normalize_rows(rows, n, dim);
+}
+
+float katoann_dist_value(int64_t l2, double step_sq) {
+  return kato::dist_value(l2, kato::make_dist_scale(step_sq));
+}
+
+}  // extern "C"

@@ -1,0 +1,426 @@
+// Host side of katoann::Index: reads the reference's index files, uploads
+// them, codes them on the GPU and runs searches through libkatoann_gpu.so.
+//
+// Load follows Index::load (src/index.cpp:777-807): read .meta / .centroids /
+// .invlist / .dimc (:550-611), rotate the lists (:613-629), one global 16-bit
+// scale from the min and max rotated value (:632-650), codes and norms
+// (:656-689), head norms over the prefix dims (:694-715) and the centroid
+// planes coded with the database scale (:718-750) - all of it on the device.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <fstream>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "katoann/index.h"
+#include "katoann_gpu.h"
+
+namespace katoann {
+
+namespace {
+
+constexpr uint32_t kDimcMagic = 0x434D4944u;  // "DIMC"
+
+void cuda_check(cudaError_t e, const char *what) {
+  if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+void gpu_check(int rc) {
+  if (rc == KATO_OK) return;
+  const std::string msg = katoann_gpu_last_error();
+  if (rc == KATO_EINVAL) throw std::invalid_argument(msg);
+  if (rc == KATO_ELOGIC) throw std::logic_error(msg);
+  throw std::runtime_error(msg);
+}
+
+uint32_t round_up(uint32_t x, uint32_t m) { return (x + m - 1) / m * m; }
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() { reset(); }
+  void reset() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void alloc(size_t bytes) {
+    reset();
+    if (bytes == 0) bytes = 256;
+    cuda_check(cudaMalloc(&p, bytes), "cudaMalloc");
+    n = bytes;
+  }
+  void ensure(size_t bytes) {
+    if (bytes > n) alloc(bytes);
+  }
+  template <class T>
+  T *as() const {
+    return static_cast<T *>(p);
+  }
+};
+
+}  // namespace
+
+struct Index::State {
+  uint32_t dim = 0, nlist = 0, npts = 0, dc = 0, head = 0, max_list = 0, max_batch = 4096;
+  bool normalized = false, rotated = false;
+  float lo = 0;
+  double inv_step = 0, step = 0, step_sq = 0;
+  std::vector<uint32_t> sizes;
+  DevBuf rot, hi, lop, norm, hinorm, headnorm, ids, list_off, chi, clo, cnorm;
+  katoann_gpu_index view{};
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;
+  mutable std::mutex mu;
+  mutable DevBuf ws, dq, dids, ddists;
+  mutable void *last_stream = nullptr;
+
+  ~State() {
+    if (done) cudaEventDestroy(done);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+bool amx_available() { return false; }
+
+void normalize_rows(float *v, size_t n, uint32_t d) {
+  for (size_t i = 0; i < n; ++i) {
+    float *r = v + i * d;
+    double s = 0;
+    for (uint32_t k = 0; k < d; ++k) s += static_cast<double>(r[k]) * r[k];
+    if (s > 0) {
+      const float inv = static_cast<float>(1.0 / std::sqrt(s));
+      for (uint32_t k = 0; k < d; ++k) r[k] *= inv;
+    }
+  }
+}
+
+Index::Index() = default;
+Index::~Index() = default;
+Index::Index(Index &&) noexcept = default;
+Index &Index::operator=(Index &&) noexcept = default;
+
+void Index::load(const std::string &prefix, const LoadOptions &opt) {
+  IndexArrays a;
+  std::vector<float> centroids, vectors, rotation;
+  std::vector<uint32_t> sizes, ids;
+  {
+    std::ifstream f(prefix + ".meta", std::ios::binary);
+    if (!f) throw std::runtime_error("cannot open " + prefix + ".meta");
+    uint32_t meta[3] = {0, 0, 0};
+    f.read(reinterpret_cast<char *>(meta), sizeof(meta));
+    if (!f) throw std::runtime_error("truncated " + prefix + ".meta");
+    a.dim = meta[0];
+    a.nlist = meta[1];
+    a.npts = meta[2];
+    uint32_t extra[2] = {0, 0};
+    f.read(reinterpret_cast<char *>(extra), sizeof(extra));
+    if (f.gcount() == static_cast<std::streamsize>(sizeof(extra))) {
+      if (extra[0] != 0) throw std::runtime_error("only the L2 metric is supported");
+      a.normalized = extra[1] != 0;
+    }
+  }
+  if (a.dim == 0 || a.dim > kMaxDim || a.nlist == 0)
+    throw std::runtime_error("bad header in " + prefix + ".meta");
+  centroids.assign(static_cast<size_t>(a.nlist) * a.dim, 0.0f);
+  {
+    std::ifstream f(prefix + ".centroids", std::ios::binary);
+    f.read(reinterpret_cast<char *>(centroids.data()), centroids.size() * sizeof(float));
+    if (!f) throw std::runtime_error("cannot read " + prefix + ".centroids");
+  }
+  {
+    std::ifstream f(prefix + ".invlist", std::ios::binary);
+    if (!f) throw std::runtime_error("cannot open " + prefix + ".invlist");
+    sizes.assign(a.nlist, 0);
+    uint64_t total = 0;
+    for (uint32_t c = 0; c < a.nlist && f; ++c) {
+      uint32_t sz = 0;
+      f.read(reinterpret_cast<char *>(&sz), sizeof(sz));
+      if (!f) break;
+      if (total + sz > a.npts) {
+        total += sz;
+        break;
+      }
+      sizes[c] = sz;
+      const size_t r0 = ids.size();
+      ids.resize(r0 + sz);
+      f.read(reinterpret_cast<char *>(ids.data() + r0), static_cast<std::streamsize>(sz) * 4);
+      vectors.resize((r0 + sz) * static_cast<size_t>(a.dim));
+      f.read(reinterpret_cast<char *>(vectors.data() + r0 * a.dim),
+             static_cast<std::streamsize>(sz) * a.dim * sizeof(float));
+      total += sz;
+    }
+    if (!f || total != a.npts) throw std::runtime_error("truncated " + prefix + ".invlist");
+  }
+  {
+    std::ifstream f(prefix + ".dimc", std::ios::binary);
+    if (f) {
+      uint32_t hdr[8] = {0};
+      f.read(reinterpret_cast<char *>(hdr), sizeof(hdr));
+      if (!f || hdr[0] != kDimcMagic || (hdr[1] != 1u && hdr[1] != 2u))
+        throw std::runtime_error("bad header in " + prefix + ".dimc");
+      if (hdr[2] != a.dim || hdr[3] != a.nlist || hdr[4] != a.npts)
+        throw std::runtime_error(prefix + ".dimc does not match the index");
+      a.has_dimc = true;
+      a.head_dims = hdr[5];
+      if (hdr[6] == 1u) {
+        rotation.resize(static_cast<size_t>(a.dim) * a.dim);
+        f.read(reinterpret_cast<char *>(rotation.data()),
+               static_cast<std::streamsize>(rotation.size() * sizeof(float)));
+        if (!f) throw std::runtime_error("truncated rotation in " + prefix + ".dimc");
+        a.rotation = rotation.data();
+      }
+    }
+  }
+  a.centroids = centroids.data();
+  a.list_sizes = sizes.data();
+  a.ids = ids.data();
+  a.vectors = vectors.data();
+  load_arrays(a, opt);
+}
+
+void Index::load_arrays(const IndexArrays &a, const LoadOptions &opt) {
+  if (opt.precision == Precision::kBf16)
+    throw std::invalid_argument("bf16 precision is not part of the GPU search path");
+  if (!opt.batched_coarse)
+    throw std::invalid_argument("the per-query float coarse search is not part of the GPU search path");
+  if (a.dim == 0 || a.dim > kMaxDim || a.nlist == 0)
+    throw std::invalid_argument("bad index shape: dimension must be 1 to 4096 and nlist >= 1");
+  s_.reset();
+  auto st = std::make_unique<State>();
+  State &s = *st;
+  s.dim = a.dim;
+  s.nlist = a.nlist;
+  s.npts = a.npts;
+  s.normalized = a.normalized;
+  s.dc = round_up(a.dim, 64u);
+  s.max_batch = std::max(1u, opt.max_batch);
+  cuda_check(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  cuda_check(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming), "cudaEventCreate");
+  katoann_stream_t ks = reinterpret_cast<katoann_stream_t>(s.stream);
+  const cudaMemcpyKind up = a.on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  const uint32_t d = s.dim, dc = s.dc, n = s.npts, L = s.nlist;
+
+  s.sizes.assign(a.list_sizes, a.list_sizes + L);
+  std::vector<uint32_t> off(L + 1, 0);
+  for (uint32_t c = 0; c < L; ++c) {
+    off[c + 1] = off[c] + s.sizes[c];
+    s.max_list = std::max(s.max_list, s.sizes[c]);
+  }
+  if (off[L] != n) throw std::invalid_argument("list sizes do not add up to the vector count");
+  s.list_off.alloc((L + 1) * 4ull);
+  cuda_check(cudaMemcpy(s.list_off.p, off.data(), (L + 1) * 4ull, cudaMemcpyHostToDevice), "upload");
+  s.ids.alloc(static_cast<size_t>(n) * 4);
+  if (n) cuda_check(cudaMemcpy(s.ids.p, a.ids, static_cast<size_t>(n) * 4, up), "upload ids");
+
+  // Vectors, rotated on the device when the index has a rotation.
+  DevBuf raw, rotd;
+  const size_t nv = static_cast<size_t>(n) * d;
+  const float *vec = a.vectors;
+  if (!a.on_device) {
+    raw.alloc(nv * 4);
+    if (nv) cuda_check(cudaMemcpy(raw.p, a.vectors, nv * 4, cudaMemcpyHostToDevice), "upload vectors");
+    vec = raw.as<float>();
+  }
+  s.rotated = a.rotation != nullptr;
+  if (s.rotated) {
+    s.rot.alloc(static_cast<size_t>(d) * d * 4);
+    cuda_check(cudaMemcpy(s.rot.p, a.rotation, static_cast<size_t>(d) * d * 4, up), "upload rotation");
+    rotd.alloc(nv * 4);
+    gpu_check(katoann_gpu_rotate_rows(vec, n, d, s.rot.as<float>(), rotd.as<float>(), ks));
+    vec = rotd.as<float>();
+    raw.reset();
+  }
+  // Global scale (src/index.cpp:634-650).
+  float glo = FLT_MAX, ghi = -FLT_MAX;
+  if (nv) {
+    DevBuf keys;
+    keys.alloc(8);
+    float mm[2];
+    gpu_check(katoann_gpu_minmax(vec, nv, keys.as<uint32_t>(), mm, ks));
+    glo = mm[0];
+    ghi = mm[1];
+  }
+  s.lo = glo;
+  const double rng = static_cast<double>(ghi) - glo;
+  s.inv_step = 65535.0 / rng;
+  s.step = rng / 65535.0;
+  s.step_sq = s.step * s.step;
+  // Head dims (src/index.cpp:792-793, :695-696).
+  const uint32_t dims = opt.prefix_dims ? opt.prefix_dims : a.head_dims;
+  if (a.has_dimc && dims) {
+    if (dims % 64 || dims > dc)
+      throw std::invalid_argument("prefix_dims must be a multiple of 64 within the dimension");
+    s.head = dims;
+  }
+  s.hi.alloc(static_cast<size_t>(n) * dc);
+  s.lop.alloc(static_cast<size_t>(n) * dc);
+  s.norm.alloc(static_cast<size_t>(n) * 8);
+  s.hinorm.alloc(static_cast<size_t>(n) * 8);
+  if (s.head) s.headnorm.alloc(static_cast<size_t>(n) * 8);
+  gpu_check(katoann_gpu_quantize_rows(vec, n, d, dc, s.lo, s.inv_step, s.head, s.hi.as<uint8_t>(),
+                                      s.lop.as<uint8_t>(), s.norm.as<int64_t>(),
+                                      s.hinorm.as<int64_t>(),
+                                      s.head ? s.headnorm.as<int64_t>() : nullptr, ks));
+  // Centroid planes with the database scale (src/index.cpp:718-750).
+  {
+    DevBuf cen, cenr, chn;
+    cen.alloc(static_cast<size_t>(L) * d * 4);
+    cuda_check(cudaMemcpy(cen.p, a.centroids, static_cast<size_t>(L) * d * 4, up), "upload centroids");
+    const float *cv = cen.as<float>();
+    if (s.rotated) {
+      cenr.alloc(static_cast<size_t>(L) * d * 4);
+      gpu_check(katoann_gpu_rotate_rows(cv, L, d, s.rot.as<float>(), cenr.as<float>(), ks));
+      cv = cenr.as<float>();
+    }
+    s.chi.alloc(static_cast<size_t>(L) * dc);
+    s.clo.alloc(static_cast<size_t>(L) * dc);
+    s.cnorm.alloc(static_cast<size_t>(L) * 8);
+    chn.alloc(static_cast<size_t>(L) * 8);
+    gpu_check(katoann_gpu_quantize_rows(cv, L, d, dc, s.lo, s.inv_step, 0, s.chi.as<uint8_t>(),
+                                        s.clo.as<uint8_t>(), s.cnorm.as<int64_t>(),
+                                        chn.as<int64_t>(), nullptr, ks));
+    cuda_check(cudaStreamSynchronize(s.stream), "load");
+  }
+  cuda_check(cudaStreamSynchronize(s.stream), "load");
+  rotd.reset();
+
+  katoann_gpu_index &v = s.view;
+  v.dim = d;
+  v.dc = dc;
+  v.nlist = L;
+  v.npts = n;
+  v.head_dims = s.head;
+  v.rotated = s.rotated ? 1 : 0;
+  v.max_list = s.max_list;
+  v.lo = s.lo;
+  v.inv_step = s.inv_step;
+  v.step_sq = s.step_sq;
+  v.d_rotation = s.rot.as<float>();
+  v.d_hi = s.hi.as<uint8_t>();
+  v.d_lo = s.lop.as<uint8_t>();
+  v.d_norm = s.norm.as<int64_t>();
+  v.d_hinorm = s.hinorm.as<int64_t>();
+  v.d_headnorm = s.head ? s.headnorm.as<int64_t>() : nullptr;
+  v.d_ids = s.ids.as<uint32_t>();
+  v.d_list_off = s.list_off.as<uint32_t>();
+  v.d_chi = s.chi.as<uint8_t>();
+  v.d_clo = s.clo.as<uint8_t>();
+  v.d_cnorm = s.cnorm.as<int64_t>();
+  s_ = std::move(st);
+}
+
+namespace {
+
+int ranking_code(Ranking r) {
+  return r == Ranking::kFull ? KATO_RANK_FULL : r == Ranking::kHighBytes ? KATO_RANK_HIGH : KATO_RANK_PREFIX;
+}
+
+// src/index.cpp:879-892
+void validate(const void *state, uint32_t nlist, uint32_t head, const SearchParams &p) {
+  if (!state || nlist == 0) throw std::logic_error("search before load");
+  if (p.k == 0 || p.nprobe == 0 || p.nprobe > nlist)
+    throw std::invalid_argument("need k >= 1 and 1 <= nprobe <= nlist");
+  if (p.ranking == Ranking::kPrefix && head == 0)
+    throw std::invalid_argument("prefix ranking needs the rotation file (.dimc)");
+}
+
+}  // namespace
+
+void Index::search(const float *queries, uint32_t nq, const SearchParams &p, uint32_t *ids,
+                   float *dists) const {
+  if (nq == 0) return;
+  validate(s_.get(), s_ ? s_->nlist : 0, s_ ? s_->head : 0, p);
+  State &s = *s_;
+  std::lock_guard<std::mutex> lock(s.mu);
+  const uint32_t mb = s.max_batch, b = std::min(nq, mb);
+  const int rk = ranking_code(p.ranking);
+  const size_t need = katoann_gpu_search_workspace(&s.view, b, p.k, p.nprobe, rk, p.survivors);
+  if (need == 0) gpu_check(KATO_EINVAL);
+  s.ws.ensure(need);
+  s.dq.ensure(static_cast<size_t>(b) * s.dim * 4);
+  s.dids.ensure(static_cast<size_t>(b) * p.k * 4);
+  s.ddists.ensure(static_cast<size_t>(b) * p.k * 4);
+  if (s.last_stream && s.last_stream != s.stream)
+    cuda_check(cudaStreamWaitEvent(s.stream, s.done, 0), "cudaStreamWaitEvent");
+  for (uint32_t q0 = 0; q0 < nq; q0 += mb) {
+    const uint32_t nb = std::min(mb, nq - q0);
+    cuda_check(cudaMemcpyAsync(s.dq.p, queries + static_cast<size_t>(q0) * s.dim,
+                               static_cast<size_t>(nb) * s.dim * 4, cudaMemcpyHostToDevice, s.stream),
+               "copy queries");
+    gpu_check(katoann_gpu_search(&s.view, s.dq.as<float>(), nb, p.k, p.nprobe, rk, p.survivors, mb,
+                                 s.ws.p, s.ws.n, s.dids.as<uint32_t>(), s.ddists.as<float>(),
+                                 reinterpret_cast<katoann_stream_t>(s.stream)));
+    cuda_check(cudaMemcpyAsync(ids + static_cast<size_t>(q0) * p.k, s.dids.p,
+                               static_cast<size_t>(nb) * p.k * 4, cudaMemcpyDeviceToHost, s.stream),
+               "copy ids");
+    cuda_check(cudaMemcpyAsync(dists + static_cast<size_t>(q0) * p.k, s.ddists.p,
+                               static_cast<size_t>(nb) * p.k * 4, cudaMemcpyDeviceToHost, s.stream),
+               "copy dists");
+  }
+  cuda_check(cudaEventRecord(s.done, s.stream), "cudaEventRecord");
+  s.last_stream = s.stream;
+  cuda_check(cudaStreamSynchronize(s.stream), "search");
+}
+
+void Index::search_device(const float *d_queries, uint32_t nq, const SearchParams &p,
+                          uint32_t *d_ids, float *d_dists, void *stream) const {
+  if (nq == 0) return;
+  validate(s_.get(), s_ ? s_->nlist : 0, s_ ? s_->head : 0, p);
+  State &s = *s_;
+  std::lock_guard<std::mutex> lock(s.mu);
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : s.stream;
+  const int rk = ranking_code(p.ranking);
+  const size_t need =
+      katoann_gpu_search_workspace(&s.view, std::min(nq, s.max_batch), p.k, p.nprobe, rk, p.survivors);
+  if (need == 0) gpu_check(KATO_EINVAL);
+  if (need > s.ws.n) {
+    cuda_check(cudaDeviceSynchronize(), "workspace resize");
+    s.ws.ensure(need);
+  }
+  if (s.last_stream && s.last_stream != st)
+    cuda_check(cudaStreamWaitEvent(st, s.done, 0), "cudaStreamWaitEvent");
+  gpu_check(katoann_gpu_search(&s.view, d_queries, nq, p.k, p.nprobe, rk, p.survivors, s.max_batch,
+                               s.ws.p, s.ws.n, d_ids, d_dists, reinterpret_cast<katoann_stream_t>(st)));
+  cuda_check(cudaEventRecord(s.done, st), "cudaEventRecord");
+  s.last_stream = st;
+}
+
+std::vector<uint64_t> Index::last_search_stats() const {
+  std::vector<uint64_t> out(3, 0);
+  if (!s_ || !s_->ws.p) return out;
+  std::lock_guard<std::mutex> lock(s_->mu);
+  cuda_check(cudaEventSynchronize(s_->done), "stats");
+  gpu_check(katoann_gpu_workspace_stats(s_->ws.p, out.data(), 3,
+                                        reinterpret_cast<katoann_stream_t>(s_->stream)));
+  return out;
+}
+
+const void *Index::device_view() const { return s_ ? &s_->view : nullptr; }
+
+uint32_t Index::dim() const { return s_ ? s_->dim : 0; }
+uint32_t Index::nlist() const { return s_ ? s_->nlist : 0; }
+uint32_t Index::size() const { return s_ ? s_->npts : 0; }
+bool Index::normalized() const { return s_ && s_->normalized; }
+uint32_t Index::prefix_dims() const { return s_ ? s_->head : 0; }
+bool Index::rotated() const { return s_ && s_->rotated; }
+bool Index::batched_coarse() const { return s_ != nullptr; }
+std::vector<uint32_t> Index::list_sizes() const { return s_ ? s_->sizes : std::vector<uint32_t>{}; }
+
+size_t Index::memory_bytes() const {
+  if (!s_) return 0;
+  const State &s = *s_;
+  return s.rot.n + s.hi.n + s.lop.n + s.norm.n + s.hinorm.n + s.headnorm.n + s.ids.n +
+         s.list_off.n + s.chi.n + s.clo.n + s.cnorm.n + s.sizes.size() * 4;
+}
+
+}  // namespace katoann

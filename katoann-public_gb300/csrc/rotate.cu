@@ -1,0 +1,222 @@
+// Rotation and 16-bit coding of rows on the GPU, bit-identical to the
+// reference's float arithmetic.
+//
+// The reference computes every rotated value out[i][j] = <x_i, r_j> with 16
+// lane accumulators: lane l sums x[k] * r[k] over k = l, l + 16, ... by fused
+// multiply-add in k order, the 16 lanes are added as (l, l+8), (l, l+4),
+// (l, l+2), (0, 1), and the last d % 16 dimensions follow one by one
+// (src/index.cpp:139-208). Here 16 consecutive threads of a warp play the 16
+// lanes: each thread keeps the lane sums of an 8 x 8 block of outputs, and the
+// lane reduction is a xor-butterfly of shuffles (8, 4, 2, 1), which adds the
+// same pairs in the same order, so every thread ends with the reference's
+// bits. The scalar parts are replayed with explicit rounding: the reference's
+// compiler evaluates those chains four products at a time with the products
+// rounded, then fuses the last (length % 4) terms.
+#include "kcommon.cuh"
+
+namespace kato {
+
+namespace {
+
+constexpr int kRotRows = 32;     // output rows per CTA
+constexpr int kRotCols = 32;     // output columns per CTA
+constexpr int kRotK = 64;        // k-chunk staged in shared memory
+constexpr int kRotStride = 66;   // floats per staged row (66 = 2 mod 4: no bank conflicts)
+
+// Scalar tail of one output: dimensions [k0, d), the first ((d - k0) & ~3) of
+// them with rounded products, the rest fused.
+__device__ __forceinline__ float rot_tail(float s, const float *x, const float *r, uint32_t k0,
+                                          uint32_t d) {
+  const uint32_t m = k0 + ((d - k0) & ~3u);
+  uint32_t k = k0;
+  for (; k < m; ++k) s = __fadd_rn(s, __fmul_rn(x[k], r[k]));
+  for (; k < d; ++k) s = __fmaf_rn(x[k], r[k], s);
+  return s;
+}
+
+__global__ void __launch_bounds__(256) rotate_lanes_kernel(const float *__restrict__ in,
+                                                           uint32_t nrows, uint32_t d,
+                                                           const float *__restrict__ rot,
+                                                           float *__restrict__ out) {
+  __shared__ float xs[kRotRows * kRotStride];
+  __shared__ float rs[kRotCols * kRotStride];
+  const uint32_t d4 = d & ~3u, d16 = d & ~15u;
+  const uint32_t i0 = blockIdx.x * kRotRows, j0 = blockIdx.y * kRotCols;
+  const int t = threadIdx.x, l = t & 15, g = t >> 4;
+  const int rb = (g >> 2) * 8, cb = (g & 3) * 8;
+  float acc[8][8];
+#pragma unroll
+  for (int a = 0; a < 8; ++a)
+#pragma unroll
+    for (int b = 0; b < 8; ++b) acc[a][b] = 0.0f;
+
+  for (uint32_t k0 = 0; k0 < d16; k0 += kRotK) {
+    for (int idx = t; idx < kRotRows * kRotK; idx += 256) {
+      const int r = idx / kRotK, c = idx % kRotK;
+      const uint32_t gk = k0 + c;
+      const uint32_t gi = i0 + r, gj = j0 + r;
+      xs[r * kRotStride + c] = (gi < nrows && gk < d16) ? in[static_cast<size_t>(gi) * d + gk] : 0.0f;
+      rs[r * kRotStride + c] = (gj < d4 && gk < d16) ? rot[static_cast<size_t>(gj) * d + gk] : 0.0f;
+    }
+    __syncthreads();
+    const uint32_t kend = min(static_cast<uint32_t>(kRotK), d16 - k0);
+    for (uint32_t c = 0; c < kend; c += 16) {
+      float xv[8], rv[8];
+#pragma unroll
+      for (int a = 0; a < 8; ++a) xv[a] = xs[(rb + a) * kRotStride + c + l];
+#pragma unroll
+      for (int b = 0; b < 8; ++b) rv[b] = rs[(cb + b) * kRotStride + c + l];
+#pragma unroll
+      for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) acc[a][b] = __fmaf_rn(xv[a], rv[b], acc[a][b]);
+    }
+    __syncthreads();
+  }
+  // Lane reduction in the order of the reference's horizontal add.
+#pragma unroll
+  for (int a = 0; a < 8; ++a)
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+      float v = acc[a][b];
+      v = __fadd_rn(v, __shfl_xor_sync(0xffffffffu, v, 8));
+      v = __fadd_rn(v, __shfl_xor_sync(0xffffffffu, v, 4));
+      v = __fadd_rn(v, __shfl_xor_sync(0xffffffffu, v, 2));
+      v = __fadd_rn(v, __shfl_xor_sync(0xffffffffu, v, 1));
+      acc[a][b] = v;
+    }
+  // Each of the 16 lanes finishes 4 of the 64 outputs (tail and store).
+#pragma unroll
+  for (int a = 0; a < 8; ++a)
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+      if (((a * 8 + b) & 15) != l) continue;
+      const uint32_t i = i0 + rb + a, j = j0 + cb + b;
+      if (i >= nrows || j >= d4) continue;
+      const float *x = in + static_cast<size_t>(i) * d;
+      const float *r = rot + static_cast<size_t>(j) * d;
+      out[static_cast<size_t>(i) * d + j] = rot_tail(acc[a][b], x, r, d16, d);
+    }
+}
+
+// The last d % 4 output columns: one chain over all d dimensions
+// (src/index.cpp:171-179, :247-257).
+__global__ void rotate_seq_kernel(const float *__restrict__ in, uint32_t nrows, uint32_t d,
+                                  const float *__restrict__ rot, float *__restrict__ out) {
+  const uint32_t d4 = d & ~3u, nc = d - d4;
+  const uint64_t idx = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= static_cast<uint64_t>(nrows) * nc) return;
+  const uint32_t i = static_cast<uint32_t>(idx / nc), j = d4 + static_cast<uint32_t>(idx % nc);
+  out[static_cast<size_t>(i) * d + j] =
+      rot_tail(0.0f, in + static_cast<size_t>(i) * d, rot + static_cast<size_t>(j) * d, 0, d);
+}
+
+__global__ void minmax_init_kernel(uint32_t *keys) {
+  keys[0] = 0xFFFFFFFFu;  // min
+  keys[1] = 0u;           // max
+}
+
+__global__ void minmax_kernel(const float *__restrict__ x, size_t n, uint32_t *keys) {
+  uint32_t mn = 0xFFFFFFFFu, mx = 0u;
+  for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    const uint32_t k = float_order_key(x[i]);
+    mn = min(mn, k);
+    mx = max(mx, k);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(keys, mn);
+    atomicMax(keys + 1, mx);
+  }
+}
+
+// One warp per row: codes, byte planes (padding zero) and the three norms.
+__global__ void quantize_rows_kernel(const float *__restrict__ x, uint32_t nrows, uint32_t d,
+                                     uint32_t dc, float lo, double inv_step, uint32_t head,
+                                     uint8_t *__restrict__ hi, uint8_t *__restrict__ lop,
+                                     int64_t *__restrict__ norm, int64_t *__restrict__ hinorm,
+                                     int64_t *__restrict__ headnorm) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t warp = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
+  for (uint64_t row = warp; row < nrows; row += nwarps) {
+    const float *xr = x + row * d;
+    uint8_t *hr = hi + row * dc;
+    uint8_t *lr = lop + row * dc;
+    uint64_t s = 0, sh = 0, s0 = 0;
+    for (uint32_t k = lane; k < dc; k += 32) {
+      uint32_t v = 0;
+      if (k < d) v = quantize1(xr[k], lo, inv_step);
+      const uint32_t vh = v >> 8;
+      hr[k] = static_cast<uint8_t>(vh);
+      lr[k] = static_cast<uint8_t>(v & 0xFFu);
+      s += static_cast<uint64_t>(v) * v;
+      sh += vh * vh;
+      if (k < head) s0 += vh * vh;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      s += __shfl_xor_sync(0xffffffffu, s, o);
+      sh += __shfl_xor_sync(0xffffffffu, sh, o);
+      s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+    }
+    if (lane == 0) {
+      norm[row] = static_cast<int64_t>(s);
+      hinorm[row] = static_cast<int64_t>(sh);
+      if (headnorm) headnorm[row] = static_cast<int64_t>(s0);
+    }
+  }
+}
+
+}  // namespace
+
+int rotate_rows(const float *in, uint32_t nrows, uint32_t d, const float *rot, float *out,
+                cudaStream_t st) {
+  if (nrows == 0) return KATO_OK;
+  const uint32_t d4 = d & ~3u;
+  if (d4) {
+    dim3 grid(div_up(nrows, kRotRows), div_up(d4, kRotCols));
+    rotate_lanes_kernel<<<grid, 256, 0, st>>>(in, nrows, d, rot, out);
+    KATO_LAUNCHED("rotate_lanes_kernel");
+  }
+  if (d4 < d) {
+    const uint64_t n = static_cast<uint64_t>(nrows) * (d - d4);
+    rotate_seq_kernel<<<static_cast<uint32_t>((n + 255) / 256), 256, 0, st>>>(in, nrows, d, rot, out);
+    KATO_LAUNCHED("rotate_seq_kernel");
+  }
+  return KATO_OK;
+}
+
+int minmax(const float *x, size_t n, uint32_t *d_keys, float *h_out, cudaStream_t st) {
+  minmax_init_kernel<<<1, 1, 0, st>>>(d_keys);
+  KATO_LAUNCHED("minmax_init_kernel");
+  if (n) {
+    const uint32_t blocks = static_cast<uint32_t>(std::min<size_t>((n + 255) / 256, 152 * 16));
+    minmax_kernel<<<blocks, 256, 0, st>>>(x, n, d_keys);
+    KATO_LAUNCHED("minmax_kernel");
+  }
+  uint32_t keys[2];
+  KATO_CUDA(cudaMemcpyAsync(keys, d_keys, sizeof(keys), cudaMemcpyDeviceToHost, st));
+  KATO_CUDA(cudaStreamSynchronize(st));
+  h_out[0] = float_from_order_key(keys[0]);
+  h_out[1] = float_from_order_key(keys[1]);
+  return KATO_OK;
+}
+
+int quantize_rows(const float *x, uint32_t nrows, uint32_t d, uint32_t dc, float lo,
+                  double inv_step, uint32_t head, uint8_t *hi, uint8_t *lop, int64_t *norm,
+                  int64_t *hinorm, int64_t *headnorm, cudaStream_t st) {
+  if (nrows == 0) return KATO_OK;
+  const uint32_t blocks = std::min<uint32_t>(div_up(nrows, 8), 152 * 64);
+  quantize_rows_kernel<<<blocks, 256, 0, st>>>(x, nrows, d, dc, lo, inv_step, head, hi, lop, norm,
+                                              hinorm, headnorm);
+  KATO_LAUNCHED("quantize_rows_kernel");
+  return KATO_OK;
+}
+
+}  // namespace kato

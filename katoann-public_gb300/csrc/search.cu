@@ -1,0 +1,806 @@
+// The batched search pipeline after the coarse step: inversion of the probe
+// lists, the ranking pass, the survivor merge and the exact refinement.
+//
+// Reference: Index::search_sq16_ranked_ (src/index.cpp:909-1128) and
+// Index::search_sq16_full_ (:1131-1219). The reference inverts the probe
+// lists into a hash map (invert, :403-412) and scans each probed list once
+// for all the queries that probe it (:998-1044); here the inversion is a CSR
+// built with a histogram, a scan and an atomic scatter, and each CTA of the
+// ranking kernel takes one list and up to kQG of its queries, stages the
+// list's rows in shared memory tile by tile and keeps, per query, the best S
+// candidates by (distance, id) in shared memory. Selection by (distance, id)
+// is the reference's Selection::kLocal result (:101-135 then :1063-1069) and
+// its kThreshold result wherever that has no tie on the survivor boundary.
+#include <algorithm>
+
+#include "kcommon.cuh"
+
+namespace kato {
+
+namespace {
+
+constexpr int kQG = 16;            // queries per ranking work item
+constexpr int kRT = 16;            // list rows per ranking tile
+constexpr uint32_t kChunk = 1024;  // bytes of a row staged at once
+constexpr uint32_t kSelMax = 256;  // largest per-slot S kept in shared memory
+constexpr uint32_t kEmpty = 0xFFFFFFFFu;
+constexpr int kThreads = 256;
+constexpr uint32_t kSortMax = 4096;
+
+struct Work {
+  uint32_t list, first;
+};
+
+// ---------------------------------------------------------------- inversion
+__global__ void count_kernel(const uint32_t *__restrict__ probed, uint32_t total,
+                             uint32_t *__restrict__ cnt) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < total) atomicAdd(&cnt[probed[i]], 1u);
+}
+
+// One CTA: exclusive scans of the per-list query counts (off) and of the
+// per-list work-item counts (woff); clears the scatter cursors.
+__global__ void __launch_bounds__(1024) scan_kernel(const uint32_t *__restrict__ cnt, uint32_t L,
+                                                    uint32_t *__restrict__ off,
+                                                    uint32_t *__restrict__ woff,
+                                                    uint32_t *__restrict__ cursor) {
+  __shared__ uint32_t s1[1024], s2[1024];
+  const uint32_t t = threadIdx.x, per = (L + 1023) / 1024;
+  const uint32_t b = min(L, t * per), e = min(L, b + per);
+  uint32_t a1 = 0, a2 = 0;
+  for (uint32_t c = b; c < e; ++c) {
+    a1 += cnt[c];
+    a2 += (cnt[c] + kQG - 1) / kQG;
+  }
+  s1[t] = a1;
+  s2[t] = a2;
+  __syncthreads();
+  for (uint32_t o = 1; o < 1024; o <<= 1) {
+    const uint32_t v1 = t >= o ? s1[t - o] : 0, v2 = t >= o ? s2[t - o] : 0;
+    __syncthreads();
+    s1[t] += v1;
+    s2[t] += v2;
+    __syncthreads();
+  }
+  uint32_t r1 = s1[t] - a1, r2 = s2[t] - a2;
+  for (uint32_t c = b; c < e; ++c) {
+    off[c] = r1;
+    woff[c] = r2;
+    cursor[c] = 0;
+    r1 += cnt[c];
+    r2 += (cnt[c] + kQG - 1) / kQG;
+  }
+  if (t == 1023) {
+    off[L] = s1[1023];
+    woff[L] = s2[1023];
+  }
+}
+
+__global__ void scatter_kernel(const uint32_t *__restrict__ probed, uint32_t total,
+                               const uint32_t *__restrict__ off, uint32_t *__restrict__ cursor,
+                               uint32_t *__restrict__ entries) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= total) return;
+  const uint32_t c = probed[i];
+  entries[off[c] + atomicAdd(&cursor[c], 1u)] = i;  // i = query * nprobe + rank
+}
+
+__global__ void work_kernel(const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ woff,
+                            uint32_t L, Work *__restrict__ work) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= L) return;
+  const uint32_t nw = (cnt[c] + kQG - 1) / kQG;
+  for (uint32_t j = 0; j < nw; ++j) work[woff[c] + j] = Work{c, j * kQG};
+}
+
+// ------------------------------------------------------------- ranking pass
+struct RankArgs {
+  const uint8_t *xhi, *xlo;
+  const int64_t *xnorm;  // per row norm matching the mode
+  const uint32_t *ids, *list_off;
+  const uint8_t *qhi, *qlo;
+  const int64_t *qnorm;  // per query norm matching the mode
+  const Work *work;
+  const uint32_t *woff_total;
+  const uint32_t *off, *entries;
+  uint32_t dc, dims, nprobe, S, SC;
+  uint2 *slots;  // (query * nprobe + rank) * SC entries of (key, row)
+  DistScale scale;
+};
+
+__host__ __device__ inline size_t rank_smem_bytes(int planes, bool select, uint32_t dims,
+                                                  uint32_t S) {
+  const uint32_t qw = dims / 4 + 1, kch = dims < kChunk ? dims : kChunk, rw = kch / 4 + 1;
+  size_t b = static_cast<size_t>(planes) * kQG * qw * 4 + static_cast<size_t>(planes) * kRT * rw * 4;
+  b += kRT * 4 + 3 * kQG * 4;           // sids, ccount, bcount, query ids
+  b = (b + 15) / 16 * 16;
+  b += kQG * 8;                         // query norms
+  if (select) b += static_cast<size_t>(kQG) * S * 12 + static_cast<size_t>(kQG) * kRT * 12;
+  return b;
+}
+
+// kFull: four products over dc (Ranking::kFull); otherwise high bytes over
+// `dims` (kHighBytes: dims = dc; kPrefix: dims = head dims).
+// kSelect: keep the best S per (query, list) in shared memory (S <= kSelMax);
+// otherwise write every candidate to its slot (slot capacity >= list size).
+template <bool kFull, bool kSelect>
+__global__ void __launch_bounds__(kThreads) rank_kernel(RankArgs A) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const uint32_t w = blockIdx.x;
+  if (w >= *A.woff_total) return;
+  const Work wk = A.work[w];
+  const uint32_t c = wk.list;
+  const uint32_t e0 = A.off[c] + wk.first;
+  const uint32_t ne = min(static_cast<uint32_t>(kQG), A.off[c + 1] - e0);
+  const uint32_t r0 = A.list_off[c], nrows = A.list_off[c + 1] - r0;
+  const uint32_t dims = A.dims, qw = dims / 4 + 1;
+  const uint32_t kch = min(dims, kChunk), rw = kch / 4 + 1;
+  constexpr int kPlanes = kFull ? 2 : 1;
+  const uint32_t S = A.S;
+
+  uint32_t *sq = reinterpret_cast<uint32_t *>(smem);   // [planes][kQG][qw]
+  uint32_t *sr = sq + kPlanes * kQG * qw;              // [planes][kRT][rw]
+  uint32_t *sids = sr + kPlanes * kRT * rw;            // [kRT]
+  uint32_t *ccount = sids + kRT;                       // [kQG]
+  uint32_t *bcount = ccount + kQG;                     // [kQG]
+  uint32_t *sslot = bcount + kQG;                      // [kQG]
+  size_t off = (reinterpret_cast<unsigned char *>(sslot + kQG) - smem + 15) / 16 * 16;
+  int64_t *sqn = reinterpret_cast<int64_t *>(smem + off);                      // [kQG]
+  unsigned long long *bkid = reinterpret_cast<unsigned long long *>(sqn + kQG);  // [kQG][S]
+  unsigned long long *ckid = bkid + (kSelect ? kQG * S : 0);                   // [kQG][kRT]
+  uint32_t *brow = reinterpret_cast<uint32_t *>(ckid + (kSelect ? kQG * kRT : 0));  // [kQG][S]
+  uint32_t *crow = brow + (kSelect ? kQG * S : 0);                             // [kQG][kRT]
+
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const int j = t & 15, rr = t >> 4;
+  if (t < kQG) {
+    ccount[t] = 0;
+    bcount[t] = 0;
+    sslot[t] = t < static_cast<int>(ne) ? A.entries[e0 + t] : 0;
+  }
+  __syncthreads();
+  if (t < static_cast<int>(ne)) sqn[t] = A.qnorm[sslot[t] / A.nprobe];
+  // Stage the queries' bytes (16-byte loads; dims is a multiple of 64).
+  const uint32_t v16 = dims / 16;
+  for (uint32_t idx = t; idx < ne * v16 * kPlanes; idx += kThreads) {
+    const uint32_t pl = idx / (ne * v16), rem = idx % (ne * v16);
+    const uint32_t jj = rem / v16, v = rem % v16;
+    const uint32_t q = sslot[jj] / A.nprobe;
+    const uint8_t *src = (pl == 0 ? A.qhi : A.qlo) + static_cast<size_t>(q) * A.dc + v * 16;
+    const uint4 x = *reinterpret_cast<const uint4 *>(src);
+    uint32_t *dst = sq + (pl * kQG + jj) * qw + v * 4;
+    dst[0] = x.x; dst[1] = x.y; dst[2] = x.z; dst[3] = x.w;
+  }
+  // Slots of rows past the list end are padding (store-all mode writes every row).
+  if (!kSelect) {
+    for (uint32_t idx = t; idx < ne * (A.SC - min(nrows, A.SC)); idx += kThreads) {
+      const uint32_t jj = idx / (A.SC - nrows), pos = nrows + idx % (A.SC - nrows);
+      A.slots[static_cast<size_t>(sslot[jj]) * A.SC + pos] = make_uint2(kEmpty, 0);
+    }
+  }
+  __syncthreads();
+
+  for (uint32_t rt = 0; rt < nrows; rt += kRT) {
+    const uint32_t nr = min(static_cast<uint32_t>(kRT), nrows - rt);
+    uint32_t hh = 0, mx = 0, ll = 0;
+    for (uint32_t k0 = 0; k0 < dims; k0 += kch) {
+      const uint32_t kc = min(kch, dims - k0), c16 = kc / 16;
+      __syncthreads();
+      for (uint32_t idx = t; idx < nr * c16 * kPlanes; idx += kThreads) {
+        const uint32_t pl = idx / (nr * c16), rem = idx % (nr * c16);
+        const uint32_t i = rem / c16, v = rem % c16;
+        const uint8_t *src =
+            (pl == 0 ? A.xhi : A.xlo) + static_cast<size_t>(r0 + rt + i) * A.dc + k0 + v * 16;
+        const uint4 x = *reinterpret_cast<const uint4 *>(src);
+        uint32_t *dst = sr + (pl * kRT + i) * rw + v * 4;
+        dst[0] = x.x; dst[1] = x.y; dst[2] = x.z; dst[3] = x.w;
+      }
+      if (k0 == 0 && t < static_cast<int>(nr)) sids[t] = A.ids[r0 + rt + t];
+      __syncthreads();
+      if (j < static_cast<int>(ne) && rr < static_cast<int>(nr)) {
+        const uint32_t *qa = sq + j * qw + k0 / 4;
+        const uint32_t *xa = sr + rr * rw;
+        const uint32_t nw = kc / 4;
+        if (kFull) {
+          const uint32_t *qb = sq + (kQG + j) * qw + k0 / 4;
+          const uint32_t *xb = sr + (kRT + rr) * rw;
+#pragma unroll 8
+          for (uint32_t u = 0; u < nw; ++u) {
+            const uint32_t ah = qa[u], al = qb[u], bh = xa[u], bl = xb[u];
+            hh = dp4(ah, bh, hh);
+            mx = dp4(ah, bl, mx);
+            mx = dp4(al, bh, mx);
+            ll = dp4(al, bl, ll);
+          }
+        } else {
+#pragma unroll 8
+          for (uint32_t u = 0; u < nw; ++u) hh = dp4(qa[u], xa[u], hh);
+        }
+      }
+    }
+    // The candidate of (row rr, query j).
+    if (j < static_cast<int>(ne) && rr < static_cast<int>(nr)) {
+      const uint32_t row = r0 + rt + rr;
+      const int64_t dot = kFull ? static_cast<int64_t>((static_cast<uint64_t>(hh) << 16) +
+                                                       (static_cast<uint64_t>(mx) << 8) + ll)
+                                : static_cast<int64_t>(hh);
+      const float dist = dist_value(sqn[j] + A.xnorm[row] - 2 * dot, A.scale);
+      const uint32_t key = __float_as_uint(dist);
+      if (kSelect) {
+        const unsigned long long kid = (static_cast<unsigned long long>(key) << 32) | sids[rr];
+        const unsigned long long thr = bcount[j] == S ? bkid[j * S + S - 1] : ~0ull;
+        if (kid < thr) {
+          const uint32_t pos = atomicAdd(&ccount[j], 1u);
+          ckid[j * kRT + pos] = kid;
+          crow[j * kRT + pos] = row;
+        }
+      } else {
+        A.slots[static_cast<size_t>(sslot[j]) * A.SC + rt + rr] = make_uint2(key, row);
+      }
+    }
+    if (kSelect) {
+      __syncthreads();
+      // Merge each query's new candidates (at most kRT, unsorted) into its
+      // sorted best list: one warp per query.
+      for (int jj = warp; jj < static_cast<int>(ne); jj += kThreads / 32) {
+        const uint32_t nc = ccount[jj];
+        if (nc == 0) continue;
+        const uint32_t nb = bcount[jj];
+        unsigned long long *B = bkid + jj * S;
+        uint32_t *Br = brow + jj * S;
+        const unsigned long long ck = lane < static_cast<int>(nc) ? ckid[jj * kRT + lane] : ~0ull;
+        const uint32_t cr = lane < static_cast<int>(nc) ? crow[jj * kRT + lane] : 0;
+        // rank of this candidate among the candidates (ties by lane)
+        uint32_t crank = 0;
+        for (uint32_t i = 0; i < nc; ++i) {
+          const unsigned long long o = __shfl_sync(0xffffffffu, ck, i);
+          crank += (o < ck) || (o == ck && static_cast<int>(i) < lane);
+        }
+        // number of best entries <= candidate (upper bound)
+        uint32_t lo = 0, hi = nb;
+        while (lo < hi) {
+          const uint32_t mid = (lo + hi) >> 1;
+          if (B[mid] <= ck) lo = mid + 1;
+          else hi = mid;
+        }
+        const uint32_t cpos = lo + crank;
+        // new index of each old entry
+        constexpr int kPer = kSelMax / 32;
+        unsigned long long okid[kPer];
+        uint32_t orow[kPer], onew[kPer];
+#pragma unroll
+        for (int u = 0; u < kPer; ++u) {
+          const uint32_t b = lane + 32 * u;
+          okid[u] = b < nb ? B[b] : ~0ull;
+          orow[u] = b < nb ? Br[b] : 0;
+          onew[u] = b < nb ? b : 0xFFFFFFFFu;
+        }
+        for (uint32_t i = 0; i < nc; ++i) {
+          const unsigned long long o = __shfl_sync(0xffffffffu, ck, i);
+#pragma unroll
+          for (int u = 0; u < kPer; ++u) onew[u] += (onew[u] != 0xFFFFFFFFu && o < okid[u]);
+        }
+        __syncwarp();
+#pragma unroll
+        for (int u = 0; u < kPer; ++u)
+          if (onew[u] < S) {
+            B[onew[u]] = okid[u];
+            Br[onew[u]] = orow[u];
+          }
+        if (lane < static_cast<int>(nc) && cpos < S) {
+          B[cpos] = ck;
+          Br[cpos] = cr;
+        }
+        __syncwarp();
+        if (lane == 0) {
+          bcount[jj] = min(S, nb + nc);
+          ccount[jj] = 0;
+        }
+      }
+      __syncthreads();
+    }
+  }
+  if (kSelect) {
+    for (uint32_t idx = t; idx < ne * S; idx += kThreads) {
+      const uint32_t jj = idx / S, i = idx % S;
+      uint2 v = make_uint2(kEmpty, 0);
+      if (i < bcount[jj]) v = make_uint2(static_cast<uint32_t>(bkid[jj * S + i] >> 32), brow[jj * S + i]);
+      A.slots[static_cast<size_t>(sslot[jj]) * A.SC + i] = v;
+    }
+  }
+}
+
+// ---------------------------------------------------- block selection helper
+// Chooses the `p` smallest of n entries by (key, id), where entry i gives
+// key = K(i) and id = I(i); keys == kEmpty are never chosen. Writes the chosen
+// (key << 32 | id, position) pairs into sel/pos (unsorted) and returns how
+// many were chosen (min(p, non-empty)). Radix selection over 8-bit digits,
+// first of the key, then of the id among the entries tied at the boundary key.
+template <class KeyF, class IdF>
+__device__ uint32_t block_select(uint32_t n, uint32_t p, KeyF K, IdF I, unsigned long long *sel,
+                                 uint32_t *pos, uint32_t *hist, uint32_t *scratch,
+                                 bool *boundary_tie) {
+  const uint32_t tid = threadIdx.x, nt = blockDim.x;
+  // count non-empty
+  if (tid == 0) scratch[0] = 0;
+  __syncthreads();
+  {
+    uint32_t m = 0;
+    for (uint32_t i = tid; i < n; i += nt) m += K(i) != kEmpty;
+    atomicAdd(&scratch[0], m);
+  }
+  __syncthreads();
+  const uint32_t valid = scratch[0];
+  __syncthreads();
+  const uint32_t want = min(p, valid);
+  *boundary_tie = false;
+  if (want == 0) return 0;
+  uint32_t T = kEmpty, idmax = 0xFFFFFFFFu;
+  if (want < valid) {
+    // radix select of the want-th key
+    uint32_t prefix = 0, rank = want - 1;
+    for (int shift = 24; shift >= 0; shift -= 8) {
+      for (uint32_t i = tid; i < 256; i += nt) hist[i] = 0;
+      __syncthreads();
+      const uint32_t hm = shift == 24 ? 0u : (0xFFFFFFFFu << (shift + 8));
+      for (uint32_t i = tid; i < n; i += nt) {
+        const uint32_t k = K(i);
+        if (k != kEmpty && (k & hm) == prefix) atomicAdd(&hist[(k >> shift) & 0xFFu], 1u);
+      }
+      __syncthreads();
+      if (tid == 0) {
+        uint32_t acc = 0, b = 0;
+        for (; b < 256; ++b) {
+          if (rank < acc + hist[b]) break;
+          acc += hist[b];
+        }
+        scratch[1] = b;
+        scratch[2] = acc;
+      }
+      __syncthreads();
+      rank -= scratch[2];
+      prefix |= scratch[1] << shift;
+      __syncthreads();
+    }
+    T = prefix;
+    const uint32_t need = rank + 1;
+    if (tid == 0) scratch[3] = 0;
+    __syncthreads();
+    {
+      uint32_t m = 0;
+      for (uint32_t i = tid; i < n; i += nt) m += K(i) == T;
+      atomicAdd(&scratch[3], m);
+    }
+    __syncthreads();
+    const uint32_t neq = scratch[3];
+    *boundary_tie = neq > need;
+    if (neq > need) {
+      uint32_t ip = 0, ir = need - 1;
+      for (int shift = 24; shift >= 0; shift -= 8) {
+        for (uint32_t i = tid; i < 256; i += nt) hist[i] = 0;
+        __syncthreads();
+        const uint32_t hm = shift == 24 ? 0u : (0xFFFFFFFFu << (shift + 8));
+        for (uint32_t i = tid; i < n; i += nt) {
+          if (K(i) != T) continue;
+          const uint32_t id = I(i);
+          if ((id & hm) == ip) atomicAdd(&hist[(id >> shift) & 0xFFu], 1u);
+        }
+        __syncthreads();
+        if (tid == 0) {
+          uint32_t acc = 0, b = 0;
+          for (; b < 256; ++b) {
+            if (ir < acc + hist[b]) break;
+            acc += hist[b];
+          }
+          scratch[1] = b;
+          scratch[2] = acc;
+        }
+        __syncthreads();
+        ir -= scratch[2];
+        ip |= scratch[1] << shift;
+        __syncthreads();
+      }
+      idmax = ip;
+    }
+  }
+  if (tid == 0) scratch[4] = 0;
+  __syncthreads();
+  for (uint32_t i = tid; i < n; i += nt) {
+    const uint32_t k = K(i);
+    if (k == kEmpty) continue;
+    bool take = k < T;
+    uint32_t id = 0;
+    if (!take && k == T) {
+      id = I(i);
+      take = id <= idmax;
+    } else if (take) {
+      id = I(i);
+    }
+    if (take) {
+      const uint32_t at = atomicAdd(&scratch[4], 1u);
+      if (at < want) {
+        sel[at] = (static_cast<unsigned long long>(k) << 32) | id;
+        pos[at] = i;
+      }
+    }
+  }
+  __syncthreads();
+  return want;
+}
+
+// In-shared-memory bitonic sort of n (key, payload) pairs, ascending by key.
+__device__ void block_sort_pairs(unsigned long long *key, uint32_t *val, uint32_t n) {
+  uint32_t np2 = 1;
+  while (np2 < n) np2 <<= 1;
+  for (uint32_t i = n + threadIdx.x; i < np2; i += blockDim.x) {
+    key[i] = ~0ull;
+    val[i] = 0;
+  }
+  __syncthreads();
+  for (uint32_t size = 2; size <= np2; size <<= 1)
+    for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+      for (uint32_t i = threadIdx.x; i < np2; i += blockDim.x) {
+        const uint32_t jx = i ^ stride;
+        if (jx > i) {
+          const bool up = (i & size) == 0;
+          const unsigned long long a = key[i], b = key[jx];
+          if ((a > b) == up) {
+            key[i] = b;
+            key[jx] = a;
+            const uint32_t tv = val[i];
+            val[i] = val[jx];
+            val[jx] = tv;
+          }
+        }
+      }
+      __syncthreads();
+    }
+}
+
+// -------------------------------------------------------------------- merge
+// Per query: the best S of its nprobe * SC slot entries by (distance, id).
+// Ranked modes write the survivors in descending (distance, id) order - the
+// order in which the reference pops its merged heap into the refinement
+// (:1088-1112). The full mode writes the final top-k, ascending, padded.
+__global__ void __launch_bounds__(kThreads) merge_kernel(
+    const uint2 *__restrict__ slots, uint32_t per_query, const uint32_t *__restrict__ ids,
+    uint32_t S, bool final_topk, uint32_t k, uint2 *__restrict__ surv, uint32_t *__restrict__ nsurv,
+    uint32_t *__restrict__ out_ids, float *__restrict__ out_dists,
+    unsigned long long *__restrict__ tie_count) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ uint32_t hist[256], scratch[8];
+  __shared__ bool tie;
+  unsigned long long *sel = reinterpret_cast<unsigned long long *>(smem);
+  uint32_t np2 = 1;
+  while (np2 < S) np2 <<= 1;
+  uint32_t *pos = reinterpret_cast<uint32_t *>(sel + np2);
+  const uint32_t q = blockIdx.x;
+  const uint2 *e = slots + static_cast<size_t>(q) * per_query;
+  auto K = [&](uint32_t i) { return e[i].x; };
+  auto I = [&](uint32_t i) { return ids[e[i].y]; };
+  const uint32_t got = block_select(per_query, S, K, I, sel, pos, hist, scratch, &tie);
+  if (threadIdx.x == 0 && tie && tie_count) atomicAdd(tie_count, 1ull);
+  block_sort_pairs(sel, pos, got);
+  if (final_topk) {
+    for (uint32_t i = threadIdx.x; i < k; i += blockDim.x) {
+      uint32_t id = 0xFFFFFFFFu;
+      float dd = 3.402823466e+38f;
+      if (i < got) {
+        id = static_cast<uint32_t>(sel[i] & 0xFFFFFFFFu);
+        dd = __uint_as_float(static_cast<uint32_t>(sel[i] >> 32));
+      }
+      out_ids[static_cast<size_t>(q) * k + i] = id;
+      out_dists[static_cast<size_t>(q) * k + i] = dd;
+    }
+    return;
+  }
+  for (uint32_t i = threadIdx.x; i < got; i += blockDim.x) {
+    const uint32_t src = got - 1 - i;  // descending
+    surv[static_cast<size_t>(q) * S + i] = e[pos[src]];
+  }
+  if (threadIdx.x == 0) nsurv[q] = got;
+}
+
+// ------------------------------------------------------------------- refine
+// Per query: exact distances of the survivors (in the order given), then the
+// reference's top-k heap: the first k enter, later ones replace the largest
+// (distance, id) when their distance is strictly smaller (:1113-1124); output
+// ascending by (distance, id), padded (emit_topk, :384-398).
+__global__ void __launch_bounds__(kThreads) refine_kernel(
+    const uint8_t *__restrict__ qhi, const uint8_t *__restrict__ qlo,
+    const int64_t *__restrict__ qnorm, const uint8_t *__restrict__ xhi,
+    const uint8_t *__restrict__ xlo, const int64_t *__restrict__ xnorm,
+    const uint32_t *__restrict__ ids, uint32_t npts, uint32_t dc, const uint2 *__restrict__ surv,
+    const uint32_t *__restrict__ nsurv, uint32_t S, uint32_t k, DistScale scale,
+    uint32_t *__restrict__ out_ids, float *__restrict__ out_dists) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const uint32_t q = blockIdx.x, ns = nsurv[q];
+  uint32_t *sq = reinterpret_cast<uint32_t *>(smem);  // [2][dc/4]
+  float *ex = reinterpret_cast<float *>(sq + dc / 2);  // [S]
+  uint32_t *eid = reinterpret_cast<uint32_t *>(ex + S);  // [S]
+  float *hd = reinterpret_cast<float *>(eid + S);      // [k]
+  uint32_t *hid = reinterpret_cast<uint32_t *>(hd + k);  // [k]
+  const uint32_t nw = dc / 4;
+  for (uint32_t i = threadIdx.x; i < nw; i += blockDim.x) {
+    sq[i] = reinterpret_cast<const uint32_t *>(qhi + static_cast<size_t>(q) * dc)[i];
+    sq[nw + i] = reinterpret_cast<const uint32_t *>(qlo + static_cast<size_t>(q) * dc)[i];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t qn = qnorm[q];
+  for (uint32_t s = warp; s < ns; s += blockDim.x / 32) {
+    const uint2 v = surv[static_cast<size_t>(q) * S + s];
+    const uint32_t row = v.y, id = ids[row];
+    const uint32_t *xh = reinterpret_cast<const uint32_t *>(xhi + static_cast<size_t>(row) * dc);
+    const uint32_t *xl = reinterpret_cast<const uint32_t *>(xlo + static_cast<size_t>(row) * dc);
+    uint32_t hh = 0, mx = 0, ll = 0;
+    for (uint32_t u = lane; u < nw; u += 32) {
+      const uint32_t ah = sq[u], al = sq[nw + u], bh = xh[u], bl = xl[u];
+      hh = dp4(ah, bh, hh);
+      mx = dp4(ah, bl, mx);
+      mx = dp4(al, bh, mx);
+      ll = dp4(al, bl, ll);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      hh += __shfl_xor_sync(0xffffffffu, hh, o);
+      mx += __shfl_xor_sync(0xffffffffu, mx, o);
+      ll += __shfl_xor_sync(0xffffffffu, ll, o);
+    }
+    if (lane == 0) {
+      const int64_t dot = static_cast<int64_t>((static_cast<uint64_t>(hh) << 16) +
+                                               (static_cast<uint64_t>(mx) << 8) + ll);
+      ex[s] = dist_value(qn + xnorm[row] - 2 * dot, scale);
+      eid[s] = id;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t n = 0;
+    for (uint32_t s = 0; s < ns; ++s) {
+      const float dd = ex[s];
+      const uint32_t id = eid[s];
+      if (id >= npts) continue;  // ids without a row are skipped (:1091-1094)
+      if (n < k) {
+        hd[n] = dd;
+        hid[n] = id;
+        ++n;
+        continue;
+      }
+      uint32_t mi = 0;  // the largest (distance, id)
+      for (uint32_t i = 1; i < n; ++i)
+        if (hd[i] > hd[mi] || (hd[i] == hd[mi] && hid[i] > hid[mi])) mi = i;
+      if (dd < hd[mi]) {
+        hd[mi] = dd;
+        hid[mi] = id;
+      }
+    }
+    // ascending by (distance, id)
+    for (uint32_t i = 1; i < n; ++i) {
+      const float d0 = hd[i];
+      const uint32_t i0 = hid[i];
+      uint32_t m = i;
+      while (m > 0 && (hd[m - 1] > d0 || (hd[m - 1] == d0 && hid[m - 1] > i0))) {
+        hd[m] = hd[m - 1];
+        hid[m] = hid[m - 1];
+        --m;
+      }
+      hd[m] = d0;
+      hid[m] = i0;
+    }
+    for (uint32_t i = 0; i < k; ++i) {
+      out_ids[static_cast<size_t>(q) * k + i] = i < n ? hid[i] : 0xFFFFFFFFu;
+      out_dists[static_cast<size_t>(q) * k + i] = i < n ? hd[i] : 3.402823466e+38f;
+    }
+  }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------ orchestration
+int rotate_rows(const float *in, uint32_t nrows, uint32_t d, const float *rot, float *out,
+                cudaStream_t st);
+int quantize_rows(const float *x, uint32_t nrows, uint32_t d, uint32_t dc, float lo,
+                  double inv_step, uint32_t head, uint8_t *hi, uint8_t *lop, int64_t *norm,
+                  int64_t *hinorm, int64_t *headnorm, cudaStream_t st);
+int sq16_tiles(const uint8_t *qhi, const uint8_t *qlo, const uint8_t *xhi, const uint8_t *xlo,
+               const int64_t *qn, const int64_t *xn, double step_sq, uint32_t m, uint32_t n,
+               uint32_t dims, uint32_t qstride, uint32_t xstride, float *out, bool full,
+               cudaStream_t st);
+int select_topp(const float *dists, uint32_t nq, uint32_t n, uint32_t p, uint32_t *probed,
+                unsigned long long *tie_count, cudaStream_t st);
+
+struct Plan {
+  uint32_t B, k, p, S, SC, dims;
+  int ranking;
+  bool select;
+  size_t off_fq, off_qhi, off_qlo, off_qn, off_qhn, off_qh0, off_cd, off_probed, off_cnt, off_off,
+      off_woff, off_cur, off_work, off_ent, off_slots, off_surv, off_nsurv, off_stats, total;
+};
+
+static size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+
+int make_plan(const katoann_gpu_index *ix, uint32_t B, uint32_t k, uint32_t p, int ranking,
+              uint32_t survivors, Plan *P) {
+  if (k == 0 || p == 0 || p > ix->nlist) return invalid("need k >= 1 and 1 <= nprobe <= nlist");
+  if (ranking == KATO_RANK_PREFIX && ix->head_dims == 0)
+    return invalid("prefix ranking needs the rotation file (.dimc)");
+  if (ranking < 0 || ranking > 2) return invalid("unknown ranking");
+  Plan &pl = *P;
+  pl.B = B;
+  pl.k = k;
+  pl.p = p;
+  pl.ranking = ranking;
+  pl.S = ranking == KATO_RANK_FULL ? k : std::max(survivors, k);
+  if (pl.S > kSortMax) return invalid("survivors (or k) above 4096 are not supported on the GPU");
+  const uint32_t ml = std::max(ix->max_list, 1u);
+  pl.SC = std::min(pl.S, ml);
+  pl.select = pl.SC <= kSelMax;
+  if (!pl.select) pl.SC = ml;
+  pl.dims = ranking == KATO_RANK_PREFIX ? ix->head_dims : ix->dc;
+  const uint32_t L = ix->nlist;
+  const size_t bp = static_cast<size_t>(B) * p;
+  const size_t wmax = std::min<size_t>(L, bp) + bp / kQG + 1;
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    const size_t at = o;
+    o += align256(bytes);
+    return at;
+  };
+  pl.off_stats = take(8 * sizeof(unsigned long long));
+  pl.off_fq = take(static_cast<size_t>(B) * ix->dim * 4);
+  pl.off_qhi = take(static_cast<size_t>(B) * ix->dc);
+  pl.off_qlo = take(static_cast<size_t>(B) * ix->dc);
+  pl.off_qn = take(static_cast<size_t>(B) * 8);
+  pl.off_qhn = take(static_cast<size_t>(B) * 8);
+  pl.off_qh0 = take(static_cast<size_t>(B) * 8);
+  pl.off_cd = take(static_cast<size_t>(B) * L * 4);
+  pl.off_probed = take(bp * 4);
+  pl.off_cnt = take(static_cast<size_t>(L) * 4);
+  pl.off_off = take((static_cast<size_t>(L) + 1) * 4);
+  pl.off_woff = take((static_cast<size_t>(L) + 1) * 4);
+  pl.off_cur = take(static_cast<size_t>(L) * 4);
+  pl.off_work = take(wmax * sizeof(Work));
+  pl.off_ent = take(bp * 4);
+  pl.off_slots = take(bp * pl.SC * sizeof(uint2));
+  pl.off_surv = take(static_cast<size_t>(B) * pl.S * sizeof(uint2));
+  pl.off_nsurv = take(static_cast<size_t>(B) * 4);
+  pl.total = o;
+  return KATO_OK;
+}
+
+int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *queries, uint32_t nq,
+                unsigned char *ws, uint32_t *out_ids, float *out_dists, cudaStream_t st) {
+  int rc;
+  const uint32_t L = ix->nlist, p = pl.p, dc = ix->dc;
+  float *fq = reinterpret_cast<float *>(ws + pl.off_fq);
+  uint8_t *qhi = ws + pl.off_qhi, *qlo = ws + pl.off_qlo;
+  int64_t *qn = reinterpret_cast<int64_t *>(ws + pl.off_qn);
+  int64_t *qhn = reinterpret_cast<int64_t *>(ws + pl.off_qhn);
+  int64_t *qh0 = reinterpret_cast<int64_t *>(ws + pl.off_qh0);
+  float *cd = reinterpret_cast<float *>(ws + pl.off_cd);
+  uint32_t *probed = reinterpret_cast<uint32_t *>(ws + pl.off_probed);
+  uint32_t *cnt = reinterpret_cast<uint32_t *>(ws + pl.off_cnt);
+  uint32_t *off = reinterpret_cast<uint32_t *>(ws + pl.off_off);
+  uint32_t *woff = reinterpret_cast<uint32_t *>(ws + pl.off_woff);
+  uint32_t *cur = reinterpret_cast<uint32_t *>(ws + pl.off_cur);
+  Work *work = reinterpret_cast<Work *>(ws + pl.off_work);
+  uint32_t *ent = reinterpret_cast<uint32_t *>(ws + pl.off_ent);
+  uint2 *slots = reinterpret_cast<uint2 *>(ws + pl.off_slots);
+  uint2 *surv = reinterpret_cast<uint2 *>(ws + pl.off_surv);
+  uint32_t *nsurv = reinterpret_cast<uint32_t *>(ws + pl.off_nsurv);
+  unsigned long long *stats = reinterpret_cast<unsigned long long *>(ws + pl.off_stats);
+
+  // 1. rotation and quantization of the queries (src/index.cpp:895-899, :917-943)
+  const float *src = queries;
+  if (ix->rotated) {
+    if ((rc = rotate_rows(queries, nq, ix->dim, ix->d_rotation, fq, st))) return rc;
+    src = fq;
+  }
+  if ((rc = quantize_rows(src, nq, ix->dim, dc, ix->lo, ix->inv_step, ix->head_dims, qhi, qlo, qn,
+                          qhn, qh0, st)))
+    return rc;
+  // 2. coarse product and top-nprobe (:846-877)
+  if ((rc = sq16_tiles(qhi, qlo, ix->d_chi, ix->d_clo, qn, ix->d_cnorm, ix->step_sq, nq, L, dc, dc,
+                       dc, cd, true, st)))
+    return rc;
+  if ((rc = select_topp(cd, nq, L, p, probed, stats + 0, st))) return rc;
+  // 3. inversion (:403-412)
+  const uint32_t total = nq * p;
+  KATO_CUDA(cudaMemsetAsync(cnt, 0, static_cast<size_t>(L) * 4, st));
+  count_kernel<<<div_up(total, 256), 256, 0, st>>>(probed, total, cnt);
+  scan_kernel<<<1, 1024, 0, st>>>(cnt, L, off, woff, cur);
+  scatter_kernel<<<div_up(total, 256), 256, 0, st>>>(probed, total, off, cur, ent);
+  work_kernel<<<div_up(L, 256), 256, 0, st>>>(cnt, woff, L, work);
+  KATO_LAUNCHED("inversion kernels");
+  // 4. ranking pass (:998-1044 / :1167-1204)
+  const bool full = pl.ranking == KATO_RANK_FULL;
+  RankArgs A{};
+  A.xhi = ix->d_hi;
+  A.xlo = ix->d_lo;
+  A.xnorm = full ? ix->d_norm : (pl.ranking == KATO_RANK_PREFIX ? ix->d_headnorm : ix->d_hinorm);
+  A.ids = ix->d_ids;
+  A.list_off = ix->d_list_off;
+  A.qhi = qhi;
+  A.qlo = qlo;
+  A.qnorm = full ? qn : (pl.ranking == KATO_RANK_PREFIX ? qh0 : qhn);
+  A.work = work;
+  A.woff_total = woff + L;
+  A.off = off;
+  A.entries = ent;
+  A.dc = dc;
+  A.dims = pl.dims;
+  A.nprobe = p;
+  A.S = pl.SC;  // a slot never holds more than min(S, largest list) candidates
+  A.SC = pl.SC;
+  A.slots = slots;
+  A.scale = make_dist_scale(ix->step_sq);
+  const size_t bp = static_cast<size_t>(nq) * p;
+  const uint32_t grid = static_cast<uint32_t>(std::min<size_t>(L, bp) + bp / kQG + 1);
+  const size_t smem = rank_smem_bytes(full ? 2 : 1, pl.select, pl.dims, pl.SC);
+  if (smem > 227 * 1024) return invalid("ranking tile does not fit in shared memory");
+  auto launch = [&](auto kern) -> int {
+    KATO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(smem)));
+    kern<<<grid, kThreads, smem, st>>>(A);
+    KATO_LAUNCHED("rank_kernel");
+    return KATO_OK;
+  };
+  if (full) rc = pl.select ? launch(rank_kernel<true, true>) : launch(rank_kernel<true, false>);
+  else rc = pl.select ? launch(rank_kernel<false, true>) : launch(rank_kernel<false, false>);
+  if (rc) return rc;
+  // 5. per-query merge of the slot lists (:1058-1080 / :1205-1218)
+  uint32_t np2 = 1;
+  while (np2 < pl.S) np2 <<= 1;
+  const size_t msmem = static_cast<size_t>(np2) * 12;
+  KATO_CUDA(cudaFuncSetAttribute(merge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(msmem)));
+  merge_kernel<<<nq, kThreads, msmem, st>>>(slots, p * pl.SC, ix->d_ids, pl.S, full, pl.k, surv,
+                                            nsurv, out_ids, out_dists, stats + 1);
+  KATO_LAUNCHED("merge_kernel");
+  if (full) return KATO_OK;
+  // 6. exact refinement and top-k (:1081-1125)
+  const size_t rsmem = static_cast<size_t>(dc) * 2 + static_cast<size_t>(pl.S) * 8 +
+                       static_cast<size_t>(pl.k) * 8;
+  KATO_CUDA(cudaFuncSetAttribute(refine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(rsmem)));
+  refine_kernel<<<nq, kThreads, rsmem, st>>>(qhi, qlo, qn, ix->d_hi, ix->d_lo, ix->d_norm,
+                                             ix->d_ids, ix->npts, dc, surv, nsurv, pl.S, pl.k,
+                                             make_dist_scale(ix->step_sq), out_ids, out_dists);
+  KATO_LAUNCHED("refine_kernel");
+  return KATO_OK;
+}
+
+int search(const katoann_gpu_index *ix, const float *queries, uint32_t nq, uint32_t k, uint32_t p,
+           int ranking, uint32_t survivors, uint32_t max_batch, void *ws, size_t ws_bytes,
+           uint32_t *out_ids, float *out_dists, cudaStream_t st) {
+  if (nq == 0) return KATO_OK;
+  if (max_batch == 0) return invalid("max_batch must be positive");
+  Plan pl{};
+  int rc = make_plan(ix, std::min(nq, max_batch), k, p, ranking, survivors, &pl);
+  if (rc) return rc;
+  if (ws_bytes < pl.total) {
+    set_error("search workspace too small");
+    return KATO_ENOMEM;
+  }
+  unsigned char *w = static_cast<unsigned char *>(ws);
+  KATO_CUDA(cudaMemsetAsync(w + pl.off_stats, 0, 8 * sizeof(unsigned long long), st));
+  for (uint32_t q0 = 0; q0 < nq; q0 += max_batch) {
+    const uint32_t b = std::min(max_batch, nq - q0);
+    if ((rc = search_pass(ix, pl, queries + static_cast<size_t>(q0) * ix->dim, b, w,
+                          out_ids + static_cast<size_t>(q0) * k,
+                          out_dists + static_cast<size_t>(q0) * k, st)))
+      return rc;
+  }
+  return KATO_OK;
+}
+
+size_t search_workspace(const katoann_gpu_index *ix, uint32_t max_batch, uint32_t k, uint32_t p,
+                        int ranking, uint32_t survivors) {
+  Plan pl{};
+  if (make_plan(ix, max_batch, k, p, ranking, survivors, &pl)) return 0;
+  return pl.total;
+}
+
+
+}  // namespace kato

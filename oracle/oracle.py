@@ -9,11 +9,12 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import platform
 
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "liboracle.so")
+LIB_PATH = os.path.join(HERE, f"liboracle-{platform.machine()}.so")
 RANKING = {"full": 0, "high": 1, "prefix": 2}
 
 _lib = None

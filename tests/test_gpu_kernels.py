@@ -1,0 +1,137 @@
+"""Kernel-level checks through the C ABI of libkatoann_gpu.so: the exact
+SQ16 distance kernels on the reference's own test grid
+(tests/test_kernels.cpp:151-154), the float rotation in the reference's
+arithmetic, the 16-bit coding of the lists and centroids, and the coarse
+probes, each against the oracle."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle
+from _gpu import check, dptr, gpu, to_host, view_of
+from _util import FIXTURES, fixture
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch
+    assert torch.cuda.is_available()
+    return torch
+
+
+def _draw(rng, shape):
+    c = rng.integers(0, 4, shape)
+    return np.where(c == 0, 0, np.where(c == 1, 255, rng.integers(0, 256, shape))).astype(np.uint8)
+
+
+def test_sq16_kernels_on_reference_grid(torch):
+    rng = np.random.default_rng(7)
+    step_sq = 1.0 / (65535.0 * 65535.0)
+    keep = []
+
+    def dev(a):  # device copy kept alive until the kernel has run
+        t = torch.from_numpy(np.ascontiguousarray(a)).cuda()
+        keep.append(t)
+        return t
+
+    for dc in (64, 128, 1024, 3072):
+        for m in (1, 5, 16, 70):
+            for n in (1, 15, 16, 17, 70, 256):
+                qh, ql, xh, xl = _draw(rng, (m, dc)), _draw(rng, (m, dc)), _draw(rng, (n, dc)), _draw(rng, (n, dc))
+                code = lambda h, l: h.astype(np.int64) * 256 + l
+                qn = (code(qh, ql) ** 2).sum(1)
+                xn = (code(xh, xl) ** 2).sum(1)
+                out = torch.empty((m, n), dtype=torch.float32, device="cuda")
+                check(gpu().katoann_gpu_sq16_l2(dptr(dev(qh)), dptr(dev(ql)), dptr(dev(xh)), dptr(dev(xl)),
+                                               dptr(dev(qn)), dptr(dev(xn)), step_sq, m, n, dc, dptr(out), None))
+                want = oracle.sq16_l2(qh, ql, xh, xl, qn, xn, step_sq)
+                assert np.array_equal(out.cpu().numpy(), want), ("full", dc, m, n)
+                # high bytes, and the leading pd dims of the dc-wide rows in place
+                pds = [dc] + [pd for pd in (64, 128, 256, 512, 1024) if pd < dc]
+                for pd in pds:
+                    qp = np.ascontiguousarray(qh[:, :pd])
+                    qpn = (qp.astype(np.int64) ** 2).sum(1)
+                    xpn = (xh[:, :pd].astype(np.int64) ** 2).sum(1)
+                    out = torch.empty((m, n), dtype=torch.float32, device="cuda")
+                    check(gpu().katoann_gpu_sq16_high_l2(dptr(dev(qp)), dptr(dev(xh)), dptr(dev(qpn)),
+                                                        dptr(dev(xpn)), step_sq, m, n, pd, dc, dptr(out), None))
+                    want = oracle.sq16_high_l2(qp, xh, qpn, xpn, step_sq, dims=pd)
+                    assert np.array_equal(out.cpu().numpy(), want), ("high", dc, m, n, pd)
+                keep.clear()
+
+
+def test_dist_values_on_device(torch):
+    rng = np.random.default_rng(3)
+    for step_sq in (1.76061467e-08, 2.98203776e-09, 1.0 / 65535.0 ** 2):
+        l2 = rng.integers(0, 1 << 45, 1 << 20, dtype=np.int64)
+        l2[:64] = np.arange(64)
+        d = torch.from_numpy(l2).cuda()
+        out = torch.empty(len(l2), dtype=torch.float32, device="cuda")
+        check(gpu().katoann_gpu_dist_values(dptr(d), len(l2), step_sq, dptr(out), None))
+        assert np.array_equal(out.cpu().numpy(), (l2.astype(np.float64) * step_sq).astype(np.float32))
+
+
+@pytest.mark.parametrize("d", [4, 5, 7, 9, 15, 16, 17, 19, 31, 33, 47, 63, 64, 65, 100, 102, 127,
+                               128, 129, 255, 1023, 1024])
+def test_rotation_matches_reference_arithmetic(torch, d):
+    rng = np.random.default_rng(d)
+    for nrows in (1, 3, 33, 100):
+        x = (rng.standard_normal((nrows, d)) * rng.uniform(0.01, 3.0, d)).astype(np.float32)
+        r = rng.standard_normal((d, d)).astype(np.float32) / np.float32(np.sqrt(d))
+        out = torch.empty((nrows, d), dtype=torch.float32, device="cuda")
+        xd, rd = torch.from_numpy(x).cuda(), torch.from_numpy(r).cuda()
+        check(gpu().katoann_gpu_rotate_rows(dptr(xd), nrows, d, dptr(rd), dptr(out), None))
+        assert np.array_equal(out.cpu().numpy(), oracle.rotate_with(x, r)), nrows
+
+
+@pytest.mark.parametrize("name", FIXTURES)
+def test_load_codes_match_oracle(name):
+    import katoann
+    spec, z, prefix, queries = fixture(name)
+    idx = katoann.Index()
+    idx.load(prefix)
+    v = view_of(idx)
+    ref = oracle.OracleIndex(prefix)
+    c = ref.codes()
+    n, dc = ref.npts, ref.dc
+    assert (v.npts, v.dc, v.head_dims) == (n, dc, ref.head_dims)
+    assert (float(v.lo), float(v.inv_step), float(v.step_sq)) == (np.float32(ref.lo), ref.inv_step, ref.step_sq)
+    assert np.array_equal(to_host(v.d_hi, n * dc, np.uint8).reshape(n, dc), c["hi"])
+    assert np.array_equal(to_host(v.d_lo, n * dc, np.uint8).reshape(n, dc), c["lo"])
+    assert np.array_equal(to_host(v.d_norm, n * 8, np.int64), c["norm"])
+    assert np.array_equal(to_host(v.d_hinorm, n * 8, np.int64), c["hinorm"])
+    if ref.head_dims:
+        assert np.array_equal(to_host(v.d_headnorm, n * 8, np.int64), c["headnorm"])
+    assert np.array_equal(to_host(v.d_ids, n * 4, np.uint32), c["ids"])
+    cc = ref.centroid_codes()
+    L = ref.nlist
+    assert np.array_equal(to_host(v.d_chi, L * dc, np.uint8).reshape(L, dc), cc["hi"])
+    assert np.array_equal(to_host(v.d_clo, L * dc, np.uint8).reshape(L, dc), cc["lo"])
+    assert np.array_equal(to_host(v.d_cnorm, L * 8, np.int64), cc["norm"])
+
+
+@pytest.mark.parametrize("name", ["d128", "d1024", "pca", "d100"])
+def test_coarse_probes_match_reference(torch, name):
+    import katoann
+    spec, z, prefix, queries = fixture(name)
+    idx = katoann.Index()
+    idx.load(prefix)
+    ref = oracle.OracleIndex(prefix)
+    q = ref.quantize(ref.rotate(queries))
+    nprobe = int(z["probed"].shape[1])
+    nq = len(queries)
+    qh, ql, qn = (torch.from_numpy(np.ascontiguousarray(q[k])).cuda() for k in ("hi", "lo", "norm"))
+    dists = torch.empty((nq, ref.nlist), dtype=torch.float32, device="cuda")
+    probed = torch.empty((nq, nprobe), dtype=torch.int32, device="cuda")
+    check(gpu().katoann_gpu_coarse(C.c_void_p(idx.device_view), dptr(qh), dptr(ql), dptr(qn), nq,
+                                   nprobe, dptr(dists), dptr(probed), None))
+    got = probed.cpu().numpy().astype(np.uint32)
+    assert np.array_equal(np.sort(got, 1), np.sort(z["probed"], 1))
+    # ascending by (distance, list)
+    d = dists.cpu().numpy()
+    rows = np.arange(nq)[:, None]
+    dd = d[rows, got]
+    assert np.all((dd[:, 1:] > dd[:, :-1]) | ((dd[:, 1:] == dd[:, :-1]) & (got[:, 1:] > got[:, :-1])))
