@@ -110,8 +110,10 @@ class Index {
 
   // The same with device pointers on `stream` (a cudaStream_t; nullptr = the
   // index's own stream). Returns without synchronising.
+  // `timer` (from katoann_gpu_timer_create, may be null) records the phase
+  // events of every device pass.
   void search_device(const float *d_queries, uint32_t nq, const SearchParams &p, uint32_t *d_ids,
-                     float *d_dists, void *stream = nullptr) const;
+                     float *d_dists, void *stream = nullptr, void *timer = nullptr) const;
 
   uint32_t dim() const;
   uint32_t nlist() const;

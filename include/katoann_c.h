@@ -49,10 +49,10 @@ int katoann_index_search(void *index, const float *queries, uint32_t nq, uint32_
                          uint32_t *ids, float *dists);
 
 /* The same on device memory and a caller stream (cudaStream_t, NULL = the
- * index's stream); asynchronous. */
+ * index's stream); asynchronous. timer: katoann_gpu_timer_create() or NULL. */
 int katoann_index_search_device(void *index, const float *d_queries, uint32_t nq, uint32_t k,
                                 uint32_t nprobe, int ranking, uint32_t survivors, int selection,
-                                uint32_t *d_ids, float *d_dists, void *stream);
+                                uint32_t *d_ids, float *d_dists, void *stream, void *timer);
 
 /* info[8] = {dim, nlist, size, prefix_dims, rotated, normalized, batched_coarse, engine=2} */
 int katoann_index_info(void *index, uint32_t *info);

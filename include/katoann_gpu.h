@@ -134,12 +134,34 @@ int katoann_gpu_search(const katoann_gpu_index *index, const float *d_queries, u
                        uint32_t max_batch, void *d_ws, size_t ws_bytes, uint32_t *d_ids,
                        float *d_dists, katoann_stream_t stream);
 
+/* Phase timer: CUDA events recorded on the search stream at the boundaries of
+ * the pipeline's phases, so the duration of every phase of every pass in a
+ * timed region is measured where it runs. Phases: 0 rotation+quantization of
+ * the queries, 1 coarse product, 2 top-nprobe selection, 3 inversion,
+ * 4 ranking pass, 5 survivor merge, 6 refinement. */
+#define KATO_PHASES 7
+void *katoann_gpu_timer_create(uint32_t max_passes);
+void katoann_gpu_timer_destroy(void *timer);
+/* Sums the phase durations (ms) of all passes recorded since the last read
+ * into h_ms[0..KATO_PHASES) and their count into *passes; synchronous. */
+int katoann_gpu_timer_read(void *timer, float *h_ms, uint32_t *passes);
+
+/* katoann_gpu_search that also records phase events into `timer` (may be
+ * NULL, then identical to katoann_gpu_search). */
+int katoann_gpu_search_timed(const katoann_gpu_index *index, const float *d_queries, uint32_t nq,
+                             uint32_t k, uint32_t nprobe, int ranking, uint32_t survivors,
+                             uint32_t max_batch, void *d_ws, size_t ws_bytes, uint32_t *d_ids,
+                             float *d_dists, katoann_stream_t stream, void *timer);
+
 /* Diagnostics that katoann_gpu_search left in its workspace, copied to the
  * host (synchronous on `stream`): [0] queries whose nprobe-th coarse distance
  * was tied with a list outside the probe set, [1] queries whose survivor
  * boundary (S-th ranking distance) was tied, [2] queries searched. */
 int katoann_gpu_workspace_stats(const void *d_ws, uint64_t *h_stats, uint32_t n,
                                 katoann_stream_t stream);
+
+/* Synchronous device-to-host copy of n bytes (exports the device index). */
+int katoann_gpu_copy_to_host(void *h_dst, const void *d_src, size_t n);
 
 /* float(double(l2) * step_sq) for n int64 values on the device (test hook of
  * the exact conversion every kernel uses). */

@@ -34,7 +34,10 @@ int select_topp(const float *dists, uint32_t nq, uint32_t n, uint32_t p, uint32_
 int dist_values(const int64_t *l2, uint32_t n, double step_sq, float *out, cudaStream_t st);
 int search(const katoann_gpu_index *ix, const float *queries, uint32_t nq, uint32_t k, uint32_t p,
            int ranking, uint32_t survivors, uint32_t max_batch, void *ws, size_t ws_bytes,
-           uint32_t *out_ids, float *out_dists, cudaStream_t st);
+           uint32_t *out_ids, float *out_dists, cudaStream_t st, void *timer);
+void *timer_create(uint32_t max_passes);
+void timer_destroy(void *t);
+int timer_read(void *t, float *ms, uint32_t *passes);
 size_t search_workspace(const katoann_gpu_index *ix, uint32_t max_batch, uint32_t k, uint32_t p,
                         int ranking, uint32_t survivors);
 
@@ -115,7 +118,29 @@ int katoann_gpu_search(const katoann_gpu_index *ix, const float *d_queries, uint
     return KATO_ELOGIC;
   }
   return kato::search(ix, d_queries, nq, k, nprobe, ranking, survivors, max_batch, d_ws, ws_bytes,
-                      d_ids, d_dists, as_stream(stream));
+                      d_ids, d_dists, as_stream(stream), nullptr);
+}
+
+int katoann_gpu_search_timed(const katoann_gpu_index *ix, const float *d_queries, uint32_t nq,
+                             uint32_t k, uint32_t nprobe, int ranking, uint32_t survivors,
+                             uint32_t max_batch, void *d_ws, size_t ws_bytes, uint32_t *d_ids,
+                             float *d_dists, katoann_stream_t stream, void *timer) {
+  if (!ix) return kato::invalid("null index");
+  if (ix->nlist == 0) {
+    kato::set_error("search before load");
+    return KATO_ELOGIC;
+  }
+  return kato::search(ix, d_queries, nq, k, nprobe, ranking, survivors, max_batch, d_ws, ws_bytes,
+                      d_ids, d_dists, as_stream(stream), timer);
+}
+
+void *katoann_gpu_timer_create(uint32_t max_passes) { return kato::timer_create(max_passes); }
+
+void katoann_gpu_timer_destroy(void *timer) { kato::timer_destroy(timer); }
+
+int katoann_gpu_timer_read(void *timer, float *h_ms, uint32_t *passes) {
+  if (!timer) return kato::invalid("null timer");
+  return kato::timer_read(timer, h_ms, passes);
 }
 
 int katoann_gpu_workspace_stats(const void *d_ws, uint64_t *h_stats, uint32_t n,
@@ -124,6 +149,11 @@ int katoann_gpu_workspace_stats(const void *d_ws, uint64_t *h_stats, uint32_t n,
   KATO_CUDA(cudaMemcpyAsync(h_stats, d_ws, n * sizeof(uint64_t), cudaMemcpyDeviceToHost,
                             as_stream(stream)));
   KATO_CUDA(cudaStreamSynchronize(as_stream(stream)));
+  return KATO_OK;
+}
+
+int katoann_gpu_copy_to_host(void *h_dst, const void *d_src, size_t n) {
+  KATO_CUDA(cudaMemcpy(h_dst, d_src, n, cudaMemcpyDeviceToHost));
   return KATO_OK;
 }
 

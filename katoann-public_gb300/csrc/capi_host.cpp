@@ -118,10 +118,10 @@ int katoann_index_search(void *index, const float *queries, uint32_t nq, uint32_
 
 int katoann_index_search_device(void *index, const float *d_queries, uint32_t nq, uint32_t k,
                                 uint32_t nprobe, int ranking, uint32_t survivors, int selection,
-                                uint32_t *d_ids, float *d_dists, void *stream) {
+                                uint32_t *d_ids, float *d_dists, void *stream, void *timer) {
   return guarded([&] {
     I(index)->search_device(d_queries, nq, params(k, nprobe, ranking, survivors, selection), d_ids,
-                            d_dists, stream);
+                            d_dists, stream, timer);
   });
 }
 

@@ -373,7 +373,7 @@ void Index::search(const float *queries, uint32_t nq, const SearchParams &p, uin
 }
 
 void Index::search_device(const float *d_queries, uint32_t nq, const SearchParams &p,
-                          uint32_t *d_ids, float *d_dists, void *stream) const {
+                          uint32_t *d_ids, float *d_dists, void *stream, void *timer) const {
   if (nq == 0) return;
   validate(s_.get(), s_ ? s_->nlist : 0, s_ ? s_->head : 0, p);
   State &s = *s_;
@@ -389,8 +389,9 @@ void Index::search_device(const float *d_queries, uint32_t nq, const SearchParam
   }
   if (s.last_stream && s.last_stream != st)
     cuda_check(cudaStreamWaitEvent(st, s.done, 0), "cudaStreamWaitEvent");
-  gpu_check(katoann_gpu_search(&s.view, d_queries, nq, p.k, p.nprobe, rk, p.survivors, s.max_batch,
-                               s.ws.p, s.ws.n, d_ids, d_dists, reinterpret_cast<katoann_stream_t>(st)));
+  gpu_check(katoann_gpu_search_timed(&s.view, d_queries, nq, p.k, p.nprobe, rk, p.survivors,
+                                     s.max_batch, s.ws.p, s.ws.n, d_ids, d_dists,
+                                     reinterpret_cast<katoann_stream_t>(st), timer));
   cuda_check(cudaEventRecord(s.done, st), "cudaEventRecord");
   s.last_stream = st;
 }

@@ -12,6 +12,7 @@
 // is the reference's Selection::kLocal result (:101-135 then :1063-1069) and
 // its kThreshold result wherever that has no tie on the survivor boundary.
 #include <algorithm>
+#include <vector>
 
 #include "kcommon.cuh"
 
@@ -610,6 +611,16 @@ int sq16_tiles(const uint8_t *qhi, const uint8_t *qlo, const uint8_t *xhi, const
 int select_topp(const float *dists, uint32_t nq, uint32_t n, uint32_t p, uint32_t *probed,
                 unsigned long long *tie_count, cudaStream_t st);
 
+struct PhaseTimer {
+  std::vector<cudaEvent_t> ev;  // (KATO_PHASES + 1) per pass
+  uint32_t max_passes = 0, used = 0;
+};
+
+static void mark(PhaseTimer *t, uint32_t phase, cudaStream_t st) {
+  if (!t || t->used >= t->max_passes) return;
+  cudaEventRecord(t->ev[t->used * (KATO_PHASES + 1) + phase], st);
+}
+
 struct Plan {
   uint32_t B, k, p, S, SC, dims;
   int ranking;
@@ -670,7 +681,8 @@ int make_plan(const katoann_gpu_index *ix, uint32_t B, uint32_t k, uint32_t p, i
 }
 
 int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *queries, uint32_t nq,
-                unsigned char *ws, uint32_t *out_ids, float *out_dists, cudaStream_t st) {
+                unsigned char *ws, uint32_t *out_ids, float *out_dists, cudaStream_t st,
+                PhaseTimer *tm) {
   int rc;
   const uint32_t L = ix->nlist, p = pl.p, dc = ix->dc;
   float *fq = reinterpret_cast<float *>(ws + pl.off_fq);
@@ -691,6 +703,7 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
   uint32_t *nsurv = reinterpret_cast<uint32_t *>(ws + pl.off_nsurv);
   unsigned long long *stats = reinterpret_cast<unsigned long long *>(ws + pl.off_stats);
 
+  mark(tm, 0, st);
   // 1. rotation and quantization of the queries (src/index.cpp:895-899, :917-943)
   const float *src = queries;
   if (ix->rotated) {
@@ -700,11 +713,14 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
   if ((rc = quantize_rows(src, nq, ix->dim, dc, ix->lo, ix->inv_step, ix->head_dims, qhi, qlo, qn,
                           qhn, qh0, st)))
     return rc;
+  mark(tm, 1, st);
   // 2. coarse product and top-nprobe (:846-877)
   if ((rc = sq16_tiles(qhi, qlo, ix->d_chi, ix->d_clo, qn, ix->d_cnorm, ix->step_sq, nq, L, dc, dc,
                        dc, cd, true, st)))
     return rc;
+  mark(tm, 2, st);
   if ((rc = select_topp(cd, nq, L, p, probed, stats + 0, st))) return rc;
+  mark(tm, 3, st);
   // 3. inversion (:403-412)
   const uint32_t total = nq * p;
   KATO_CUDA(cudaMemsetAsync(cnt, 0, static_cast<size_t>(L) * 4, st));
@@ -713,6 +729,7 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
   scatter_kernel<<<div_up(total, 256), 256, 0, st>>>(probed, total, off, cur, ent);
   work_kernel<<<div_up(L, 256), 256, 0, st>>>(cnt, woff, L, work);
   KATO_LAUNCHED("inversion kernels");
+  mark(tm, 4, st);
   // 4. ranking pass (:998-1044 / :1167-1204)
   const bool full = pl.ranking == KATO_RANK_FULL;
   RankArgs A{};
@@ -749,6 +766,7 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
   if (full) rc = pl.select ? launch(rank_kernel<true, true>) : launch(rank_kernel<true, false>);
   else rc = pl.select ? launch(rank_kernel<false, true>) : launch(rank_kernel<false, false>);
   if (rc) return rc;
+  mark(tm, 5, st);
   // 5. per-query merge of the slot lists (:1058-1080 / :1205-1218)
   uint32_t np2 = 1;
   while (np2 < pl.S) np2 <<= 1;
@@ -758,7 +776,12 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
   merge_kernel<<<nq, kThreads, msmem, st>>>(slots, p * pl.SC, ix->d_ids, pl.S, full, pl.k, surv,
                                             nsurv, out_ids, out_dists, stats + 1);
   KATO_LAUNCHED("merge_kernel");
-  if (full) return KATO_OK;
+  mark(tm, 6, st);
+  if (full) {
+    mark(tm, 7, st);
+    if (tm && tm->used < tm->max_passes) ++tm->used;
+    return KATO_OK;
+  }
   // 6. exact refinement and top-k (:1081-1125)
   const size_t rsmem = static_cast<size_t>(dc) * 2 + static_cast<size_t>(pl.S) * 8 +
                        static_cast<size_t>(pl.k) * 8;
@@ -768,12 +791,14 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
                                              ix->d_ids, ix->npts, dc, surv, nsurv, pl.S, pl.k,
                                              make_dist_scale(ix->step_sq), out_ids, out_dists);
   KATO_LAUNCHED("refine_kernel");
+  mark(tm, 7, st);
+  if (tm && tm->used < tm->max_passes) ++tm->used;
   return KATO_OK;
 }
 
 int search(const katoann_gpu_index *ix, const float *queries, uint32_t nq, uint32_t k, uint32_t p,
            int ranking, uint32_t survivors, uint32_t max_batch, void *ws, size_t ws_bytes,
-           uint32_t *out_ids, float *out_dists, cudaStream_t st) {
+           uint32_t *out_ids, float *out_dists, cudaStream_t st, void *timer) {
   if (nq == 0) return KATO_OK;
   if (max_batch == 0) return invalid("max_batch must be positive");
   Plan pl{};
@@ -789,9 +814,45 @@ int search(const katoann_gpu_index *ix, const float *queries, uint32_t nq, uint3
     const uint32_t b = std::min(max_batch, nq - q0);
     if ((rc = search_pass(ix, pl, queries + static_cast<size_t>(q0) * ix->dim, b, w,
                           out_ids + static_cast<size_t>(q0) * k,
-                          out_dists + static_cast<size_t>(q0) * k, st)))
+                          out_dists + static_cast<size_t>(q0) * k, st,
+                          static_cast<PhaseTimer *>(timer))))
       return rc;
   }
+  return KATO_OK;
+}
+
+void *timer_create(uint32_t max_passes) {
+  auto *t = new PhaseTimer();
+  t->max_passes = max_passes;
+  t->ev.resize(static_cast<size_t>(max_passes) * (KATO_PHASES + 1));
+  for (auto &e : t->ev)
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      delete t;
+      return nullptr;
+    }
+  return t;
+}
+
+void timer_destroy(void *p) {
+  auto *t = static_cast<PhaseTimer *>(p);
+  if (!t) return;
+  for (auto &e : t->ev) cudaEventDestroy(e);
+  delete t;
+}
+
+int timer_read(void *p, float *ms, uint32_t *passes) {
+  auto *t = static_cast<PhaseTimer *>(p);
+  for (int i = 0; i < KATO_PHASES; ++i) ms[i] = 0.0f;
+  *passes = t->used;
+  if (t->used == 0) return KATO_OK;
+  KATO_CUDA(cudaEventSynchronize(t->ev[t->used * (KATO_PHASES + 1) - 1]));
+  for (uint32_t u = 0; u < t->used; ++u)
+    for (int i = 0; i < KATO_PHASES; ++i) {
+      float x = 0;
+      const cudaEvent_t a = t->ev[u * (KATO_PHASES + 1) + i], b = t->ev[u * (KATO_PHASES + 1) + i + 1];
+      if (cudaEventElapsedTime(&x, a, b) == cudaSuccess) ms[i] += x;
+    }
+  t->used = 0;
   return KATO_OK;
 }
 

@@ -29,8 +29,15 @@ def _load():
     path = os.path.join(_LIBDIR, "libkatoann.so")
     if not os.path.exists(path):
         raise ImportError(f"{path} is missing: build with `python -c 'import __graft_entry__ as g; g.build()'`")
-    C.CDLL(os.path.join(_LIBDIR, "libkatoann_gpu.so"), mode=C.RTLD_GLOBAL)
+    gpu = C.CDLL(os.path.join(_LIBDIR, "libkatoann_gpu.so"), mode=C.RTLD_GLOBAL)
+    gpu.katoann_gpu_timer_create.argtypes = [C.c_uint32]
+    gpu.katoann_gpu_timer_create.restype = C.c_void_p
+    gpu.katoann_gpu_timer_destroy.argtypes = [C.c_void_p]
+    gpu.katoann_gpu_timer_read.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    gpu.katoann_gpu_last_error.restype = C.c_char_p
+    gpu.katoann_gpu_copy_to_host.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
     lib = C.CDLL(path)
+    lib.gpu = gpu
     P, U32, I32, U64, D, S = C.c_void_p, C.c_uint32, C.c_int, C.c_uint64, C.c_double, C.c_size_t
     lib.katoann_last_error.restype = C.c_char_p
     lib.katoann_build.argtypes = [P, U32, U32, U32, U32, U32, U64, I32, U32, U32, C.c_char_p]
@@ -40,7 +47,7 @@ def _load():
     lib.katoann_index_load_arrays.argtypes = [P, U32, U32, U32, I32, P, P, P, P, P, I32, U32, I32,
                                               U32, U32]
     lib.katoann_index_search.argtypes = [P, P, U32, U32, U32, I32, U32, I32, P, P]
-    lib.katoann_index_search_device.argtypes = [P, P, U32, U32, U32, I32, U32, I32, P, P, P]
+    lib.katoann_index_search_device.argtypes = [P, P, U32, U32, U32, I32, U32, I32, P, P, P, P]
     lib.katoann_index_info.argtypes = [P, P]
     lib.katoann_index_memory_bytes.argtypes = [P]
     lib.katoann_index_memory_bytes.restype = S
@@ -59,6 +66,15 @@ _lib = _load()
 
 def _ptr(a: np.ndarray):
     return a.ctypes.data_as(C.c_void_p)
+
+
+_CUDA_STREAM_LEGACY = 0x1  # cudaStreamLegacy
+
+
+def _stream_arg(stream):
+    if stream is None:
+        return None
+    return C.c_void_p(int(stream) if int(stream) else _CUDA_STREAM_LEGACY)
 
 
 def _check(rc: int) -> None:
@@ -99,6 +115,56 @@ def normalize_rows(x: np.ndarray) -> np.ndarray:
 def dist_value(l2: int, step_sq: float) -> float:
     """float(double(l2) * step_sq), by the integer method of the kernels."""
     return float(_lib.katoann_dist_value(int(l2), float(step_sq)))
+
+
+PHASES = ("rotate+quantize", "coarse product", "coarse select", "inversion", "ranking pass",
+          "survivor merge", "refine")
+
+
+class PhaseTimer:
+    """CUDA events at the phase boundaries of every device search pass
+    (katoann_gpu_timer_create); read() returns the summed ms per phase."""
+
+    def __init__(self, max_passes: int):
+        self.handle = _lib.gpu.katoann_gpu_timer_create(max_passes)
+        if not self.handle:
+            raise RuntimeError("cannot create the phase timer")
+
+    def read(self) -> tuple[dict, int]:
+        ms = np.zeros(len(PHASES), np.float32)
+        n = np.zeros(1, np.uint32)
+        rc = _lib.gpu.katoann_gpu_timer_read(C.c_void_p(self.handle), _ptr(ms), _ptr(n))
+        if rc:
+            raise RuntimeError(_lib.gpu.katoann_gpu_last_error().decode())
+        return dict(zip(PHASES, map(float, ms))), int(n[0])
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h:
+            _lib.gpu.katoann_gpu_timer_destroy(C.c_void_p(h))
+            self.handle = None
+
+
+class GpuIndexView(C.Structure):
+    """The katoann_gpu_index the kernels read (include/katoann_gpu.h)."""
+    _fields_ = [("dim", C.c_uint32), ("dc", C.c_uint32), ("nlist", C.c_uint32), ("npts", C.c_uint32),
+                ("head_dims", C.c_uint32), ("rotated", C.c_uint32), ("max_list", C.c_uint32),
+                ("reserved", C.c_uint32), ("lo", C.c_float), ("pad", C.c_float),
+                ("inv_step", C.c_double), ("step_sq", C.c_double),
+                ("d_rotation", C.c_void_p), ("d_hi", C.c_void_p), ("d_lo", C.c_void_p),
+                ("d_norm", C.c_void_p), ("d_hinorm", C.c_void_p), ("d_headnorm", C.c_void_p),
+                ("d_ids", C.c_void_p), ("d_list_off", C.c_void_p), ("d_chi", C.c_void_p),
+                ("d_clo", C.c_void_p), ("d_cnorm", C.c_void_p)]
+
+
+def device_to_host(ptr: int, nbytes: int, dtype) -> np.ndarray:
+    """Copy nbytes of device memory at ptr into a new host array of dtype."""
+    buf = np.empty(nbytes, np.uint8)
+    if nbytes:
+        rc = _lib.gpu.katoann_gpu_copy_to_host(_ptr(buf), C.c_void_p(ptr), nbytes)
+        if rc:
+            raise RuntimeError(_lib.gpu.katoann_gpu_last_error().decode())
+    return buf.view(dtype)
 
 
 class Index:
@@ -180,15 +246,16 @@ class Index:
 
     def search_device(self, queries, ids, dists, k: int = 10, nprobe: int = 64,
                       ranking: str = "prefix", survivors: int = 32, selection: str = "threshold",
-                      stream: int = 0) -> None:
+                      stream: int | None = None, timer: "PhaseTimer | None" = None) -> None:
         """CUDA tensors in (nq x dim float32) and out (nq x k uint32/int32,
-        float32) on `stream` (a cudaStream_t as int; 0 = the index's stream).
-        Asynchronous."""
+        float32) on `stream` (a cudaStream_t as int, e.g. torch's
+        ``Stream.cuda_stream``; 0 is the legacy default stream; None = the
+        index's own stream). Asynchronous."""
         nq = int(queries.shape[0])
         _check(_lib.katoann_index_search_device(
             self._h, C.c_void_p(queries.data_ptr()), nq, k, nprobe, _RANKING[ranking], survivors,
             _SELECTION[selection], C.c_void_p(ids.data_ptr()), C.c_void_p(dists.data_ptr()),
-            C.c_void_p(stream) if stream else None))
+            _stream_arg(stream), C.c_void_p(timer.handle) if timer else None))
 
     def search_stats(self) -> dict:
         s = np.zeros(3, np.uint64)
@@ -241,3 +308,28 @@ class Index:
     def device_view(self) -> int:
         """Address of the katoann_gpu_index the kernels read (for direct C ABI calls)."""
         return int(_lib.katoann_index_device_view(self._h) or 0)
+
+    def view(self) -> GpuIndexView:
+        return GpuIndexView.from_address(self.device_view)
+
+    def export_codes(self) -> dict:
+        """Host copies of the device-resident index: info (dim, nlist, npts, dc,
+        head_dims, rotated), scale (lo, inv_step, step, step_sq), rotation,
+        list offsets, ids, code planes (rows x dc) and norms, centroid planes."""
+        v = self.view()
+        n, dc, L, dim = v.npts, v.dc, v.nlist, v.dim
+        h = lambda ptr, nb, dt: device_to_host(ptr, nb, dt)
+        return {
+            "info": np.array([dim, L, n, dc, v.head_dims, v.rotated], np.uint32),
+            "scale": np.array([v.lo, v.inv_step, np.sqrt(v.step_sq), v.step_sq], np.float64),
+            "rotation": h(v.d_rotation, dim * dim * 4, np.float32).reshape(dim, dim) if v.rotated else None,
+            "list_off": h(v.d_list_off, (L + 1) * 4, np.uint32),
+            "ids": h(v.d_ids, n * 4, np.uint32),
+            "hi": h(v.d_hi, n * dc, np.uint8).reshape(n, dc),
+            "lo": h(v.d_lo, n * dc, np.uint8).reshape(n, dc),
+            "norm": h(v.d_norm, n * 8, np.int64), "hinorm": h(v.d_hinorm, n * 8, np.int64),
+            "headnorm": h(v.d_headnorm, n * 8, np.int64) if v.head_dims else None,
+            "chi": h(v.d_chi, L * dc, np.uint8).reshape(L, dc),
+            "clo": h(v.d_clo, L * dc, np.uint8).reshape(L, dc),
+            "cnorm": h(v.d_cnorm, L * 8, np.int64),
+        }

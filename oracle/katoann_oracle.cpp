@@ -189,12 +189,9 @@ void read_files(Index &x, const std::string &prefix, std::vector<float> &raw, ui
   }
 }
 
-// src/index.cpp:613-750, :777-807
-Index *load(const std::string &prefix, uint32_t prefix_dims) {
-  auto x = std::make_unique<Index>();
-  std::vector<float> raw;
-  uint32_t stored = 0;
-  read_files(*x, prefix, raw, &stored);
+// Coding of an index whose files have been read (src/index.cpp:613-750,
+// :777-807): raw holds the unrotated vectors in list order.
+void code_index(Index *x, std::vector<float> &raw, uint32_t dims) {
   const uint32_t d = x->dim;
   const size_t n = x->npts;
   if (x->rotated && n) {
@@ -205,9 +202,10 @@ Index *load(const std::string &prefix, uint32_t prefix_dims) {
   x->dc = round_up(d, 64u);
   const uint32_t Dc = x->dc;
   float glo = FLT_MAX, ghi = -FLT_MAX;
-  for (float v : raw) {
-    glo = std::min(glo, v);
-    ghi = std::max(ghi, v);
+#pragma omp parallel for reduction(min : glo) reduction(max : ghi)
+  for (int64_t i = 0; i < static_cast<int64_t>(raw.size()); ++i) {
+    glo = std::min(glo, raw[i]);
+    ghi = std::max(ghi, raw[i]);
   }
   x->lo = glo;
   const double rng = static_cast<double>(ghi) - glo;
@@ -232,7 +230,6 @@ Index *load(const std::string &prefix, uint32_t prefix_dims) {
     x->norm[i] = nrm;
     x->hinorm[i] = nh;
   }
-  const uint32_t dims = prefix_dims ? prefix_dims : stored;
   if (x->has_dimc && dims) {
     if (dims % 64 || dims > Dc)  // src/index.cpp:695-696
       throw std::invalid_argument("prefix_dims must be a multiple of 64 within the dimension");
@@ -268,6 +265,14 @@ Index *load(const std::string &prefix, uint32_t prefix_dims) {
   x->id_row.assign(n, UINT32_MAX);
   for (uint32_t r = 0; r < n; ++r)
     if (x->ids[r] < n) x->id_row[x->ids[r]] = r;
+}
+
+Index *load(const std::string &prefix, uint32_t prefix_dims) {
+  auto x = std::make_unique<Index>();
+  std::vector<float> raw;
+  uint32_t stored = 0;
+  read_files(*x, prefix, raw, &stored);
+  code_index(x.get(), raw, prefix_dims ? prefix_dims : stored);
   return x.release();
 }
 
@@ -504,6 +509,70 @@ void *oracle_load(const char *prefix, uint32_t prefix_dims) {
 }
 
 void oracle_free(void *h) { delete static_cast<Index *>(h); }
+
+// An oracle index from in-memory arrays in the layout of the index files
+// (lists concatenated in list order, unrotated vectors), coded on the CPU.
+void *oracle_load_arrays(uint32_t dim, uint32_t nlist, uint32_t npts, const float *centroids,
+                         const uint32_t *list_sizes, const uint32_t *ids, const float *vectors,
+                         const float *rotation, uint32_t head_dims) {
+  Index *out = nullptr;
+  if (oracle::guarded([&] {
+        auto x = std::make_unique<Index>();
+        x->dim = dim;
+        x->nlist = nlist;
+        x->npts = npts;
+        x->centroids.assign(centroids, centroids + static_cast<size_t>(nlist) * dim);
+        x->list_off.assign(nlist + 1, 0);
+        for (uint32_t c = 0; c < nlist; ++c) x->list_off[c + 1] = x->list_off[c] + list_sizes[c];
+        x->ids.assign(ids, ids + npts);
+        x->has_dimc = true;
+        x->rotated = rotation != nullptr;
+        if (x->rotated) x->rotation.assign(rotation, rotation + static_cast<size_t>(dim) * dim);
+        std::vector<float> raw(vectors, vectors + static_cast<size_t>(npts) * dim);
+        oracle::code_index(x.get(), raw, head_dims);
+        out = x.release();
+      }))
+    return nullptr;
+  return out;
+}
+
+// An oracle index from already coded arrays (row-major planes in list order),
+// so that a large index coded elsewhere can be searched on the CPU. info:
+// {dim, nlist, npts, dc, head, rotated}; scale: {lo, inv_step, step, step_sq}.
+void *oracle_load_codes(const uint32_t *info, const double *scale, const float *rotation,
+                        const uint32_t *list_off, const uint32_t *ids, const uint8_t *hi,
+                        const uint8_t *lo, const int64_t *norm, const int64_t *hinorm,
+                        const int64_t *headnorm, const uint8_t *chi, const uint8_t *clo,
+                        const int64_t *cnorm) {
+  auto *x = new Index();
+  x->dim = info[0];
+  x->nlist = info[1];
+  x->npts = info[2];
+  x->dc = info[3];
+  x->head = info[4];
+  x->rotated = info[5] != 0;
+  x->has_dimc = x->head != 0 || x->rotated;
+  x->lo = static_cast<float>(scale[0]);
+  x->inv_step = scale[1];
+  x->step = scale[2];
+  x->step_sq = scale[3];
+  const size_t n = x->npts, L = x->nlist, dc = x->dc;
+  if (x->rotated) x->rotation.assign(rotation, rotation + static_cast<size_t>(x->dim) * x->dim);
+  x->list_off.assign(list_off, list_off + L + 1);
+  x->ids.assign(ids, ids + n);
+  x->hi.assign(hi, hi + n * dc);
+  x->lo_plane.assign(lo, lo + n * dc);
+  x->norm.assign(norm, norm + n);
+  x->hinorm.assign(hinorm, hinorm + n);
+  if (x->head) x->headnorm.assign(headnorm, headnorm + n);
+  x->chi.assign(chi, chi + L * dc);
+  x->clo.assign(clo, clo + L * dc);
+  x->cnorm.assign(cnorm, cnorm + L);
+  x->id_row.assign(n, UINT32_MAX);
+  for (uint32_t r = 0; r < n; ++r)
+    if (x->ids[r] < n) x->id_row[x->ids[r]] = r;
+  return x;
+}
 
 int oracle_search(void *h, const float *q, uint32_t nq, uint32_t k, uint32_t nprobe, int ranking,
                   uint32_t survivors, uint32_t *ids, float *dists) {

@@ -31,6 +31,10 @@ def lib():
         _lib.oracle_load.argtypes = [C.c_char_p, U32]
         _lib.oracle_load.restype = P
         _lib.oracle_free.argtypes = [P]
+        _lib.oracle_load_codes.argtypes = [P] * 13
+        _lib.oracle_load_codes.restype = P
+        _lib.oracle_load_arrays.argtypes = [U32, U32, U32, P, P, P, P, P, U32]
+        _lib.oracle_load_arrays.restype = P
         _lib.oracle_search.argtypes = [P, P, U32, U32, U32, I32, U32, P, P]
         _lib.oracle_info.argtypes = [P, P, P]
         _lib.oracle_list_offsets.argtypes = [P, P]
@@ -64,10 +68,37 @@ def max_threads() -> int:
 class OracleIndex:
     """The restated reference index: codes, norms and search on the CPU."""
 
-    def __init__(self, prefix: str, prefix_dims: int = 0):
-        self.h = lib().oracle_load(prefix.encode(), prefix_dims)
+    def __init__(self, prefix: str | None, prefix_dims: int = 0, codes: dict | None = None,
+                 arrays: dict | None = None):
+        keep = []
+        if codes is not None:
+            self.h = self._from_codes(codes)
+        elif arrays is not None:
+            a = {k: (np.ascontiguousarray(v) if isinstance(v, np.ndarray) else v)
+                 for k, v in arrays.items()}
+            keep.append(a)
+            self.h = lib().oracle_load_arrays(
+                a["centroids"].shape[1], a["centroids"].shape[0], a["vectors"].shape[0],
+                _p(a["centroids"].astype(np.float32)), _p(a["list_sizes"].astype(np.uint32)),
+                _p(a["ids"].astype(np.uint32)), _p(a["vectors"].astype(np.float32, copy=False)),
+                _p(a["rotation"].astype(np.float32)) if a.get("rotation") is not None else None,
+                int(a.get("head_dims", 0)))
+        else:
+            self.h = lib().oracle_load(prefix.encode(), prefix_dims)
         if not self.h:
             raise RuntimeError(lib().oracle_last_error().decode())
+        self._read_info()
+
+    @staticmethod
+    def _from_codes(c: dict):
+        """c: info (u32[6]), scale (f64[4]), rotation, list_off, ids, hi, lo, norm,
+        hinorm, headnorm, chi, clo, cnorm as numpy arrays (host)."""
+        keys = ("info", "scale", "rotation", "list_off", "ids", "hi", "lo", "norm", "hinorm",
+                "headnorm", "chi", "clo", "cnorm")
+        arrs = [np.ascontiguousarray(c[k]) if c.get(k) is not None else None for k in keys]
+        return lib().oracle_load_codes(*[_p(a) if a is not None else None for a in arrs])
+
+    def _read_info(self):
         info = np.zeros(8, np.uint32)
         scale = np.zeros(4, np.float64)
         lib().oracle_info(self.h, _p(info), _p(scale))

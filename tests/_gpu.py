@@ -54,28 +54,11 @@ def dptr(t) -> C.c_void_p:
     return C.c_void_p(t.data_ptr())
 
 
-def view_of(index) -> GpuIndex:
+def view_of(index):
     """The katoann_gpu_index of a katoann.Index (host copy of the struct)."""
-    return GpuIndex.from_address(index.device_view)
+    return index.view()
 
 
 def to_host(ptr: int, nbytes: int, dtype) -> np.ndarray:
-    buf = np.empty(nbytes, np.uint8)
-    rc = _cudart().cudaMemcpy(buf.ctypes.data_as(C.c_void_p), C.c_void_p(ptr), C.c_size_t(nbytes), 2)
-    if rc != 0:
-        raise RuntimeError(f"cudaMemcpy failed: {rc}")
-    return buf.view(dtype)
-
-
-_rt = None
-
-
-def _cudart():
-    global _rt
-    if _rt is None:
-        import glob
-        import torch  # noqa: F401  (loads torch's cudart)
-        cands = glob.glob("/usr/local/cuda/lib64/libcudart.so*")
-        _rt = C.CDLL(cands[0] if cands else "libcudart.so")
-        _rt.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
-    return _rt
+    import katoann
+    return katoann.device_to_host(ptr, nbytes, dtype)
