@@ -67,9 +67,11 @@ def make_data(torch, n, d, ncomp, seed, queries):
     weights follow Zipf(1.1), so the inverted lists come out skewed."""
     dev = "cuda"
     g = torch.Generator(device=dev).manual_seed(seed)
-    A = torch.randn(d, d, generator=g, device=dev)
-    Q, R = torch.linalg.qr(A)
-    Q = Q * torch.sign(torch.diagonal(R))[None, :]
+    # random orthogonal basis (QR on the host: torch's linear-algebra library is
+    # not needed on the device path)
+    A = torch.randn(d, d, generator=g, device=dev).double().cpu().numpy()
+    Qn, Rn = np.linalg.qr(A)
+    Q = torch.from_numpy(Qn * np.sign(np.diag(Rn))[None, :]).float().to(dev)
     lam = torch.arange(1, d + 1, device=dev, dtype=torch.float32) ** -1.2
     B = torch.sqrt(lam / lam.sum())[:, None] * Q.T
     centres = torch.randn(ncomp, d, generator=g, device=dev) @ B
@@ -118,10 +120,11 @@ def pca_rotation(torch, x, sample, seed):
     g = torch.Generator(device="cuda").manual_seed(seed + 2)
     s = x[torch.randperm(x.shape[0], generator=g, device="cuda")[:sample]].double()
     s -= s.mean(0, keepdim=True)
-    cov = (s.T @ s) / s.shape[0]
-    evals, evecs = torch.linalg.eigh(cov)
-    order = torch.argsort(evals, descending=True)
-    return evecs[:, order].T.float().contiguous()  # row j = axis of j-th largest variance
+    cov = ((s.T @ s) / s.shape[0]).cpu().numpy()
+    evals, evecs = np.linalg.eigh(cov)
+    order = np.argsort(-evals, kind="stable")
+    # row j = axis of the j-th largest variance
+    return torch.from_numpy(np.ascontiguousarray(evecs[:, order].T)).float().cuda()
 
 
 def ground_truth(torch, x, ids, q, k, chunk=262144):
