@@ -114,6 +114,19 @@ int katoann_gpu_coarse(const katoann_gpu_index *index, const uint8_t *d_qhi, con
                        const int64_t *d_qnorm, uint32_t nq, uint32_t nprobe, float *d_dists,
                        uint32_t *d_probed, katoann_stream_t stream);
 
+/* katoann_gpu_coarse for callers that cannot allocate device memory (a host
+ * that owns every byte of device memory through its own allocator, or a
+ * latency-bound loop that cannot afford cudaMalloc's device-wide
+ * synchronisation). The nq x nlist distance scratch lives in a static device
+ * array of 1,048,576 floats (4 MiB, held by every GPU that loads the library
+ * until exit); nq * nlist above that is rejected with KATO_EINVAL. The first
+ * call on a device resolves the array's address (make it before any stream
+ * capture). Calls share the array: calls that overlap on the GPU race. This
+ * entry point has no counterpart in the reference. */
+int katoann_gpu_coarse_noalloc(const katoann_gpu_index *index, const uint8_t *d_qhi,
+                               const uint8_t *d_qlo, const int64_t *d_qnorm, uint32_t nq,
+                               uint32_t nprobe, uint32_t *d_probed, katoann_stream_t stream);
+
 /* Bytes of device workspace that katoann_gpu_search needs for up to
  * max_batch queries per pass with these parameters. */
 size_t katoann_gpu_search_workspace(const katoann_gpu_index *index, uint32_t max_batch,
