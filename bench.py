@@ -34,7 +34,6 @@ for _p in (os.path.join(ROOT, "katoann-public_gb300"), os.path.join(ROOT, "oracl
         sys.path.insert(0, _p)
 
 PUBLISHED_QPS_099 = 6294.0  # README.md:84 (BioASQ-1024-10M, 28-core Xeon, nlist 8192)
-KERNELS_PER_PASS = 11       # rotate, quantize, coarse, select, 4 inversion, rank, merge, refine
 
 
 def parse_args():
@@ -349,6 +348,10 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = world * B * args.steps / (ms / 1e3)
+    idx.search_device(queries, ids_d, dists_d, k=k, nprobe=p, survivors=S, stream=stream)
+    torch.cuda.synchronize()
+    search_stats = idx.search_stats()
+    launches_per_search = katoann.last_launches()
 
     # ---- end to end through the public host API (pinned host buffers)
     qh = torch.empty((B, d), dtype=torch.float32).pin_memory()
@@ -425,11 +428,12 @@ def main():
         "e2e": {"value": round(e2e_qps, 1), "unit": "queries/s", "recall": round(e2e_recall, 5),
                 "h2d_bytes_per_step": B * d * 4, "d2h_bytes_per_step": B * k * 8,
                 "api": "katoann.Index.search_into (pinned host buffers)"},
-        "gpu_launches": KERNELS_PER_PASS * args.steps,
+        "gpu_launches": launches_per_search * args.steps,
         "clocks": clk,
         "cpu_baseline": cpu,
         "parity_full_size": parity,
         "lists": skew,
+        "search_stats": search_stats,
         "setup_s": round(setup_s, 1), "load_s": round(load_s, 1),
         "host": platform.machine(),
     }

@@ -159,6 +159,16 @@ void katoann_gpu_timer_destroy(void *timer);
  * into h_ms[0..KATO_PHASES) and their count into *passes; synchronous. */
 int katoann_gpu_timer_read(void *timer, float *h_ms, uint32_t *passes);
 
+/* Kernel launches of this thread's last katoann_gpu_search call (all passes). */
+uint32_t katoann_gpu_last_launches(void);
+
+/* Entries per query of the tensor-core ranking pass's candidate buffer
+ * (default 16384, range [16, 2^20]; process-wide, read when a workspace is
+ * sized and at each search). Queries with more candidates than this are
+ * rescanned exactly; searches with survivors above it use the CUDA-core pass.
+ * Results do not depend on it. */
+int katoann_gpu_set_candidate_cap(uint32_t cap);
+
 /* katoann_gpu_search that also records phase events into `timer` (may be
  * NULL, then identical to katoann_gpu_search). */
 int katoann_gpu_search_timed(const katoann_gpu_index *index, const float *d_queries, uint32_t nq,
@@ -169,7 +179,18 @@ int katoann_gpu_search_timed(const katoann_gpu_index *index, const float *d_quer
 /* Diagnostics that katoann_gpu_search left in its workspace, copied to the
  * host (synchronous on `stream`): [0] queries whose nprobe-th coarse distance
  * was tied with a list outside the probe set, [1] queries whose survivor
- * boundary (S-th ranking distance) was tied, [2] queries searched. */
+ * boundary (S-th ranking distance) was tied, [2] unused, [3] persistent
+ * ranking CTAs whose bounded tensor-core wait ran out (their remaining work
+ * is lost; never expected, reported so that it cannot pass silently), [4]
+ * 128-row tiles the tensor-core ranking pass scored, [5] candidates it
+ * appended (rows within their query's seed bound), [6] queries whose
+ * candidate buffer overflowed and were rescanned exactly, [7] the largest
+ * number of candidates one query had (last batch pass), [16..29] SM cycles
+ * of the tensor-core ranking pass's warp roles, summed over CTAs (first
+ * thread of each role): converters waiting for raw tiles, for free A stages,
+ * total; MMA waiting for query tiles, free accumulators, converted tiles,
+ * total; epilogue waiting for query tiles, accumulators, total; TMA waiting
+ * for free stages, total; query staging waiting for free query tiles, total. */
 int katoann_gpu_workspace_stats(const void *d_ws, uint64_t *h_stats, uint32_t n,
                                 katoann_stream_t stream);
 

@@ -1,6 +1,7 @@
 // extern "C" entry points of libkatoann_gpu.so (declared in
 // include/katoann_gpu.h). Argument checks mirror the reference's exceptions
 // (src/index.cpp:882-892) as status codes; nothing throws across the ABI.
+#include <atomic>
 #include <cstdio>
 #include <string>
 
@@ -36,6 +37,8 @@ int search(const katoann_gpu_index *ix, const float *queries, uint32_t nq, uint3
            int ranking, uint32_t survivors, uint32_t max_batch, void *ws, size_t ws_bytes,
            uint32_t *out_ids, float *out_dists, cudaStream_t st, void *timer);
 void *timer_create(uint32_t max_passes);
+uint32_t last_launches();
+extern std::atomic<uint32_t> g_candidate_cap;
 void timer_destroy(void *t);
 int timer_read(void *t, float *ms, uint32_t *passes);
 size_t search_workspace(const katoann_gpu_index *ix, uint32_t max_batch, uint32_t k, uint32_t p,
@@ -136,6 +139,14 @@ int katoann_gpu_search_timed(const katoann_gpu_index *ix, const float *d_queries
 
 void *katoann_gpu_timer_create(uint32_t max_passes) { return kato::timer_create(max_passes); }
 
+uint32_t katoann_gpu_last_launches(void) { return kato::last_launches(); }
+
+int katoann_gpu_set_candidate_cap(uint32_t cap) {
+  if (cap < 16 || cap > (1u << 20)) return kato::invalid("candidate buffer size must be in [16, 2^20]");
+  kato::g_candidate_cap.store(cap);
+  return KATO_OK;
+}
+
 void katoann_gpu_timer_destroy(void *timer) { kato::timer_destroy(timer); }
 
 int katoann_gpu_timer_read(void *timer, float *h_ms, uint32_t *passes) {
@@ -145,7 +156,7 @@ int katoann_gpu_timer_read(void *timer, float *h_ms, uint32_t *passes) {
 
 int katoann_gpu_workspace_stats(const void *d_ws, uint64_t *h_stats, uint32_t n,
                                 katoann_stream_t stream) {
-  if (n > 8) return kato::invalid("at most 8 statistics");
+  if (n > 32) return kato::invalid("at most 32 statistics");
   KATO_CUDA(cudaMemcpyAsync(h_stats, d_ws, n * sizeof(uint64_t), cudaMemcpyDeviceToHost,
                             as_stream(stream)));
   KATO_CUDA(cudaStreamSynchronize(as_stream(stream)));

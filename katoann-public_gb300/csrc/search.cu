@@ -12,11 +12,17 @@
 // is the reference's Selection::kLocal result (:101-135 then :1063-1069) and
 // its kThreshold result wherever that has no tie on the survivor boundary.
 #include <algorithm>
+#include <atomic>
 #include <vector>
 
 #include "kcommon.cuh"
+#include "rank_tc.cuh"
 
 namespace kato {
+
+thread_local uint32_t g_launches = 0;  // kernel launches of the last search pass
+// Entries per query of the tensor-core ranking pass's candidate buffer.
+std::atomic<uint32_t> g_candidate_cap{16384};
 
 namespace {
 
@@ -459,12 +465,14 @@ __device__ void block_sort_pairs(unsigned long long *key, uint32_t *val, uint32_
 }
 
 // -------------------------------------------------------------------- merge
-// Per query: the best S of its nprobe * SC slot entries by (distance, id).
+// Per query: the best S of its nprobe * SC slot entries (or of the first
+// qcount[q] entries of its candidate buffer) by (distance, id).
 // Ranked modes write the survivors in descending (distance, id) order - the
 // order in which the reference pops its merged heap into the refinement
 // (:1088-1112). The full mode writes the final top-k, ascending, padded.
 __global__ void __launch_bounds__(kThreads) merge_kernel(
-    const uint2 *__restrict__ slots, uint32_t per_query, const uint32_t *__restrict__ ids,
+    const uint2 *__restrict__ slots, uint32_t per_query, const uint32_t *__restrict__ qcount,
+    const uint32_t *__restrict__ ids,
     uint32_t S, bool final_topk, uint32_t k, uint2 *__restrict__ surv, uint32_t *__restrict__ nsurv,
     uint32_t *__restrict__ out_ids, float *__restrict__ out_dists,
     unsigned long long *__restrict__ tie_count) {
@@ -477,9 +485,10 @@ __global__ void __launch_bounds__(kThreads) merge_kernel(
   uint32_t *pos = reinterpret_cast<uint32_t *>(sel + np2);
   const uint32_t q = blockIdx.x;
   const uint2 *e = slots + static_cast<size_t>(q) * per_query;
+  const uint32_t n = qcount ? min(qcount[q], per_query) : per_query;
   auto K = [&](uint32_t i) { return e[i].x; };
   auto I = [&](uint32_t i) { return ids[e[i].y]; };
-  const uint32_t got = block_select(per_query, S, K, I, sel, pos, hist, scratch, &tie);
+  const uint32_t got = block_select(n, S, K, I, sel, pos, hist, scratch, &tie);
   if (threadIdx.x == 0 && tie && tie_count) atomicAdd(tie_count, 1ull);
   block_sort_pairs(sel, pos, got);
   if (final_topk) {
@@ -625,8 +634,13 @@ struct Plan {
   uint32_t B, k, p, S, SC, dims;
   int ranking;
   bool select;
+  bool tc;                          // tensor-core ranking pass
+  TcShape tcs;
+  uint32_t tcitems, cap, seed_rows, ctas, rec_cap;
   size_t off_fq, off_qhi, off_qlo, off_qn, off_qhn, off_qh0, off_cd, off_probed, off_cnt, off_off,
-      off_woff, off_cur, off_work, off_ent, off_slots, off_surv, off_nsurv, off_stats, total;
+      off_woff, off_cur, off_work, off_ent, off_slots, off_surv, off_nsurv, off_stats,
+      off_tcscratch, off_tcitems, off_tileoff, off_nitems, off_qcount, off_qfill, off_bound,
+      off_rec, off_recn, off_rlist, off_rkey, off_rcount, total;
 };
 
 static size_t align256(size_t x) { return (x + 255) / 256 * 256; }
@@ -652,13 +666,31 @@ int make_plan(const katoann_gpu_index *ix, uint32_t B, uint32_t k, uint32_t p, i
   const uint32_t L = ix->nlist;
   const size_t bp = static_cast<size_t>(B) * p;
   const size_t wmax = std::min<size_t>(L, bp) + bp / kQG + 1;
+  // tensor-core ranking: every query's candidates within its seed bound go
+  // to a buffer of `cap` entries (an overflowing query is rescanned exactly)
+  pl.cap = g_candidate_cap.load();
+  pl.tc = ranking != KATO_RANK_FULL && pl.S <= pl.cap && rank_tc_plan(pl.dims, ix->dc, &pl.tcs);
+  if (pl.tc) {
+    pl.select = true;
+    pl.SC = pl.S;
+    pl.seed_rows = std::max(1024u, 8 * pl.S);
+    pl.tcitems = static_cast<uint32_t>(bp / pl.tcs.N + std::min<size_t>(L, bp) + 1);
+    // candidate records per CTA: room for 32 S per query of the batch, spread
+    // over the CTAs (a CTA that runs out flags the queries it drops)
+    pl.ctas = rank_tc_ctas();
+    pl.rec_cap = static_cast<uint32_t>(
+        std::max<size_t>(8192, static_cast<size_t>(B) * pl.S * 32 / pl.ctas));
+  } else {
+    pl.ctas = 1;
+    pl.rec_cap = 0;
+  }
   size_t o = 0;
   auto take = [&](size_t bytes) {
     const size_t at = o;
     o += align256(bytes);
     return at;
   };
-  pl.off_stats = take(8 * sizeof(unsigned long long));
+  pl.off_stats = take(32 * sizeof(unsigned long long));
   pl.off_fq = take(static_cast<size_t>(B) * ix->dim * 4);
   pl.off_qhi = take(static_cast<size_t>(B) * ix->dc);
   pl.off_qlo = take(static_cast<size_t>(B) * ix->dc);
@@ -673,7 +705,19 @@ int make_plan(const katoann_gpu_index *ix, uint32_t B, uint32_t k, uint32_t p, i
   pl.off_cur = take(static_cast<size_t>(L) * 4);
   pl.off_work = take(wmax * sizeof(Work));
   pl.off_ent = take(bp * 4);
-  pl.off_slots = take(bp * pl.SC * sizeof(uint2));
+  pl.off_slots = take((pl.tc ? static_cast<size_t>(B) * pl.cap : bp * pl.SC) * sizeof(uint2));
+  pl.off_tcscratch = take(2 * (static_cast<size_t>(L) + 1) * 4);
+  pl.off_tcitems = take(pl.tc ? (static_cast<size_t>(pl.tcitems) + 1) * sizeof(TcItem) : 16);
+  pl.off_tileoff = take(pl.tc ? (static_cast<size_t>(pl.tcitems) + 1) * 4 : 16);
+  pl.off_nitems = take(16);
+  pl.off_qcount = take(static_cast<size_t>(B) * 4);
+  pl.off_qfill = take(static_cast<size_t>(B) * 4);
+  pl.off_bound = take(static_cast<size_t>(B) * 4);
+  pl.off_rec = take(pl.tc ? static_cast<size_t>(pl.ctas) * pl.rec_cap * 16 : 16);
+  pl.off_recn = take(static_cast<size_t>(pl.ctas) * 4);
+  pl.off_rlist = take(static_cast<size_t>(B) * 4);
+  pl.off_rkey = take(static_cast<size_t>(B) * 8);
+  pl.off_rcount = take(kRescanCounters * 4);
   pl.off_surv = take(static_cast<size_t>(B) * pl.S * sizeof(uint2));
   pl.off_nsurv = take(static_cast<size_t>(B) * 4);
   pl.total = o;
@@ -713,6 +757,7 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
   if ((rc = quantize_rows(src, nq, ix->dim, dc, ix->lo, ix->inv_step, ix->head_dims, qhi, qlo, qn,
                           qhn, qh0, st)))
     return rc;
+  g_launches += (ix->rotated ? ((ix->dim & 3) ? 2 : 1) : 0) + 1 + 2;  // rotation, quantize, coarse, select
   mark(tm, 1, st);
   // 2. coarse product and top-nprobe (:846-877)
   if ((rc = sq16_tiles(qhi, qlo, ix->d_chi, ix->d_clo, qn, ix->d_cnorm, ix->step_sq, nq, L, dc, dc,
@@ -727,9 +772,67 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
   count_kernel<<<div_up(total, 256), 256, 0, st>>>(probed, total, cnt);
   scan_kernel<<<1, 1024, 0, st>>>(cnt, L, off, woff, cur);
   scatter_kernel<<<div_up(total, 256), 256, 0, st>>>(probed, total, off, cur, ent);
-  work_kernel<<<div_up(L, 256), 256, 0, st>>>(cnt, woff, L, work);
+  g_launches += 3;
+  if (!pl.tc) {
+    work_kernel<<<div_up(L, 256), 256, 0, st>>>(cnt, woff, L, work);
+    ++g_launches;
+  }
   KATO_LAUNCHED("inversion kernels");
   mark(tm, 4, st);
+  uint32_t *qcount = nullptr;
+  if (pl.tc) {
+    // 4'. ranking pass on the tensor cores: seed bounds, work items, the
+    // scan, and the exact rescan of any query whose buffer overflowed
+    int32_t *bound = reinterpret_cast<int32_t *>(ws + pl.off_bound);
+    TcItem *items = reinterpret_cast<TcItem *>(ws + pl.off_tcitems);
+    uint32_t *tile_off = reinterpret_cast<uint32_t *>(ws + pl.off_tileoff);
+    uint32_t *nitems = reinterpret_cast<uint32_t *>(ws + pl.off_nitems);
+    uint32_t *qfill = reinterpret_cast<uint32_t *>(ws + pl.off_qfill);
+    uint4 *rec = reinterpret_cast<uint4 *>(ws + pl.off_rec);
+    uint32_t *rec_n = reinterpret_cast<uint32_t *>(ws + pl.off_recn);
+    qcount = reinterpret_cast<uint32_t *>(ws + pl.off_qcount);
+    const bool prefix_mode = pl.ranking == KATO_RANK_PREFIX;
+    const int64_t *xnorm = prefix_mode ? ix->d_headnorm : ix->d_hinorm;
+    const int64_t *qnorm = prefix_mode ? qh0 : qhn;
+    const DistScale scale = make_dist_scale(ix->step_sq);
+    if ((rc = rank_seed(ix->d_hi, xnorm, qhi, qnorm, probed, ix->d_list_off, nq, p, dc, pl.dims,
+                        pl.S, pl.seed_rows, bound, st)))
+      return rc;
+    if ((rc = rank_tc_prepare(cnt, ix->d_list_off, L, pl.tcs.N, nq,
+                              reinterpret_cast<uint32_t *>(ws + pl.off_tcscratch), items, tile_off,
+                              nitems, qcount, qfill, st)))
+      return rc;
+    RankTcArgs T{};
+    T.qhi = qhi;
+    T.qnorm = qnorm;
+    T.entries = ent;
+    T.off = off;
+    T.items = items;
+    T.tile_off = tile_off;
+    T.nitems = nitems;
+    T.bound = bound;
+    T.qcount = qcount;
+    T.rec = rec;
+    T.rec_n = rec_n;
+    T.rec_cap = pl.rec_cap;
+    T.timeouts = reinterpret_cast<uint32_t *>(stats + 3);
+    T.counters = stats + 4;
+    T.prof = stats + 16;
+    T.dc = dc;
+    T.h = pl.dims;
+    T.nprobe = p;
+    T.scale = scale;
+    if ((rc = rank_tc(T, ix->d_hi, ix->npts, pl.tcs, st))) return rc;
+    if ((rc = rank_tc_bucket(rec, rec_n, pl.rec_cap, pl.ctas, qfill, slots, pl.cap, scale, st)))
+      return rc;
+    const RescanBufs rb{reinterpret_cast<uint32_t *>(ws + pl.off_rlist),
+                        reinterpret_cast<unsigned long long *>(ws + pl.off_rkey),
+                        reinterpret_cast<uint32_t *>(ws + pl.off_rcount), qfill};
+    if ((rc = rank_overflow(ix->d_hi, xnorm, ix->d_ids, qhi, qnorm, probed, ix->d_list_off, nq, p,
+                            dc, pl.dims, pl.S, scale, qcount, slots, pl.cap, rb, stats + 6, st)))
+      return rc;
+    g_launches += 11;  // seed, 3 preparation, scan, bucket, 2 x 2 rescan rounds, exact rescan
+  }
   // 4. ranking pass (:998-1044 / :1167-1204)
   const bool full = pl.ranking == KATO_RANK_FULL;
   RankArgs A{};
@@ -755,7 +858,7 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
   const size_t bp = static_cast<size_t>(nq) * p;
   const uint32_t grid = static_cast<uint32_t>(std::min<size_t>(L, bp) + bp / kQG + 1);
   const size_t smem = rank_smem_bytes(full ? 2 : 1, pl.select, pl.dims, pl.SC);
-  if (smem > 227 * 1024) return invalid("ranking tile does not fit in shared memory");
+  if (!pl.tc && smem > 227 * 1024) return invalid("ranking tile does not fit in shared memory");
   auto launch = [&](auto kern) -> int {
     KATO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(smem)));
@@ -763,9 +866,12 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
     KATO_LAUNCHED("rank_kernel");
     return KATO_OK;
   };
-  if (full) rc = pl.select ? launch(rank_kernel<true, true>) : launch(rank_kernel<true, false>);
-  else rc = pl.select ? launch(rank_kernel<false, true>) : launch(rank_kernel<false, false>);
-  if (rc) return rc;
+  if (!pl.tc) {
+    if (full) rc = pl.select ? launch(rank_kernel<true, true>) : launch(rank_kernel<true, false>);
+    else rc = pl.select ? launch(rank_kernel<false, true>) : launch(rank_kernel<false, false>);
+    if (rc) return rc;
+    ++g_launches;
+  }
   mark(tm, 5, st);
   // 5. per-query merge of the slot lists (:1058-1080 / :1205-1218)
   uint32_t np2 = 1;
@@ -773,8 +879,10 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
   const size_t msmem = static_cast<size_t>(np2) * 12;
   KATO_CUDA(cudaFuncSetAttribute(merge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(msmem)));
-  merge_kernel<<<nq, kThreads, msmem, st>>>(slots, p * pl.SC, ix->d_ids, pl.S, full, pl.k, surv,
-                                            nsurv, out_ids, out_dists, stats + 1);
+  merge_kernel<<<nq, kThreads, msmem, st>>>(slots, pl.tc ? pl.cap : p * pl.SC, qcount, ix->d_ids,
+                                            pl.S, full, pl.k, surv, nsurv, out_ids, out_dists,
+                                            stats + 1);
+  ++g_launches;
   KATO_LAUNCHED("merge_kernel");
   mark(tm, 6, st);
   if (full) {
@@ -791,6 +899,7 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
                                              ix->d_ids, ix->npts, dc, surv, nsurv, pl.S, pl.k,
                                              make_dist_scale(ix->step_sq), out_ids, out_dists);
   KATO_LAUNCHED("refine_kernel");
+  ++g_launches;
   mark(tm, 7, st);
   if (tm && tm->used < tm->max_passes) ++tm->used;
   return KATO_OK;
@@ -809,7 +918,8 @@ int search(const katoann_gpu_index *ix, const float *queries, uint32_t nq, uint3
     return KATO_ENOMEM;
   }
   unsigned char *w = static_cast<unsigned char *>(ws);
-  KATO_CUDA(cudaMemsetAsync(w + pl.off_stats, 0, 8 * sizeof(unsigned long long), st));
+  KATO_CUDA(cudaMemsetAsync(w + pl.off_stats, 0, 32 * sizeof(unsigned long long), st));
+  g_launches = 0;
   for (uint32_t q0 = 0; q0 < nq; q0 += max_batch) {
     const uint32_t b = std::min(max_batch, nq - q0);
     if ((rc = search_pass(ix, pl, queries + static_cast<size_t>(q0) * ix->dim, b, w,
@@ -820,6 +930,8 @@ int search(const katoann_gpu_index *ix, const float *queries, uint32_t nq, uint3
   }
   return KATO_OK;
 }
+
+uint32_t last_launches() { return g_launches; }
 
 void *timer_create(uint32_t max_passes) {
   auto *t = new PhaseTimer();

@@ -1,0 +1,207 @@
+// 5th-generation tensor core (tcgen05) helpers for sm_103a, as inline PTX.
+//
+// Operands are fp16 tiles in shared memory in the K-major, no-swizzle
+// canonical layout: 8-row x 16-byte core matrices of 128 contiguous bytes;
+// core matrix (row group g, k group j) of a tile that is KT elements wide sits
+// at byte (g * (KT / 8) + j) * 128, row r of it at + 16 * (r % 8). The
+// descriptor's leading byte offset is the distance between core matrices
+// adjacent in K (128) and its stride byte offset the distance between row
+// groups (KT * 16). Accumulators are fp32 in tensor memory (TMEM): lane = row
+// of the 128-row tile, column = column of the output.
+//
+// Exactness: integer-valued fp16 operands with |a|, |b| <= 128 give products
+// of at most 2^14, so up to 1024 of them add up exactly in fp32 (|sum| <= 2^24).
+#pragma once
+
+#include <cuda_fp16.h>
+
+#include <cstdint>
+
+namespace kato {
+namespace tc {
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Shared-memory matrix descriptor (no swizzle, fixed constant at bit 46).
+__device__ __forceinline__ uint64_t desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = static_cast<uint64_t>((addr & 0x3FFFFu) >> 4);
+  d |= static_cast<uint64_t>((lbo >> 4) & 0x3FFFu) << 16;
+  d |= static_cast<uint64_t>((sbo >> 4) & 0x3FFFu) << 32;
+  d |= 1ull << 46;
+  return d;
+}
+
+// Instruction descriptor of kind::f16: fp16 A and B, K-major, fp32 accumulator.
+__host__ __device__ constexpr uint32_t idesc_f16(uint32_t m, uint32_t n) {
+  return (1u << 4) | ((n >> 3) << 17) | ((m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc,
+                                        uint32_t accumulate) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+      smem_addr(bar)));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count));
+}
+
+__device__ __forceinline__ bool mbar_try(uint64_t *bar, uint32_t phase) {
+  uint32_t ok;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      "selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(phase)
+      : "memory");
+  return ok != 0;
+}
+
+// As mbar_try, but a thread whose phase is not complete sleeps until it
+// completes or `hint_ns` nanoseconds pass, instead of returning at once.
+__device__ __forceinline__ bool mbar_try_sleep(uint64_t *bar, uint32_t phase, uint32_t hint_ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+      "selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(phase), "r"(hint_ns)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait on an mbarrier phase; false if it did not complete in time.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t phase, uint32_t limit = 1u << 26) {
+  for (uint32_t i = 0; i < limit; ++i)
+    if (mbar_try(bar, phase)) return true;
+  return false;
+}
+
+// Bounded wait on a phase with a clock deadline, giving up early once *err is
+// set by another role of the CTA; a timeout sets *err.
+// Waiting threads sleep in the barrier (up to 50 us per try) rather than
+// spin, leaving the issue slots to the warps that have work.
+__device__ __forceinline__ bool mbar_wait_or(uint64_t *bar, uint32_t phase, volatile uint32_t *err,
+                                             long long limit_cycles = 4000000000ll) {
+  const long long t0 = clock64();
+  while (!mbar_try_sleep(bar, phase, 50000)) {
+    if (*err) return false;
+    if (clock64() - t0 > limit_cycles) {
+      *err = 1;
+      return false;
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+// Arrive once and add `bytes` to the transaction count the phase waits for.
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// Barrier initialisations become visible to the async proxy (TMA, tensor core).
+__device__ __forceinline__ void fence_barrier_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// 2-D tiled TMA load of box (x, y) of `tmap` into shared memory, completing
+// on `bar` by bytes. x is the innermost coordinate (a multiple of 16 bytes).
+__device__ __forceinline__ void tma_load_2d(void *dst, const void *tmap, int32_t x, int32_t y,
+                                            uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%2, %3}], [%4];" ::"r"(smem_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(smem_addr(bar))
+      : "memory");
+}
+
+// Executed by one whole warp.
+__device__ __forceinline__ void tmem_alloc(uint32_t *dst_smem, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                   smem_addr(dst_smem)),
+               "r"(ncols));
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols));
+}
+
+__device__ __forceinline__ void fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+// Generic-proxy shared-memory writes become visible to the tensor core.
+__device__ __forceinline__ void fence_smem_to_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// 32 lanes x 16 columns of 32-bit accumulators; each thread gets its lane.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_ld1(uint32_t taddr, uint32_t &r) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%1];" : "=r"(r) : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// Byte offset of element (r, k) in a tile KT elements wide.
+__host__ __device__ __forceinline__ uint32_t canon_off(uint32_t r, uint32_t k, uint32_t kt) {
+  return ((r >> 3) * (kt >> 3) + (k >> 3)) * 128u + (r & 7u) * 16u + (k & 7u) * 2u;
+}
+
+// 16 unsigned bytes -> 16 fp16 values (byte - bias), exactly: each byte is
+// placed in the low mantissa of the fp16 number 1024 + byte, then 1024 + bias
+// is subtracted.
+__device__ __forceinline__ void bytes_to_half16(uint4 v, __half2 bias2, uint4 &lo, uint4 &hi) {
+  const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+  uint32_t o[8];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const uint32_t a = __byte_perm(w[i], 0x64646464u, 0x4140);  // bytes 0,1
+    const uint32_t b = __byte_perm(w[i], 0x64646464u, 0x4342);  // bytes 2,3
+    __half2 ha = *reinterpret_cast<const __half2 *>(&a);
+    __half2 hb = *reinterpret_cast<const __half2 *>(&b);
+    ha = __hsub2(ha, bias2);
+    hb = __hsub2(hb, bias2);
+    o[2 * i] = *reinterpret_cast<uint32_t *>(&ha);
+    o[2 * i + 1] = *reinterpret_cast<uint32_t *>(&hb);
+  }
+  lo = make_uint4(o[0], o[1], o[2], o[3]);
+  hi = make_uint4(o[4], o[5], o[6], o[7]);
+}
+
+}  // namespace tc
+}  // namespace kato

@@ -36,6 +36,7 @@ def _load():
     gpu.katoann_gpu_timer_read.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
     gpu.katoann_gpu_last_error.restype = C.c_char_p
     gpu.katoann_gpu_copy_to_host.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
+    gpu.katoann_gpu_last_launches.restype = C.c_uint32
     lib = C.CDLL(path)
     lib.gpu = gpu
     P, U32, I32, U64, D, S = C.c_void_p, C.c_uint32, C.c_int, C.c_uint64, C.c_double, C.c_size_t
@@ -62,6 +63,11 @@ def _load():
 
 
 _lib = _load()
+
+
+def last_launches() -> int:
+    """Kernel launches of this thread's last search (all its batch passes)."""
+    return int(_lib.gpu.katoann_gpu_last_launches())
 
 
 def _ptr(a: np.ndarray):
@@ -258,9 +264,18 @@ class Index:
             _stream_arg(stream), C.c_void_p(timer.handle) if timer else None))
 
     def search_stats(self) -> dict:
-        s = np.zeros(3, np.uint64)
-        _check(_lib.katoann_index_stats(self._h, _ptr(s), 3))
-        return dict(coarse_boundary_ties=int(s[0]), survivor_boundary_ties=int(s[1]))
+        """Diagnostics of the last search (see katoann_gpu_workspace_stats)."""
+        s = np.zeros(30, np.uint64)
+        _check(_lib.katoann_index_stats(self._h, _ptr(s), 30))
+        return dict(coarse_boundary_ties=int(s[0]), survivor_boundary_ties=int(s[1]),
+                    ranking_timeouts=int(s[3]), ranking_tiles=int(s[4]),
+                    ranking_candidates=int(s[5]), ranking_rescans=int(s[6]),
+                    ranking_max_candidates=int(s[7]),
+                    ranking_role_cycles=dict(zip(
+                        ("conv_wait_raw", "conv_wait_a", "conv_total", "mma_wait_b", "mma_wait_acc",
+                         "mma_wait_a", "mma_total", "epi_wait_b", "epi_wait_acc", "epi_total",
+                         "tma_wait_stage", "tma_total", "stage_wait_b", "stage_total"),
+                        (int(v) for v in s[16:30]))))
 
     def _info(self):
         info = np.zeros(8, np.uint32)

@@ -94,3 +94,12 @@ def test_bf16_precision_and_flat_coarse_are_refused(tmp_path):
         katoann.Index().load(prefix, precision="bf16")
     with pytest.raises(ValueError, match="coarse"):
         katoann.Index().load(prefix, batched_coarse=False)
+
+
+def test_candidate_cap_range_is_checked():
+    from _gpu import gpu
+    lib = gpu()
+    assert lib.katoann_gpu_set_candidate_cap(8) == -1
+    assert lib.katoann_gpu_set_candidate_cap(1 << 21) == -1
+    assert b"candidate buffer" in lib.katoann_gpu_last_error()
+    assert lib.katoann_gpu_set_candidate_cap(16384) == 0

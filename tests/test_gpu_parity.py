@@ -114,3 +114,62 @@ def test_normalized_index_normalizes_queries(tmp_path):
     ref = oracle.OracleIndex(prefix)
     rid, rd = ref.search(katoann.normalize_rows(queries), k=10, nprobe=4)
     assert np.array_equal(ids, rid) and np.array_equal(dists, rd)
+
+
+@pytest.mark.parametrize("spec,searches_", [
+    # few long lists: several 1024-row chunks per list, > 64 queries per list
+    (dict(seed=21, n=20000, dim=128, ncomp=8, nlist=4, nq=300, rotation="random"),
+     [(10, 2, "prefix", 32), (10, 1, "high", 64), (100, 2, "prefix", 32), (10, 3, "prefix", 256)]),
+    # h = 1024 in the high-byte mode (four 256-dimension chunks)
+    (dict(seed=22, n=3000, dim=1024, ncomp=8, nlist=8, nq=40, rotation="random"),
+     [(10, 2, "high", 32), (10, 3, "prefix", 48)]),
+    # h = 2048: two accumulators of 1024 dimensions
+    (dict(seed=23, n=1500, dim=2048, ncomp=6, nlist=6, nq=24, rotation="none", head_dims=2048),
+     [(10, 2, "high", 32), (5, 2, "prefix", 16)]),
+])
+def test_tensor_core_ranking_shapes_match_oracle(tmp_path, spec, searches_):
+    import katoann
+    import synth
+    prefix = str(tmp_path / "x")
+    queries, _ = synth.materialize(spec, prefix)
+    idx = _load(prefix, 0)
+    ref = oracle.OracleIndex(prefix)
+    for k, nprobe, ranking, surv in searches_:
+        ids, dists = idx.search(queries, k=k, nprobe=nprobe, ranking=ranking, survivors=surv)
+        rid, rd = ref.search(queries, k=k, nprobe=nprobe, ranking=ranking, survivors=surv)
+        bad = np.nonzero((ids != rid).any(1) | (dists != rd).any(1))[0]
+        assert len(bad) == 0, (k, nprobe, ranking, surv, bad[:5])
+        assert idx.search_stats()["coarse_boundary_ties"] >= 0
+
+
+@pytest.mark.gpu
+def test_candidate_buffer_overflow_is_rescanned_exactly(tmp_path):
+    """A candidate buffer far too small: every query overflows and is rescanned;
+    the results stay those of the oracle."""
+    import katoann
+    import synth
+    from _gpu import gpu
+    # long lists: the seed bound comes from 1024 of a query's ~10,000 nearest rows
+    spec = dict(seed=24, n=40000, dim=128, ncomp=8, nlist=4, nq=64, rotation="random")
+    prefix = str(tmp_path / "x")
+    queries, _ = synth.materialize(spec, prefix)
+    idx = _load(prefix, 0)
+    ref = oracle.OracleIndex(prefix)
+    lib = gpu()
+    idx.search(queries, k=10, nprobe=2, ranking="prefix", survivors=10)
+    most = idx.search_stats()["ranking_max_candidates"]
+    assert most > 16
+    try:
+        # cap = survivors: the bound-tightening rounds rarely converge and the
+        # rescan ends in the full selection; a cap a third of the largest
+        # candidate count with survivors 10: the rounds converge
+        for cap, ranking, surv in ((16, "prefix", 16), (16, "high", 16),
+                                   (max(16, most // 3), "prefix", 10)):
+            assert lib.katoann_gpu_set_candidate_cap(cap) == 0
+            ids, dists = idx.search(queries, k=10, nprobe=2, ranking=ranking, survivors=surv)
+            stats = idx.search_stats()
+            rid, rd = ref.search(queries, k=10, nprobe=2, ranking=ranking, survivors=surv)
+            assert np.array_equal(ids, rid) and np.array_equal(dists, rd), (cap, ranking)
+            assert stats["ranking_rescans"] > 0 and stats["ranking_timeouts"] == 0, (cap, stats)
+    finally:
+        assert lib.katoann_gpu_set_candidate_cap(16384) == 0
