@@ -64,6 +64,13 @@ typedef struct {
   const uint8_t *d_chi;      /* nlist x dc, centroids coded with the database scale */
   const uint8_t *d_clo;      /* nlist x dc */
   const int64_t *d_cnorm;    /* nlist */
+  /* Optional (NULL: the coarse step runs on the CUDA cores): the centroid
+   * planes re-centred to (byte - 128) as fp16, nlist x dc each, and the
+   * per-centroid term of the tensor-core coarse product; see
+   * katoann_gpu_centre_planes. */
+  const uint16_t *d_chi16;
+  const uint16_t *d_clo16;
+  const int64_t *d_cterm;
 } katoann_gpu_index;
 
 const char *katoann_gpu_last_error(void);
@@ -109,7 +116,11 @@ int katoann_gpu_sq16_high_l2(const uint8_t *d_qhi, const uint8_t *d_xhi, const i
  * src/index.cpp:846-877): exact SQ16 distances of nq quantized queries to the
  * centroid planes and the nprobe nearest lists per query, ascending by
  * (distance, list), into d_probed (nq x nprobe). d_dists (nq x nlist floats)
- * is caller scratch that receives the distances. */
+ * is caller scratch that receives the distances. When the view carries the
+ * centred centroid planes (d_chi16, d_clo16, d_cterm) and dc <= 1024, the
+ * product runs on the tensor cores with stream-ordered scratch for the
+ * queries' planes, and the call synchronizes the stream to check that the
+ * pipeline completed; otherwise it runs on the CUDA cores, asynchronously. */
 int katoann_gpu_coarse(const katoann_gpu_index *index, const uint8_t *d_qhi, const uint8_t *d_qlo,
                        const int64_t *d_qnorm, uint32_t nq, uint32_t nprobe, float *d_dists,
                        uint32_t *d_probed, katoann_stream_t stream);
@@ -158,6 +169,15 @@ void katoann_gpu_timer_destroy(void *timer);
 /* Sums the phase durations (ms) of all passes recorded since the last read
  * into h_ms[0..KATO_PHASES) and their count into *passes; synchronous. */
 int katoann_gpu_timer_read(void *timer, float *h_ms, uint32_t *passes);
+
+/* Tensor-core form of a plane pair: d_hi16 / d_lo16 = (byte - 128) as fp16
+ * bits, rows x dc each, and d_term[r] = norm[r] - 256 (65792 s_h + 257 s_l)
+ * - 16384 dc 66049, s = the row's sum of (byte - 128) per plane. With these
+ * for centroids and queries the coarse product is exact on fp16 tensor cores
+ * for dc <= 1024. */
+int katoann_gpu_centre_planes(const uint8_t *d_hi, const uint8_t *d_lo, const int64_t *d_norm,
+                              uint32_t rows, uint32_t dc, uint16_t *d_hi16, uint16_t *d_lo16,
+                              int64_t *d_term, katoann_stream_t stream);
 
 /* Kernel launches of this thread's last katoann_gpu_search call (all passes). */
 uint32_t katoann_gpu_last_launches(void);

@@ -5,6 +5,8 @@
 #include <cstdio>
 #include <string>
 
+#include <cuda_fp16.h>
+
 #include "kcommon.cuh"
 
 namespace kato {
@@ -38,6 +40,12 @@ int search(const katoann_gpu_index *ix, const float *queries, uint32_t nq, uint3
            uint32_t *out_ids, float *out_dists, cudaStream_t st, void *timer);
 void *timer_create(uint32_t max_passes);
 uint32_t last_launches();
+int centre_planes(const uint8_t *hi, const uint8_t *lo, const int64_t *norm, uint32_t rows,
+                  uint32_t dc, __half *hi16, __half *lo16, int64_t *term, cudaStream_t st);
+bool coarse_tc_ok(uint32_t dc);
+int coarse_tc(const __half *ch, const __half *cl, const int64_t *cterm, uint32_t n, const __half *qh,
+              const __half *ql, const int64_t *qterm, uint32_t m, uint32_t dc, double step_sq,
+              float *out, uint32_t *timeouts, cudaStream_t st);
 extern std::atomic<uint32_t> g_candidate_cap;
 void timer_destroy(void *t);
 int timer_read(void *t, float *ms, uint32_t *passes);
@@ -99,10 +107,34 @@ int katoann_gpu_coarse(const katoann_gpu_index *ix, const uint8_t *d_qhi, const 
                        uint32_t *d_probed, katoann_stream_t stream) {
   if (!ix) return kato::invalid("null index");
   if (nprobe == 0 || nprobe > ix->nlist) return kato::invalid("need k >= 1 and 1 <= nprobe <= nlist");
-  int rc = kato::sq16_tiles(d_qhi, d_qlo, ix->d_chi, ix->d_clo, d_qnorm, ix->d_cnorm, ix->step_sq,
-                            nq, ix->nlist, ix->dc, ix->dc, ix->dc, d_dists, true, as_stream(stream));
+  const cudaStream_t st = as_stream(stream);
+  int rc;
+  if (ix->d_chi16 && ix->d_clo16 && ix->d_cterm && kato::coarse_tc_ok(ix->dc) && nq) {
+    // tensor cores: the queries' centred planes in stream-ordered scratch
+    const size_t plane = static_cast<size_t>(nq) * ix->dc * 2;
+    void *scratch = nullptr;
+    KATO_CUDA(cudaMallocAsync(&scratch, 2 * plane + static_cast<size_t>(nq) * 8 + 256, st));
+    auto *qh16 = static_cast<__half *>(scratch);
+    auto *ql16 = reinterpret_cast<__half *>(static_cast<unsigned char *>(scratch) + plane);
+    auto *qterm = reinterpret_cast<int64_t *>(static_cast<unsigned char *>(scratch) + 2 * plane);
+    auto *flag = reinterpret_cast<uint32_t *>(qterm + nq);
+    rc = cudaMemsetAsync(flag, 0, 4, st) != cudaSuccess ? KATO_ERUNTIME : KATO_OK;
+    if (!rc) rc = kato::centre_planes(d_qhi, d_qlo, d_qnorm, nq, ix->dc, qh16, ql16, qterm, st);
+    if (!rc)
+      rc = kato::coarse_tc(reinterpret_cast<const __half *>(ix->d_chi16),
+                           reinterpret_cast<const __half *>(ix->d_clo16), ix->d_cterm, ix->nlist,
+                           qh16, ql16, qterm, nq, ix->dc, ix->step_sq, d_dists, flag, st);
+    uint32_t timeouts = 0;
+    if (!rc && cudaMemcpyAsync(&timeouts, flag, 4, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+        cudaStreamSynchronize(st) == cudaSuccess && timeouts)
+      rc = kato::invalid("tensor-core coarse product: a bounded pipeline wait ran out");
+    cudaFreeAsync(scratch, st);
+  } else {
+    rc = kato::sq16_tiles(d_qhi, d_qlo, ix->d_chi, ix->d_clo, d_qnorm, ix->d_cnorm, ix->step_sq, nq,
+                          ix->nlist, ix->dc, ix->dc, ix->dc, d_dists, true, st);
+  }
   if (rc) return rc;
-  return kato::select_topp(d_dists, nq, ix->nlist, nprobe, d_probed, nullptr, as_stream(stream));
+  return kato::select_topp(d_dists, nq, ix->nlist, nprobe, d_probed, nullptr, st);
 }
 
 size_t katoann_gpu_search_workspace(const katoann_gpu_index *ix, uint32_t max_batch, uint32_t k,
@@ -140,6 +172,13 @@ int katoann_gpu_search_timed(const katoann_gpu_index *ix, const float *d_queries
 void *katoann_gpu_timer_create(uint32_t max_passes) { return kato::timer_create(max_passes); }
 
 uint32_t katoann_gpu_last_launches(void) { return kato::last_launches(); }
+
+int katoann_gpu_centre_planes(const uint8_t *d_hi, const uint8_t *d_lo, const int64_t *d_norm,
+                              uint32_t rows, uint32_t dc, uint16_t *d_hi16, uint16_t *d_lo16,
+                              int64_t *d_term, katoann_stream_t stream) {
+  return kato::centre_planes(d_hi, d_lo, d_norm, rows, dc, reinterpret_cast<__half *>(d_hi16),
+                             reinterpret_cast<__half *>(d_lo16), d_term, as_stream(stream));
+}
 
 int katoann_gpu_set_candidate_cap(uint32_t cap) {
   if (cap < 16 || cap > (1u << 20)) return kato::invalid("candidate buffer size must be in [16, 2^20]");

@@ -76,7 +76,7 @@ struct Index::State {
   float lo = 0;
   double inv_step = 0, step = 0, step_sq = 0;
   std::vector<uint32_t> sizes;
-  DevBuf rot, hi, lop, norm, hinorm, headnorm, ids, list_off, chi, clo, cnorm;
+  DevBuf rot, hi, lop, norm, hinorm, headnorm, ids, list_off, chi, clo, cnorm, chi16, clo16, cterm;
   katoann_gpu_index view{};
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
@@ -289,6 +289,13 @@ void Index::load_arrays(const IndexArrays &a, const LoadOptions &opt) {
     gpu_check(katoann_gpu_quantize_rows(cv, L, d, dc, s.lo, s.inv_step, 0, s.chi.as<uint8_t>(),
                                         s.clo.as<uint8_t>(), s.cnorm.as<int64_t>(),
                                         chn.as<int64_t>(), nullptr, ks));
+    // the same planes centred as fp16 for the tensor-core coarse product
+    s.chi16.alloc(static_cast<size_t>(L) * dc * 2);
+    s.clo16.alloc(static_cast<size_t>(L) * dc * 2);
+    s.cterm.alloc(static_cast<size_t>(L) * 8);
+    gpu_check(katoann_gpu_centre_planes(s.chi.as<uint8_t>(), s.clo.as<uint8_t>(),
+                                        s.cnorm.as<int64_t>(), L, dc, s.chi16.as<uint16_t>(),
+                                        s.clo16.as<uint16_t>(), s.cterm.as<int64_t>(), ks));
     cuda_check(cudaStreamSynchronize(s.stream), "load");
   }
   cuda_check(cudaStreamSynchronize(s.stream), "load");
@@ -316,6 +323,9 @@ void Index::load_arrays(const IndexArrays &a, const LoadOptions &opt) {
   v.d_chi = s.chi.as<uint8_t>();
   v.d_clo = s.clo.as<uint8_t>();
   v.d_cnorm = s.cnorm.as<int64_t>();
+  v.d_chi16 = s.chi16.as<uint16_t>();
+  v.d_clo16 = s.clo16.as<uint16_t>();
+  v.d_cterm = s.cterm.as<int64_t>();
   s_ = std::move(st);
 }
 
@@ -421,7 +431,8 @@ size_t Index::memory_bytes() const {
   if (!s_) return 0;
   const State &s = *s_;
   return s.rot.n + s.hi.n + s.lop.n + s.norm.n + s.hinorm.n + s.headnorm.n + s.ids.n +
-         s.list_off.n + s.chi.n + s.clo.n + s.cnorm.n + s.sizes.size() * 4;
+         s.list_off.n + s.chi.n + s.clo.n + s.cnorm.n + s.chi16.n + s.clo16.n + s.cterm.n +
+         s.sizes.size() * 4;
 }
 
 }  // namespace katoann

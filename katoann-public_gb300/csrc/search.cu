@@ -15,6 +15,8 @@
 #include <atomic>
 #include <vector>
 
+#include <cuda_fp16.h>
+
 #include "kcommon.cuh"
 #include "rank_tc.cuh"
 
@@ -617,6 +619,12 @@ int sq16_tiles(const uint8_t *qhi, const uint8_t *qlo, const uint8_t *xhi, const
                const int64_t *qn, const int64_t *xn, double step_sq, uint32_t m, uint32_t n,
                uint32_t dims, uint32_t qstride, uint32_t xstride, float *out, bool full,
                cudaStream_t st);
+int centre_planes(const uint8_t *hi, const uint8_t *lo, const int64_t *norm, uint32_t rows,
+                  uint32_t dc, __half *hi16, __half *lo16, int64_t *term, cudaStream_t st);
+bool coarse_tc_ok(uint32_t dc);
+int coarse_tc(const __half *ch, const __half *cl, const int64_t *cterm, uint32_t n, const __half *qh,
+              const __half *ql, const int64_t *qterm, uint32_t m, uint32_t dc, double step_sq,
+              float *out, uint32_t *timeouts, cudaStream_t st);
 int select_topp(const float *dists, uint32_t nq, uint32_t n, uint32_t p, uint32_t *probed,
                 unsigned long long *tie_count, cudaStream_t st);
 
@@ -635,12 +643,13 @@ struct Plan {
   int ranking;
   bool select;
   bool tc;                          // tensor-core ranking pass
+  bool coarse_tc;                   // tensor-core coarse product
   TcShape tcs;
   uint32_t tcitems, cap, seed_rows, ctas, rec_cap;
   size_t off_fq, off_qhi, off_qlo, off_qn, off_qhn, off_qh0, off_cd, off_probed, off_cnt, off_off,
       off_woff, off_cur, off_work, off_ent, off_slots, off_surv, off_nsurv, off_stats,
       off_tcscratch, off_tcitems, off_tileoff, off_nitems, off_qcount, off_qfill, off_bound,
-      off_rec, off_recn, off_rlist, off_rkey, off_rcount, total;
+      off_rec, off_recn, off_rlist, off_rkey, off_rcount, off_qh16, off_ql16, off_qterm, total;
 };
 
 static size_t align256(size_t x) { return (x + 255) / 256 * 256; }
@@ -715,6 +724,10 @@ int make_plan(const katoann_gpu_index *ix, uint32_t B, uint32_t k, uint32_t p, i
   pl.off_bound = take(static_cast<size_t>(B) * 4);
   pl.off_rec = take(pl.tc ? static_cast<size_t>(pl.ctas) * pl.rec_cap * 16 : 16);
   pl.off_recn = take(static_cast<size_t>(pl.ctas) * 4);
+  pl.coarse_tc = ix->d_chi16 && ix->d_clo16 && ix->d_cterm && coarse_tc_ok(ix->dc);
+  pl.off_qh16 = take(pl.coarse_tc ? static_cast<size_t>(B) * ix->dc * 2 : 16);
+  pl.off_ql16 = take(pl.coarse_tc ? static_cast<size_t>(B) * ix->dc * 2 : 16);
+  pl.off_qterm = take(static_cast<size_t>(B) * 8);
   pl.off_rlist = take(static_cast<size_t>(B) * 4);
   pl.off_rkey = take(static_cast<size_t>(B) * 8);
   pl.off_rcount = take(kRescanCounters * 4);
@@ -760,9 +773,21 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
   g_launches += (ix->rotated ? ((ix->dim & 3) ? 2 : 1) : 0) + 1 + 2;  // rotation, quantize, coarse, select
   mark(tm, 1, st);
   // 2. coarse product and top-nprobe (:846-877)
-  if ((rc = sq16_tiles(qhi, qlo, ix->d_chi, ix->d_clo, qn, ix->d_cnorm, ix->step_sq, nq, L, dc, dc,
-                       dc, cd, true, st)))
+  if (pl.coarse_tc) {
+    // fp16 tensor cores: the queries' centred planes, then the exact product
+    __half *qh16 = reinterpret_cast<__half *>(ws + pl.off_qh16);
+    __half *ql16 = reinterpret_cast<__half *>(ws + pl.off_ql16);
+    int64_t *qterm = reinterpret_cast<int64_t *>(ws + pl.off_qterm);
+    if ((rc = centre_planes(qhi, qlo, qn, nq, dc, qh16, ql16, qterm, st))) return rc;
+    if ((rc = coarse_tc(reinterpret_cast<const __half *>(ix->d_chi16),
+                        reinterpret_cast<const __half *>(ix->d_clo16), ix->d_cterm, L, qh16, ql16,
+                        qterm, nq, dc, ix->step_sq, cd, reinterpret_cast<uint32_t *>(stats + 3), st)))
+      return rc;
+    ++g_launches;
+  } else if ((rc = sq16_tiles(qhi, qlo, ix->d_chi, ix->d_clo, qn, ix->d_cnorm, ix->step_sq, nq, L,
+                              dc, dc, dc, cd, true, st))) {
     return rc;
+  }
   mark(tm, 2, st);
   if ((rc = select_topp(cd, nq, L, p, probed, stats + 0, st))) return rc;
   mark(tm, 3, st);

@@ -135,3 +135,33 @@ def test_coarse_probes_match_reference(torch, name):
     rows = np.arange(nq)[:, None]
     dd = d[rows, got]
     assert np.all((dd[:, 1:] > dd[:, :-1]) | ((dd[:, 1:] == dd[:, :-1]) & (got[:, 1:] > got[:, :-1])))
+
+
+@pytest.mark.parametrize("name", FIXTURES)
+def test_coarse_distances_match_oracle_on_both_paths(torch, name):
+    """The full query x centroid distance matrix, bit for bit, from the
+    tensor-core product and from the CUDA-core product (view without the
+    centred planes)."""
+    import ctypes as C
+    import katoann
+    from _gpu import GpuIndex
+    spec, z, prefix, queries = fixture(name)
+    idx = katoann.Index()
+    idx.load(prefix)
+    ref = oracle.OracleIndex(prefix)
+    q = ref.quantize(ref.rotate(queries))
+    cen = ref.centroid_codes()
+    want = oracle.sq16_l2(q["hi"], q["lo"], cen["hi"], cen["lo"], q["norm"], cen["norm"], ref.step_sq)
+    nq = len(queries)
+    qh, ql, qn = (torch.from_numpy(np.ascontiguousarray(q[k])).cuda() for k in ("hi", "lo", "norm"))
+    view = GpuIndex.from_address(idx.device_view)
+    plain = GpuIndex()
+    C.pointer(plain)[0] = view
+    plain.d_chi16 = plain.d_clo16 = plain.d_cterm = None
+    for v in (view, plain):
+        dists = torch.empty((nq, ref.nlist), dtype=torch.float32, device="cuda")
+        probed = torch.empty((nq, 1), dtype=torch.int32, device="cuda")
+        check(gpu().katoann_gpu_coarse(C.byref(v), dptr(qh), dptr(ql), dptr(qn), nq, 1, dptr(dists),
+                                       dptr(probed), None))
+        got = dists.cpu().numpy()
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), v.d_chi16
