@@ -183,11 +183,17 @@ int katoann_gpu_centre_planes(const uint8_t *d_hi, const uint8_t *d_lo, const in
 uint32_t katoann_gpu_last_launches(void);
 
 /* Entries per query of the tensor-core ranking pass's candidate buffer
- * (default 16384, range [16, 2^20]; process-wide, read when a workspace is
+ * (default 32768, range [16, 2^20]; process-wide, read when a workspace is
  * sized and at each search). Queries with more candidates than this are
  * rescanned exactly; searches with survivors above it use the CUDA-core pass.
  * Results do not depend on it. */
 int katoann_gpu_set_candidate_cap(uint32_t cap);
+
+/* Rows of each query's nearest lists that give it a bound before the
+ * tensor-core ranking pass (0 = the default, max(1024, 8 x survivors); at
+ * most 4096; process-wide). A tighter bound means fewer candidates to merge,
+ * a looser one less work up front. Results do not depend on it. */
+int katoann_gpu_set_seed_rows(uint32_t rows);
 
 /* katoann_gpu_search that also records phase events into `timer` (may be
  * NULL, then identical to katoann_gpu_search). */

@@ -47,6 +47,7 @@ int coarse_tc(const __half *ch, const __half *cl, const int64_t *cterm, uint32_t
               const __half *ql, const int64_t *qterm, uint32_t m, uint32_t dc, double step_sq,
               float *out, uint32_t *timeouts, cudaStream_t st);
 extern std::atomic<uint32_t> g_candidate_cap;
+extern std::atomic<uint32_t> g_seed_rows;
 void timer_destroy(void *t);
 int timer_read(void *t, float *ms, uint32_t *passes);
 size_t search_workspace(const katoann_gpu_index *ix, uint32_t max_batch, uint32_t k, uint32_t p,
@@ -178,6 +179,12 @@ int katoann_gpu_centre_planes(const uint8_t *d_hi, const uint8_t *d_lo, const in
                               int64_t *d_term, katoann_stream_t stream) {
   return kato::centre_planes(d_hi, d_lo, d_norm, rows, dc, reinterpret_cast<__half *>(d_hi16),
                              reinterpret_cast<__half *>(d_lo16), d_term, as_stream(stream));
+}
+
+int katoann_gpu_set_seed_rows(uint32_t rows) {
+  if (rows > 4096) return kato::invalid("seed rows must be at most 4096");
+  kato::g_seed_rows.store(rows);
+  return KATO_OK;
 }
 
 int katoann_gpu_set_candidate_cap(uint32_t cap) {

@@ -13,22 +13,23 @@
 //      128-row tiles is scored against the item's queries. One CTA per SM
 //      takes an equal share of all tiles and runs them through a pipeline of
 //      warp roles connected by mbarriers:
-//        - a TMA warp loads raw tiles of high bytes (128 rows x 128 bytes,
+//        - a TMA thread loads raw tiles of high bytes (128 rows x 128 bytes,
 //          128-byte swizzle) into a ring of stages;
 //        - two staging warps gather each item's query rows, re-centred to
 //          (byte - 128) as exact fp16, into a double-buffered B tile in the
-//          canonical K-major layout, plus a row of ones;
-//        - four converter warps (thread = row) re-centre the raw tiles to fp16
-//          into two A stages in the canonical K-major layout;
-//        - one MMA thread issues tcgen05.mma (M = 128 rows, N = queries + 16,
-//          K = 16) into double-buffered fp32 TMEM accumulators. Products are at
-//          most 128 * 128, so up to 1024 dimensions add up exactly; the column
-//          of ones gives each row's centred byte sum;
+//          canonical K-major layout, with each query's bound;
+//        - eight converter warps (two threads per row) re-centre the raw tiles
+//          to fp16 into two A stages in the canonical K-major layout and sum
+//          each row's centred norm xn';
+//        - one MMA thread issues tcgen05.mma (M = 128 rows, N queries, K = 16)
+//          into double-buffered fp32 TMEM accumulators. Products are at most
+//          128 * 128, so up to 1024 dimensions add up exactly;
 //        - eight epilogue warps (thread = row, each warpgroup half of the
-//          columns) form l2 = qn' + xn' - 2 dot' (translating both vectors by
-//          128 leaves every squared distance unchanged; xn' comes from the
-//          row's stored norm and its byte sum) and append the rows within the
-//          query's bound to its candidate buffer;
+//          columns) test l2 = qn' + xn' - 2 dot' against the query's bound
+//          (translating both vectors by 128 leaves every squared distance
+//          unchanged) and append passing (query, l2, row) records to the
+//          CTA's list; tc_bucket_kernel then sorts the records into per-query
+//          buffers with their float distances;
 //   3. a query whose buffer overflowed is rescanned exactly (rescan_*
 //      kernels), and the merge kernel takes the exact best S by (distance, id)
 //      from each buffer, so results never depend on the bound or the buffer
@@ -42,6 +43,7 @@
 
 #include "kcommon.cuh"
 #include "rank_tc.cuh"
+#include "scan.cuh"
 #include "tc.cuh"
 
 namespace kato {
@@ -514,6 +516,53 @@ __device__ __forceinline__ uint32_t row_dot(const uint8_t *row, const uint32_t *
   return dot;
 }
 
+// Dot products of a query (its h bytes as words in shared memory) with rows
+// r0 .. r0 + n - 1 of a byte plane, lanes split along each row: a group of
+// G = min(32, h / 16) lanes reads a row as one coalesced run of 16-byte
+// loads and sums over the group by shuffles. A warp takes 32 rows at a time
+// (G steps, all loads of the batch in flight together) and hands row
+// base + l of the batch to one lane, so f(i, dot) runs on all 32 lanes at
+// once. All threads of the CTA take part.
+template <uint32_t G, typename F>
+__device__ __forceinline__ void rows_split(const uint8_t *__restrict__ x, uint32_t dc, uint32_t h,
+                                           const uint32_t *qw, uint32_t r0, uint32_t n, F f) {
+  constexpr uint32_t RPW = 32 / G;  // rows per step
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const uint32_t sub = lane / G, gl = lane % G, cpl = (h / 16) / G;
+  for (uint32_t base = warp * 32; base < n; base += nw * 32) {
+    uint32_t mine = 0;
+#pragma unroll
+    for (uint32_t it = 0; it < G; ++it) {
+      const uint32_t i = base + it * RPW + sub;
+      uint32_t dot = 0;
+      if (i < n) {
+        const uint4 *rv = reinterpret_cast<const uint4 *>(x + static_cast<size_t>(r0 + i) * dc);
+        for (uint32_t c = 0; c < cpl; ++c) {
+          const uint32_t u = gl + c * G;
+          const uint4 v = __ldg(rv + u);
+          const uint32_t *w = qw + 4 * u;
+          dot = dp4(v.x, w[0], dp4(v.y, w[1], dp4(v.z, w[2], dp4(v.w, w[3], dot))));
+        }
+      }
+#pragma unroll
+      for (uint32_t o = G / 2; o; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
+      if (gl == it) mine = dot;
+    }
+    const uint32_t i = base + gl * RPW + sub;
+    if (i < n) f(i, mine);
+  }
+}
+
+template <typename F>
+__device__ __forceinline__ void for_rows_split(const uint8_t *__restrict__ x, uint32_t dc, uint32_t h,
+                                               const uint32_t *qw, uint32_t r0, uint32_t n, F f) {
+  const uint32_t g = min(32u, h / 16);
+  if (g == 16) rows_split<16>(x, dc, h, qw, r0, n, f);
+  else if (g == 32) rows_split<32>(x, dc, h, qw, r0, n, f);
+  else if (g == 8) rows_split<8>(x, dc, h, qw, r0, n, f);
+  else rows_split<4>(x, dc, h, qw, r0, n, f);
+}
+
 // ------------------------------------------------------------- seed bounds
 // One CTA per query: l2 of the first `want` rows of its probed lists (probe
 // order, nearest list first), the S-th smallest by 8-bit radix digits, then
@@ -537,10 +586,9 @@ __global__ void __launch_bounds__(256) rank_seed_kernel(
   for (uint32_t r = 0; r < p && count < want; ++r) {
     const uint32_t c = probed[static_cast<size_t>(q) * p + r];
     const uint32_t r0 = list_off[c], n = min(list_off[c + 1] - r0, kSeedCap - count);
-    for (uint32_t i = tid; i < n; i += blockDim.x) {
-      const uint32_t dot = row_dot(xhi + static_cast<size_t>(r0 + i) * dc, qw, h);
+    for_rows_split(xhi, dc, h, qw, r0, n, [&](uint32_t i, uint32_t dot) {
       l2s[count + i] = static_cast<int32_t>(qn + xnorm[r0 + i] - 2 * static_cast<int64_t>(dot));
-    }
+    });
     count += n;
   }
   __syncthreads();
@@ -644,7 +692,8 @@ __global__ void __launch_bounds__(256) rescan_bound_kernel(
   if (n <= cap) return;
   // entries actually in the buffer: the bucketing step's fill in round 0,
   // the previous round's count after that
-  const uint32_t valid = min(round == 0 ? qfill[q] : n, cap);
+  // (a subset's S-th smallest key is a bound as well: look at 2048 at most)
+  const uint32_t valid = min(min(round == 0 ? qfill[q] : n, cap), 2048u);
   const uint2 *buf = qbuf + static_cast<size_t>(q) * cap;
   const unsigned long long K =
       valid < S ? ~0ull
@@ -680,13 +729,18 @@ __global__ void __launch_bounds__(256) rescan_rows_kernel(
     const int64_t qn = qnorm[q];
     const unsigned long long K = kbound[q];
     uint2 *buf = qbuf + static_cast<size_t>(q) * cap;
-    for (uint32_t row = list_off[c] + threadIdx.x; row < list_off[c + 1]; row += blockDim.x) {
-      const unsigned long long k = key(row, qw, qn);
+    const uint32_t r0 = list_off[c];
+    for_rows_split(key.xhi, key.dc, key.h, qw, r0, list_off[c + 1] - r0, [&](uint32_t i, uint32_t dot) {
+      const uint32_t row = r0 + i;
+      const int64_t l2 = qn + key.xnorm[row] - 2 * static_cast<int64_t>(dot);
+      const unsigned long long k =
+          (static_cast<unsigned long long>(__float_as_uint(dist_value(l2, key.scale))) << 32) |
+          key.ids[row];
       if (k <= K) {
         const uint32_t at = atomicAdd(qcount + q, 1u);
         if (at < cap) buf[at] = make_uint2(static_cast<uint32_t>(k >> 32), row);
       }
-    }
+    });
   }
 }
 
@@ -755,36 +809,16 @@ __global__ void tc_count_kernel(const uint32_t *__restrict__ cnt, const uint32_t
 __global__ void __launch_bounds__(1024) tc_scan_kernel(uint32_t *__restrict__ counts, uint32_t L,
                                                        uint32_t *__restrict__ nitems,
                                                        uint32_t *__restrict__ tile_off) {
-  __shared__ uint32_t sa[1024], sb[1024];
   uint32_t *ca = counts, *cb = counts + L + 1;
-  const uint32_t t = threadIdx.x, per = (L + 1023) / 1024;
-  const uint32_t b = min(L, t * per), e = min(L, b + per);
-  uint32_t a1 = 0, a2 = 0;
-  for (uint32_t i = b; i < e; ++i) {
-    a1 += ca[i];
-    a2 += cb[i];
-  }
-  sa[t] = a1;
-  sb[t] = a2;
-  __syncthreads();
-  for (uint32_t o = 1; o < 1024; o <<= 1) {
-    const uint32_t v1 = t >= o ? sa[t - o] : 0, v2 = t >= o ? sb[t - o] : 0;
-    __syncthreads();
-    sa[t] += v1;
-    sb[t] += v2;
-    __syncthreads();
-  }
-  uint32_t r1 = sa[t] - a1, r2 = sb[t] - a2;
-  for (uint32_t i = b; i < e; ++i) {
-    const uint32_t v1 = ca[i], v2 = cb[i];
-    ca[i] = r1;
-    cb[i] = r2;
-    r1 += v1;
-    r2 += v2;
-  }
-  if (t == 1023) {
-    *nitems = sa[1023];
-    tile_off[sa[1023]] = sb[1023];
+  const uint2 tot = block_scan2(
+      L, [&](uint32_t i) { return make_uint2(ca[i], cb[i]); },
+      [&](uint32_t i, uint32_t a, uint32_t b) {
+        ca[i] = a;
+        cb[i] = b;
+      });
+  if (threadIdx.x == 0) {
+    *nitems = tot.x;
+    tile_off[tot.x] = tot.y;
   }
 }
 

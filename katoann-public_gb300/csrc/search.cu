@@ -19,12 +19,15 @@
 
 #include "kcommon.cuh"
 #include "rank_tc.cuh"
+#include "scan.cuh"
 
 namespace kato {
 
 thread_local uint32_t g_launches = 0;  // kernel launches of the last search pass
 // Entries per query of the tensor-core ranking pass's candidate buffer.
-std::atomic<uint32_t> g_candidate_cap{16384};
+std::atomic<uint32_t> g_candidate_cap{32768};
+// Rows a query's seed bound looks at (0: max(1024, 8 survivors)).
+std::atomic<uint32_t> g_seed_rows{0};
 
 namespace {
 
@@ -53,35 +56,20 @@ __global__ void __launch_bounds__(1024) scan_kernel(const uint32_t *__restrict__
                                                     uint32_t *__restrict__ off,
                                                     uint32_t *__restrict__ woff,
                                                     uint32_t *__restrict__ cursor) {
-  __shared__ uint32_t s1[1024], s2[1024];
-  const uint32_t t = threadIdx.x, per = (L + 1023) / 1024;
-  const uint32_t b = min(L, t * per), e = min(L, b + per);
-  uint32_t a1 = 0, a2 = 0;
-  for (uint32_t c = b; c < e; ++c) {
-    a1 += cnt[c];
-    a2 += (cnt[c] + kQG - 1) / kQG;
-  }
-  s1[t] = a1;
-  s2[t] = a2;
-  __syncthreads();
-  for (uint32_t o = 1; o < 1024; o <<= 1) {
-    const uint32_t v1 = t >= o ? s1[t - o] : 0, v2 = t >= o ? s2[t - o] : 0;
-    __syncthreads();
-    s1[t] += v1;
-    s2[t] += v2;
-    __syncthreads();
-  }
-  uint32_t r1 = s1[t] - a1, r2 = s2[t] - a2;
-  for (uint32_t c = b; c < e; ++c) {
-    off[c] = r1;
-    woff[c] = r2;
-    cursor[c] = 0;
-    r1 += cnt[c];
-    r2 += (cnt[c] + kQG - 1) / kQG;
-  }
-  if (t == 1023) {
-    off[L] = s1[1023];
-    woff[L] = s2[1023];
+  const uint2 tot = block_scan2(
+      L,
+      [&](uint32_t c) {
+        const uint32_t v = cnt[c];
+        return make_uint2(v, (v + kQG - 1) / kQG);
+      },
+      [&](uint32_t c, uint32_t a, uint32_t b) {
+        off[c] = a;
+        woff[c] = b;
+        cursor[c] = 0;
+      });
+  if (threadIdx.x == 0) {
+    off[L] = tot.x;
+    woff[L] = tot.y;
   }
 }
 
@@ -682,7 +670,8 @@ int make_plan(const katoann_gpu_index *ix, uint32_t B, uint32_t k, uint32_t p, i
   if (pl.tc) {
     pl.select = true;
     pl.SC = pl.S;
-    pl.seed_rows = std::max(1024u, 8 * pl.S);
+    const uint32_t sr = g_seed_rows.load();
+    pl.seed_rows = sr ? std::max(sr, pl.S) : std::max(1024u, 8 * pl.S);
     pl.tcitems = static_cast<uint32_t>(bp / pl.tcs.N + std::min<size_t>(L, bp) + 1);
     // candidate records per CTA: room for 32 S per query of the batch, spread
     // over the CTAs (a CTA that runs out flags the queries it drops)

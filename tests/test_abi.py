@@ -102,4 +102,12 @@ def test_candidate_cap_range_is_checked():
     assert lib.katoann_gpu_set_candidate_cap(8) == -1
     assert lib.katoann_gpu_set_candidate_cap(1 << 21) == -1
     assert b"candidate buffer" in lib.katoann_gpu_last_error()
-    assert lib.katoann_gpu_set_candidate_cap(16384) == 0
+    assert lib.katoann_gpu_set_candidate_cap(32768) == 0
+
+
+def test_seed_rows_range_is_checked():
+    from _gpu import gpu
+    lib = gpu()
+    assert lib.katoann_gpu_set_seed_rows(5000) == -1
+    assert b"seed rows" in lib.katoann_gpu_last_error()
+    assert lib.katoann_gpu_set_seed_rows(0) == 0

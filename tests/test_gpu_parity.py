@@ -172,4 +172,4 @@ def test_candidate_buffer_overflow_is_rescanned_exactly(tmp_path):
             assert np.array_equal(ids, rid) and np.array_equal(dists, rd), (cap, ranking)
             assert stats["ranking_rescans"] > 0 and stats["ranking_timeouts"] == 0, (cap, stats)
     finally:
-        assert lib.katoann_gpu_set_candidate_cap(16384) == 0
+        assert lib.katoann_gpu_set_candidate_cap(32768) == 0
