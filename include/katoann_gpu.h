@@ -216,7 +216,10 @@ int katoann_gpu_search_timed(const katoann_gpu_index *index, const float *d_quer
  * thread of each role): converters waiting for raw tiles, for free A stages,
  * total; MMA waiting for query tiles, free accumulators, converted tiles,
  * total; epilogue waiting for query tiles, accumulators, total; TMA waiting
- * for free stages, total; query staging waiting for free query tiles, total. */
+ * for free stages, total; query staging waiting for free query tiles, total;
+ * [32..38] the same for the tensor-core coarse product: TMA waiting for free
+ * stages, total; MMA waiting for accumulators, for stages, total; first
+ * epilogue warp waiting for accumulators, total. */
 int katoann_gpu_workspace_stats(const void *d_ws, uint64_t *h_stats, uint32_t n,
                                 katoann_stream_t stream);
 

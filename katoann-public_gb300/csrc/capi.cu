@@ -45,7 +45,7 @@ int centre_planes(const uint8_t *hi, const uint8_t *lo, const int64_t *norm, uin
 bool coarse_tc_ok(uint32_t dc);
 int coarse_tc(const __half *ch, const __half *cl, const int64_t *cterm, uint32_t n, const __half *qh,
               const __half *ql, const int64_t *qterm, uint32_t m, uint32_t dc, double step_sq,
-              float *out, uint32_t *timeouts, cudaStream_t st);
+              float *out, uint32_t *timeouts, unsigned long long *prof, cudaStream_t st);
 extern std::atomic<uint32_t> g_candidate_cap;
 extern std::atomic<uint32_t> g_seed_rows;
 void timer_destroy(void *t);
@@ -124,7 +124,7 @@ int katoann_gpu_coarse(const katoann_gpu_index *ix, const uint8_t *d_qhi, const 
     if (!rc)
       rc = kato::coarse_tc(reinterpret_cast<const __half *>(ix->d_chi16),
                            reinterpret_cast<const __half *>(ix->d_clo16), ix->d_cterm, ix->nlist,
-                           qh16, ql16, qterm, nq, ix->dc, ix->step_sq, d_dists, flag, st);
+                           qh16, ql16, qterm, nq, ix->dc, ix->step_sq, d_dists, flag, nullptr, st);
     uint32_t timeouts = 0;
     if (!rc && cudaMemcpyAsync(&timeouts, flag, 4, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
         cudaStreamSynchronize(st) == cudaSuccess && timeouts)
@@ -202,7 +202,7 @@ int katoann_gpu_timer_read(void *timer, float *h_ms, uint32_t *passes) {
 
 int katoann_gpu_workspace_stats(const void *d_ws, uint64_t *h_stats, uint32_t n,
                                 katoann_stream_t stream) {
-  if (n > 32) return kato::invalid("at most 32 statistics");
+  if (n > 48) return kato::invalid("at most 48 statistics");
   KATO_CUDA(cudaMemcpyAsync(h_stats, d_ws, n * sizeof(uint64_t), cudaMemcpyDeviceToHost,
                             as_stream(stream)));
   KATO_CUDA(cudaStreamSynchronize(as_stream(stream)));

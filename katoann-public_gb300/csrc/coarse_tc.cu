@@ -91,7 +91,16 @@ struct CoarseArgs {
   uint32_t m, n, dc;
   DistScale scale;
   uint32_t *timeouts;
+  unsigned long long *prof;  // optional: TMA wait/total, MMA waits/total, epilogue wait/total
 };
+
+__device__ __forceinline__ bool cwait(uint64_t *b, uint32_t ph, volatile uint32_t *err,
+                                      unsigned long long &acc) {
+  const long long t = clock64();
+  const bool ok = tc::mbar_wait_or(b, ph, err);
+  acc += clock64() - t;
+  return ok;
+}
 
 __global__ void __launch_bounds__(kThreads, 1)
     coarse_tc_kernel(const __grid_constant__ CUtensorMap tch, const __grid_constant__ CUtensorMap tcl,
@@ -126,6 +135,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   const uint32_t tmem = *tbase;
   const uint32_t nct = (A.n + kCM - 1) / kCM, nqt = (A.m + kQN - 1) / kQN;
   const uint32_t ntiles = nct * nqt, nk = A.dc / kBK;
+  unsigned long long pw[2] = {0, 0};
+  const long long tstart = clock64();
 
   if (warp == 0) {
     // ---- TMA producer
@@ -135,7 +146,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int32_t c0 = static_cast<int32_t>((t % nct) * kCM), q0 = static_cast<int32_t>((t / nct) * kQN);
         bool ok = true;
         for (uint32_t k = 0; k < nk; ++k) {
-          if (!tc::mbar_wait_or(empty + s, ph ^ 1, err)) {
+          if (!cwait(empty + s, ph ^ 1, err, pw[0])) {
             ok = false;
             break;
           }
@@ -164,11 +175,11 @@ __global__ void __launch_bounds__(kThreads, 1)
       uint32_t s = 0, ph = 0, ab = 0, abph = 0;
       bool ok = true;
       for (uint32_t t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
-        if (!tc::mbar_wait_or(acc_empty + ab, abph ^ 1, err)) break;
+        if (!cwait(acc_empty + ab, abph ^ 1, err, pw[0])) break;
         tc::fence_after();
         const uint32_t d0 = tmem + ab * kAccCols;
         for (uint32_t k = 0; k < nk; ++k) {
-          if (!tc::mbar_wait_or(full + s, ph, err)) {
+          if (!cwait(full + s, ph, err, pw[1])) {
             ok = false;
             break;
           }
@@ -205,7 +216,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
       const uint32_t c = (t % nct) * kCM + row, qb = (t / nct) * kQN + half * 32;
       const int64_t ct = c < A.n ? A.cterm[c] : 0;
-      if (!__all_sync(0xffffffffu, tc::mbar_wait_or(acc_full + ab, abph, err))) break;
+      if (!__all_sync(0xffffffffu, cwait(acc_full + ab, abph, err, pw[0]))) break;
       tc::fence_after();
       const uint32_t taddr = tmem + ((q4 * 32u) << 16) + ab * kAccCols + half * 32;
       // the group loop stays rolled (code size); the 16 columns of a group unroll
@@ -233,6 +244,14 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (lane == 0) tc::mbar_arrive(acc_empty + ab);
       if (++ab == 2) ab = 0, abph ^= 1;
     }
+  }
+  if (A.prof && lane == 0 && warp <= 2) {
+    // slots: TMA wait, total; MMA wait for accumulators, for stages, total;
+    // first epilogue warp wait, total
+    const int base = warp == 0 ? 0 : warp == 1 ? 2 : 5;
+    const int nw = warp == 1 ? 2 : 1;
+    for (int i = 0; i < nw; ++i) atomicAdd(A.prof + base + i, pw[i]);
+    atomicAdd(A.prof + base + nw, static_cast<unsigned long long>(clock64() - tstart));
   }
   tc::fence_before();
   __syncthreads();
@@ -282,7 +301,7 @@ bool coarse_tc_ok(uint32_t dc) { return dc >= kBK && dc % kBK == 0 && dc <= 1024
 
 int coarse_tc(const __half *ch, const __half *cl, const int64_t *cterm, uint32_t n, const __half *qh,
               const __half *ql, const int64_t *qterm, uint32_t m, uint32_t dc, double step_sq,
-              float *out, uint32_t *timeouts, cudaStream_t st) {
+              float *out, uint32_t *timeouts, unsigned long long *prof, cudaStream_t st) {
   if (m == 0 || n == 0) return KATO_OK;
   if (!coarse_tc_ok(dc)) return invalid("the tensor-core coarse product needs dc in [64, 1024], a multiple of 64");
   CUtensorMap mch, mcl, mqh, mql;
@@ -298,7 +317,7 @@ int coarse_tc(const __half *ch, const __half *cl, const int64_t *cterm, uint32_t
     KATO_CUDA(cudaFuncSetAttribute(coarse_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(kSmem)));
   }
-  const CoarseArgs A{cterm, qterm, out, m, n, dc, make_dist_scale(step_sq), timeouts};
+  const CoarseArgs A{cterm, qterm, out, m, n, dc, make_dist_scale(step_sq), timeouts, prof};
   const uint32_t ntiles = div_up(n, kCM) * div_up(m, kQN);
   coarse_tc_kernel<<<std::min<uint32_t>(ntiles, sms), kThreads, kSmem, st>>>(mch, mcl, mqh, mql, A);
   KATO_LAUNCHED("coarse_tc_kernel");

@@ -68,7 +68,14 @@ KATO_HD float bits_to_float(uint32_t b) {
 #endif
 }
 
-KATO_HD float dist_value_slow(int64_t l2, const DistScale &s) {
+// The double-precision path, for the rare values outside the fast path's
+// range. Kept out of line on the GPU so that callers never evaluate it
+// speculatively (GB300's FP64 pipe is narrow).
+#if defined(__CUDACC__)
+static __host__ __device__ __noinline__ float dist_value_slow(int64_t l2, DistScale s) {
+#else
+static inline float dist_value_slow(int64_t l2, DistScale s) {
+#endif
   return static_cast<float>(static_cast<double>(l2) * s.step_sq);
 }
 

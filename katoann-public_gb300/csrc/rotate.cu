@@ -21,7 +21,8 @@ namespace {
 constexpr int kRotRows = 32;     // output rows per CTA
 constexpr int kRotCols = 32;     // output columns per CTA
 constexpr int kRotK = 64;        // k-chunk staged in shared memory
-constexpr int kRotStride = 66;   // floats per staged row (66 = 2 mod 4: no bank conflicts)
+constexpr int kRotStride = 36;   // floats per staged k (rows/columns 0..31 + pad: 16-byte
+                                 // aligned and conflict-free for 128-bit reads)
 
 // Scalar tail of one output: dimensions [k0, d), the first ((d - k0) & ~3) of
 // them with rounded products, the rest fused.
@@ -34,12 +35,39 @@ __device__ __forceinline__ float rot_tail(float s, const float *x, const float *
   return s;
 }
 
-__global__ void __launch_bounds__(256) rotate_lanes_kernel(const float *__restrict__ in,
-                                                           uint32_t nrows, uint32_t d,
-                                                           const float *__restrict__ rot,
-                                                           float *__restrict__ out) {
-  __shared__ float xs[kRotRows * kRotStride];
-  __shared__ float rs[kRotCols * kRotStride];
+// 4-byte asynchronous global -> shared copy; src_bytes 0 writes a zero.
+__device__ __forceinline__ void cp_async4(float *dst, const float *src, uint32_t src_bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(
+                   static_cast<uint32_t>(__cvta_generic_to_shared(dst))),
+               "l"(src), "r"(src_bytes)
+               : "memory");
+}
+
+// 16-byte asynchronous global -> shared copy (L2 only).
+__device__ __forceinline__ void cp_async16(float *dst, const float *src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                   static_cast<uint32_t>(__cvta_generic_to_shared(dst))),
+               "l"(src)
+               : "memory");
+}
+
+// kMajor: the staged parts are read from k-major copies xt (d x ldx, rows
+// zero-padded to ldx) and rt (d x ldr, columns zero-padded), 16 bytes per
+// copy; otherwise from the row-major inputs, 4 bytes per copy.
+template <bool kMajor>
+__global__ void __launch_bounds__(256, 2) rotate_lanes_kernel(const float *__restrict__ in,
+                                                              uint32_t nrows, uint32_t d,
+                                                              const float *__restrict__ rot,
+                                                              const float *__restrict__ xt,
+                                                              uint32_t ldx,
+                                                              const float *__restrict__ rt,
+                                                              uint32_t ldr,
+                                                              float *__restrict__ out) {
+  // two stages, each staged k-major (xs[k][row], rs[k][column]) so that a
+  // thread reads its 8 rows and 8 columns at one k with four 128-bit loads;
+  // the next chunk is copied asynchronously while the current one is used
+  __shared__ __align__(16) float xs[2][kRotK * kRotStride];
+  __shared__ __align__(16) float rs[2][kRotK * kRotStride];
   const uint32_t d4 = d & ~3u, d16 = d & ~15u;
   const uint32_t i0 = blockIdx.x * kRotRows, j0 = blockIdx.y * kRotCols;
   const int t = threadIdx.x, l = t & 15, g = t >> 4;
@@ -50,28 +78,55 @@ __global__ void __launch_bounds__(256) rotate_lanes_kernel(const float *__restri
 #pragma unroll
     for (int b = 0; b < 8; ++b) acc[a][b] = 0.0f;
 
-  for (uint32_t k0 = 0; k0 < d16; k0 += kRotK) {
+  auto stage = [&](uint32_t k0, int buf) {
+    if constexpr (kMajor) {
+      // per k: 32 rows (8 copies) of x and 32 columns of r
+      const uint32_t kn = min(static_cast<uint32_t>(kRotK), d16 - k0);
+      for (uint32_t idx = t; idx < kn * 8; idx += 256) {
+        const uint32_t c = idx >> 3, q = (idx & 7) * 4;
+        cp_async16(&xs[buf][c * kRotStride + q], xt + static_cast<size_t>(k0 + c) * ldx + i0 + q);
+        cp_async16(&rs[buf][c * kRotStride + q], rt + static_cast<size_t>(k0 + c) * ldr + j0 + q);
+      }
+      asm volatile("cp.async.commit_group;" ::: "memory");
+      return;
+    }
     for (int idx = t; idx < kRotRows * kRotK; idx += 256) {
       const int r = idx / kRotK, c = idx % kRotK;
       const uint32_t gk = k0 + c;
       const uint32_t gi = i0 + r, gj = j0 + r;
-      xs[r * kRotStride + c] = (gi < nrows && gk < d16) ? in[static_cast<size_t>(gi) * d + gk] : 0.0f;
-      rs[r * kRotStride + c] = (gj < d4 && gk < d16) ? rot[static_cast<size_t>(gj) * d + gk] : 0.0f;
+      const bool okx = gi < nrows && gk < d16, okr = gj < d4 && gk < d16;
+      cp_async4(&xs[buf][c * kRotStride + r], okx ? in + static_cast<size_t>(gi) * d + gk : in,
+                okx ? 4u : 0u);
+      cp_async4(&rs[buf][c * kRotStride + r], okr ? rot + static_cast<size_t>(gj) * d + gk : rot,
+                okr ? 4u : 0u);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  int buf = 0;
+  if (d16) stage(0, 0);
+  for (uint32_t k0 = 0; k0 < d16; k0 += kRotK, buf ^= 1) {
+    if (k0 + kRotK < d16) {
+      stage(k0 + kRotK, buf ^ 1);
+      asm volatile("cp.async.wait_group 1;" ::: "memory");
+    } else {
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
     }
     __syncthreads();
     const uint32_t kend = min(static_cast<uint32_t>(kRotK), d16 - k0);
     for (uint32_t c = 0; c < kend; c += 16) {
-      float xv[8], rv[8];
-#pragma unroll
-      for (int a = 0; a < 8; ++a) xv[a] = xs[(rb + a) * kRotStride + c + l];
-#pragma unroll
-      for (int b = 0; b < 8; ++b) rv[b] = rs[(cb + b) * kRotStride + c + l];
+      const float *xk = xs[buf] + (c + l) * kRotStride, *rk = rs[buf] + (c + l) * kRotStride;
+      const float4 x0 = *reinterpret_cast<const float4 *>(xk + rb);
+      const float4 x1 = *reinterpret_cast<const float4 *>(xk + rb + 4);
+      const float4 r0 = *reinterpret_cast<const float4 *>(rk + cb);
+      const float4 r1 = *reinterpret_cast<const float4 *>(rk + cb + 4);
+      const float xv[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+      const float rv[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
 #pragma unroll
       for (int a = 0; a < 8; ++a)
 #pragma unroll
         for (int b = 0; b < 8; ++b) acc[a][b] = __fmaf_rn(xv[a], rv[b], acc[a][b]);
     }
-    __syncthreads();
+    __syncthreads();  // the buffer is refilled by the next iteration's copies
   }
   // Lane reduction in the order of the reference's horizontal add.
 #pragma unroll
@@ -97,6 +152,25 @@ __global__ void __launch_bounds__(256) rotate_lanes_kernel(const float *__restri
       const float *r = rot + static_cast<size_t>(j) * d;
       out[static_cast<size_t>(i) * d + j] = rot_tail(acc[a][b], x, r, d16, d);
     }
+}
+
+// out[k * ld + r] = in[r * d + k] for r < rows (zero for rows <= r < ld),
+// k < kn: 32 x 32 tiles through shared memory.
+__global__ void __launch_bounds__(256) transpose_pad_kernel(const float *__restrict__ in,
+                                                            uint32_t rows, uint32_t d, uint32_t kn,
+                                                            float *__restrict__ out, uint32_t ld) {
+  __shared__ float tile[32][33];
+  const uint32_t r0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  const uint32_t tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (uint32_t y = ty; y < 32; y += 8) {
+    const uint32_t r = r0 + y, k = k0 + tx;
+    tile[y][tx] = (r < rows && k < kn) ? in[static_cast<size_t>(r) * d + k] : 0.0f;
+  }
+  __syncthreads();
+  for (uint32_t y = ty; y < 32; y += 8) {
+    const uint32_t k = k0 + y, r = r0 + tx;
+    if (k < kn && r < ld) out[static_cast<size_t>(k) * ld + r] = tile[tx][y];
+  }
 }
 
 // The last d % 4 output columns: one chain over all d dimensions
@@ -181,9 +255,36 @@ int rotate_rows(const float *in, uint32_t nrows, uint32_t d, const float *rot, f
   const uint32_t d4 = d & ~3u;
   if (d4) {
     dim3 grid(div_up(nrows, kRotRows), div_up(d4, kRotCols));
-    rotate_lanes_kernel<<<grid, 256, 0, st>>>(in, nrows, d, rot, out);
+    rotate_lanes_kernel<false><<<grid, 256, 0, st>>>(in, nrows, d, rot, nullptr, 0, nullptr, 0, out);
     KATO_LAUNCHED("rotate_lanes_kernel");
   }
+  if (d4 < d) {
+    const uint64_t n = static_cast<uint64_t>(nrows) * (d - d4);
+    rotate_seq_kernel<<<static_cast<uint32_t>((n + 255) / 256), 256, 0, st>>>(in, nrows, d, rot, out);
+    KATO_LAUNCHED("rotate_seq_kernel");
+  }
+  return KATO_OK;
+}
+
+size_t rotate_scratch_bytes(uint32_t nrows, uint32_t d) {
+  const size_t ldx = (static_cast<size_t>(nrows) + 31) / 32 * 32;
+  const size_t ldr = (static_cast<size_t>(d & ~3u) + 31) / 32 * 32;
+  return (ldx + ldr) * (d & ~15u) * 4 + 256;
+}
+
+int rotate_rows_kmajor(const float *in, uint32_t nrows, uint32_t d, const float *rot, void *scratch,
+                       float *out, cudaStream_t st) {
+  if (nrows == 0) return KATO_OK;
+  const uint32_t d4 = d & ~3u, d16 = d & ~15u;
+  if (d16 == 0) return rotate_rows(in, nrows, d, rot, out, st);
+  const uint32_t ldx = div_up(nrows, 32) * 32, ldr = div_up(d4, 32) * 32;
+  float *xt = static_cast<float *>(scratch);
+  float *rt = xt + static_cast<size_t>(ldx) * d16;
+  transpose_pad_kernel<<<dim3(ldx / 32, div_up(d16, 32)), 256, 0, st>>>(in, nrows, d, d16, xt, ldx);
+  transpose_pad_kernel<<<dim3(ldr / 32, div_up(d16, 32)), 256, 0, st>>>(rot, d4, d, d16, rt, ldr);
+  dim3 grid(div_up(nrows, kRotRows), div_up(d4, kRotCols));
+  rotate_lanes_kernel<true><<<grid, 256, 0, st>>>(in, nrows, d, rot, xt, ldx, rt, ldr, out);
+  KATO_LAUNCHED("rotate_lanes_kernel");
   if (d4 < d) {
     const uint64_t n = static_cast<uint64_t>(nrows) * (d - d4);
     rotate_seq_kernel<<<static_cast<uint32_t>((n + 255) / 256), 256, 0, st>>>(in, nrows, d, rot, out);

@@ -612,7 +612,10 @@ int centre_planes(const uint8_t *hi, const uint8_t *lo, const int64_t *norm, uin
 bool coarse_tc_ok(uint32_t dc);
 int coarse_tc(const __half *ch, const __half *cl, const int64_t *cterm, uint32_t n, const __half *qh,
               const __half *ql, const int64_t *qterm, uint32_t m, uint32_t dc, double step_sq,
-              float *out, uint32_t *timeouts, cudaStream_t st);
+              float *out, uint32_t *timeouts, unsigned long long *prof, cudaStream_t st);
+size_t rotate_scratch_bytes(uint32_t nrows, uint32_t d);
+int rotate_rows_kmajor(const float *in, uint32_t nrows, uint32_t d, const float *rot, void *scratch,
+                       float *out, cudaStream_t st);
 int select_topp(const float *dists, uint32_t nq, uint32_t n, uint32_t p, uint32_t *probed,
                 unsigned long long *tie_count, cudaStream_t st);
 
@@ -637,7 +640,8 @@ struct Plan {
   size_t off_fq, off_qhi, off_qlo, off_qn, off_qhn, off_qh0, off_cd, off_probed, off_cnt, off_off,
       off_woff, off_cur, off_work, off_ent, off_slots, off_surv, off_nsurv, off_stats,
       off_tcscratch, off_tcitems, off_tileoff, off_nitems, off_qcount, off_qfill, off_bound,
-      off_rec, off_recn, off_rlist, off_rkey, off_rcount, off_qh16, off_ql16, off_qterm, total;
+      off_rec, off_recn, off_rlist, off_rkey, off_rcount, off_qh16, off_ql16, off_qterm, off_rot,
+      total;
 };
 
 static size_t align256(size_t x) { return (x + 255) / 256 * 256; }
@@ -688,7 +692,7 @@ int make_plan(const katoann_gpu_index *ix, uint32_t B, uint32_t k, uint32_t p, i
     o += align256(bytes);
     return at;
   };
-  pl.off_stats = take(32 * sizeof(unsigned long long));
+  pl.off_stats = take(48 * sizeof(unsigned long long));
   pl.off_fq = take(static_cast<size_t>(B) * ix->dim * 4);
   pl.off_qhi = take(static_cast<size_t>(B) * ix->dc);
   pl.off_qlo = take(static_cast<size_t>(B) * ix->dc);
@@ -717,6 +721,7 @@ int make_plan(const katoann_gpu_index *ix, uint32_t B, uint32_t k, uint32_t p, i
   pl.off_qh16 = take(pl.coarse_tc ? static_cast<size_t>(B) * ix->dc * 2 : 16);
   pl.off_ql16 = take(pl.coarse_tc ? static_cast<size_t>(B) * ix->dc * 2 : 16);
   pl.off_qterm = take(static_cast<size_t>(B) * 8);
+  pl.off_rot = take(ix->rotated ? rotate_scratch_bytes(B, ix->dim) : 16);
   pl.off_rlist = take(static_cast<size_t>(B) * 4);
   pl.off_rkey = take(static_cast<size_t>(B) * 8);
   pl.off_rcount = take(kRescanCounters * 4);
@@ -753,13 +758,15 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
   // 1. rotation and quantization of the queries (src/index.cpp:895-899, :917-943)
   const float *src = queries;
   if (ix->rotated) {
-    if ((rc = rotate_rows(queries, nq, ix->dim, ix->d_rotation, fq, st))) return rc;
+    if ((rc = rotate_rows_kmajor(queries, nq, ix->dim, ix->d_rotation, ws + pl.off_rot, fq, st)))
+      return rc;
     src = fq;
   }
   if ((rc = quantize_rows(src, nq, ix->dim, dc, ix->lo, ix->inv_step, ix->head_dims, qhi, qlo, qn,
                           qhn, qh0, st)))
     return rc;
-  g_launches += (ix->rotated ? ((ix->dim & 3) ? 2 : 1) : 0) + 1 + 2;  // rotation, quantize, coarse, select
+  // rotation (two transposes and the product, plus the d % 4 columns), quantize, coarse, select
+  g_launches += (ix->rotated ? ((ix->dim & ~15u) ? 3 : 1) + ((ix->dim & 3) ? 1 : 0) : 0) + 1 + 2;
   mark(tm, 1, st);
   // 2. coarse product and top-nprobe (:846-877)
   if (pl.coarse_tc) {
@@ -770,7 +777,8 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
     if ((rc = centre_planes(qhi, qlo, qn, nq, dc, qh16, ql16, qterm, st))) return rc;
     if ((rc = coarse_tc(reinterpret_cast<const __half *>(ix->d_chi16),
                         reinterpret_cast<const __half *>(ix->d_clo16), ix->d_cterm, L, qh16, ql16,
-                        qterm, nq, dc, ix->step_sq, cd, reinterpret_cast<uint32_t *>(stats + 3), st)))
+                        qterm, nq, dc, ix->step_sq, cd, reinterpret_cast<uint32_t *>(stats + 3),
+                        stats + 32, st)))
       return rc;
     ++g_launches;
   } else if ((rc = sq16_tiles(qhi, qlo, ix->d_chi, ix->d_clo, qn, ix->d_cnorm, ix->step_sq, nq, L,
@@ -932,7 +940,7 @@ int search(const katoann_gpu_index *ix, const float *queries, uint32_t nq, uint3
     return KATO_ENOMEM;
   }
   unsigned char *w = static_cast<unsigned char *>(ws);
-  KATO_CUDA(cudaMemsetAsync(w + pl.off_stats, 0, 32 * sizeof(unsigned long long), st));
+  KATO_CUDA(cudaMemsetAsync(w + pl.off_stats, 0, 48 * sizeof(unsigned long long), st));
   g_launches = 0;
   for (uint32_t q0 = 0; q0 < nq; q0 += max_batch) {
     const uint32_t b = std::min(max_batch, nq - q0);

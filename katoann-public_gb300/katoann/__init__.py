@@ -266,8 +266,8 @@ class Index:
 
     def search_stats(self) -> dict:
         """Diagnostics of the last search (see katoann_gpu_workspace_stats)."""
-        s = np.zeros(30, np.uint64)
-        _check(_lib.katoann_index_stats(self._h, _ptr(s), 30))
+        s = np.zeros(39, np.uint64)
+        _check(_lib.katoann_index_stats(self._h, _ptr(s), 39))
         return dict(coarse_boundary_ties=int(s[0]), survivor_boundary_ties=int(s[1]),
                     ranking_timeouts=int(s[3]), ranking_tiles=int(s[4]),
                     ranking_candidates=int(s[5]), ranking_rescans=int(s[6]),
@@ -276,7 +276,10 @@ class Index:
                         ("conv_wait_raw", "conv_wait_a", "conv_total", "mma_wait_b", "mma_wait_acc",
                          "mma_wait_a", "mma_total", "epi_wait_b", "epi_wait_acc", "epi_total",
                          "tma_wait_stage", "tma_total", "stage_wait_b", "stage_total"),
-                        (int(v) for v in s[16:30]))))
+                        (int(v) for v in s[16:30]))),
+                    coarse_role_cycles=dict(zip(
+                        ("tma_wait", "tma_total", "mma_wait_acc", "mma_wait_stage", "mma_total",
+                         "epi_wait", "epi_total"), (int(v) for v in s[32:39]))))
 
     def _info(self):
         info = np.zeros(8, np.uint32)
