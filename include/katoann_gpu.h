@@ -217,6 +217,7 @@ int katoann_gpu_search_timed(const katoann_gpu_index *index, const float *d_quer
  * total; MMA waiting for query tiles, free accumulators, converted tiles,
  * total; epilogue waiting for query tiles, accumulators, total; TMA waiting
  * for free stages, total; query staging waiting for free query tiles, total;
+ * [30] cycles the ranking pass's MMA thread spent issuing MMAs and commits;
  * [32..38] the same for the tensor-core coarse product: TMA waiting for free
  * stages, total; MMA waiting for accumulators, for stages, total; first
  * epilogue warp waiting for accumulators, total. */

@@ -371,6 +371,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       if (lane == 0) {
         const uint32_t idesc = tc::idesc_f16(kTcRows, N);
         uint32_t as = 0, aph = 0, ab = 0, abph = 0, ib = 0, bph = 0;
+        unsigned long long pi = 0;  // cycles issuing MMAs and commits
         bool ok = true;
         for (; ok && w.t < t1; ++w.t) {
           w.step();
@@ -384,6 +385,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
               break;
             }
             tc::fence_after();
+            const long long ti = clock64();
             // descriptors of the chunk's first K step; each further step of
             // 16 dimensions advances A by 256 bytes and B by 256 bytes (two
             // core matrices), i.e. the encoded start address by 16
@@ -395,6 +397,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             for (uint32_t s = 0; s < 8; ++s)
               if (s < steps) tc::mma_f16(dcol, ad0 + 16 * s, bd0 + 16 * s, idesc, (kc | s) != 0);
             tc::commit(bar.a_empty + as);
+            pi += clock64() - ti;
             if (++as == kTcAStages) as = 0, aph ^= 1;
           }
           if (!ok) break;
@@ -408,6 +411,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         // every MMA issued has completed before tensor memory is released
         tc::commit(bar.done);
         tc::mbar_wait(bar.done, 0);
+        if (A.prof) atomicAdd(A.prof + 14, pi);
       }
       __syncwarp();
     } else {
@@ -531,22 +535,41 @@ __device__ __forceinline__ void rows_split(const uint8_t *__restrict__ x, uint32
   const uint32_t sub = lane / G, gl = lane % G, cpl = (h / 16) / G;
   for (uint32_t base = warp * 32; base < n; base += nw * 32) {
     uint32_t mine = 0;
+    if (G <= 16 && cpl == 1) {
+      // every load of the batch first, then the sums
+      uint4 v[G <= 16 ? G : 1];
+      const uint32_t *w = qw + 4 * gl;
 #pragma unroll
-    for (uint32_t it = 0; it < G; ++it) {
-      const uint32_t i = base + it * RPW + sub;
-      uint32_t dot = 0;
-      if (i < n) {
-        const uint4 *rv = reinterpret_cast<const uint4 *>(x + static_cast<size_t>(r0 + i) * dc);
-        for (uint32_t c = 0; c < cpl; ++c) {
-          const uint32_t u = gl + c * G;
-          const uint4 v = __ldg(rv + u);
-          const uint32_t *w = qw + 4 * u;
-          dot = dp4(v.x, w[0], dp4(v.y, w[1], dp4(v.z, w[2], dp4(v.w, w[3], dot))));
-        }
+      for (uint32_t it = 0; it < (G <= 16 ? G : 1); ++it) {
+        const uint32_t i = base + it * RPW + sub;
+        v[it] = i < n ? __ldg(reinterpret_cast<const uint4 *>(x + static_cast<size_t>(r0 + i) * dc) + gl)
+                      : make_uint4(0, 0, 0, 0);
       }
 #pragma unroll
-      for (uint32_t o = G / 2; o; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
-      if (gl == it) mine = dot;
+      for (uint32_t it = 0; it < (G <= 16 ? G : 1); ++it) {
+        uint32_t dot = dp4(v[it].x, w[0], dp4(v[it].y, w[1], dp4(v[it].z, w[2], dp4(v[it].w, w[3], 0))));
+#pragma unroll
+        for (uint32_t o = G / 2; o; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
+        if (gl == it) mine = dot;
+      }
+    } else {
+#pragma unroll
+      for (uint32_t it = 0; it < G; ++it) {
+        const uint32_t i = base + it * RPW + sub;
+        uint32_t dot = 0;
+        if (i < n) {
+          const uint4 *rv = reinterpret_cast<const uint4 *>(x + static_cast<size_t>(r0 + i) * dc);
+          for (uint32_t c = 0; c < cpl; ++c) {
+            const uint32_t u = gl + c * G;
+            const uint4 vv = __ldg(rv + u);
+            const uint32_t *w = qw + 4 * u;
+            dot = dp4(vv.x, w[0], dp4(vv.y, w[1], dp4(vv.z, w[2], dp4(vv.w, w[3], dot))));
+          }
+        }
+#pragma unroll
+        for (uint32_t o = G / 2; o; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
+        if (gl == it) mine = dot;
+      }
     }
     const uint32_t i = base + gl * RPW + sub;
     if (i < n) f(i, mine);

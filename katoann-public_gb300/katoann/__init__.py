@@ -275,8 +275,8 @@ class Index:
                     ranking_role_cycles=dict(zip(
                         ("conv_wait_raw", "conv_wait_a", "conv_total", "mma_wait_b", "mma_wait_acc",
                          "mma_wait_a", "mma_total", "epi_wait_b", "epi_wait_acc", "epi_total",
-                         "tma_wait_stage", "tma_total", "stage_wait_b", "stage_total"),
-                        (int(v) for v in s[16:30]))),
+                         "tma_wait_stage", "tma_total", "stage_wait_b", "stage_total",
+                         "mma_issue"), (int(v) for v in s[16:31]))),
                     coarse_role_cycles=dict(zip(
                         ("tma_wait", "tma_total", "mma_wait_acc", "mma_wait_stage", "mma_total",
                          "epi_wait", "epi_total"), (int(v) for v in s[32:39]))))
