@@ -143,17 +143,13 @@ __device__ __forceinline__ uint32_t block_scan_bins(uint32_t *hist, uint32_t ran
   return *sh_sel;
 }
 
-__global__ void __launch_bounds__(kSelThreads) select_topp_kernel(
-    const float *__restrict__ dists, uint32_t n, uint32_t p, uint32_t *__restrict__ probed,
-    unsigned long long *__restrict__ tie_count) {
-  extern __shared__ unsigned long long sel[];  // up to kSortMax (key << 32 | id)
-  __shared__ uint32_t hist[256];
-  __shared__ uint32_t sh_sel, sh_below, sh_cnt, sh_eq;
-  const uint32_t q = blockIdx.x;
-  const uint32_t *keys = reinterpret_cast<const uint32_t *>(dists) + static_cast<size_t>(q) * n;
-  uint32_t *outp = probed + static_cast<size_t>(q) * p;
+// Smallest p keys of a row by (key, index) in up to six passes over the row
+// (8-bit radix digits of the p-th key, then of the tied indices, then the
+// gather). sel holds np2(p) 64-bit words, hist 256 counters, scal 4 words.
+__device__ void select_passes(const uint32_t *__restrict__ keys, uint32_t n, uint32_t p,
+                              uint32_t *__restrict__ outp, unsigned long long *__restrict__ tie_count,
+                              unsigned long long *sel, uint32_t *hist, uint32_t *scal) {
   const uint32_t tid = threadIdx.x;
-
   // 1) the p-th smallest key (rank p-1), and how many keys are below it.
   uint32_t prefix = 0, rank = p - 1, below = 0;
   for (int shift = 24; shift >= 0; shift -= 8) {
@@ -165,21 +161,21 @@ __global__ void __launch_bounds__(kSelThreads) select_topp_kernel(
       if ((k & hmask) == prefix) atomicAdd(&hist[(k >> shift) & 0xFFu], 1u);
     }
     __syncthreads();
-    const uint32_t bin = block_scan_bins(hist, rank, &sh_sel, &sh_below);
-    rank -= sh_below;
-    below += sh_below;
+    const uint32_t bin = block_scan_bins(hist, rank, scal, scal + 1);
+    rank -= scal[1];
+    below += scal[1];
     prefix |= bin << shift;
     __syncthreads();
   }
   const uint32_t T = prefix;        // the p-th smallest key
   const uint32_t need = rank + 1;   // ids to take among keys == T
   // 2) among keys == T, the need-th smallest list id (only when ties exceed need).
-  if (tid == 0) sh_eq = 0;
+  if (tid == 0) scal[3] = 0;
   __syncthreads();
   for (uint32_t i = tid; i < n; i += kSelThreads)
-    if (keys[i] == T) atomicAdd(&sh_eq, 1u);
+    if (keys[i] == T) atomicAdd(&scal[3], 1u);
   __syncthreads();
-  const uint32_t neq = sh_eq;
+  const uint32_t neq = scal[3];
   uint32_t idmax = 0xFFFFFFFFu;
   if (neq > need) {
     if (tid == 0 && tie_count) atomicAdd(tie_count, 1ull);
@@ -191,21 +187,21 @@ __global__ void __launch_bounds__(kSelThreads) select_topp_kernel(
       for (uint32_t i = tid; i < n; i += kSelThreads)
         if (keys[i] == T && (i & hmask) == ip) atomicAdd(&hist[(i >> shift) & 0xFFu], 1u);
       __syncthreads();
-      const uint32_t bin = block_scan_bins(hist, ir, &sh_sel, &sh_below);
-      ir -= sh_below;
+      const uint32_t bin = block_scan_bins(hist, ir, scal, scal + 1);
+      ir -= scal[1];
       ip |= bin << shift;
       __syncthreads();
     }
     idmax = ip;
   }
   // 3) gather the p selected.
-  if (tid == 0) sh_cnt = 0;
+  if (tid == 0) scal[2] = 0;
   __syncthreads();
   const bool sorted = p <= kSortMax;
   for (uint32_t i = tid; i < n; i += kSelThreads) {
     const uint32_t k = keys[i];
     if (k < T || (k == T && i <= idmax)) {
-      const uint32_t pos = atomicAdd(&sh_cnt, 1u);
+      const uint32_t pos = atomicAdd(&scal[2], 1u);
       if (sorted) sel[pos] = (static_cast<unsigned long long>(k) << 32) | i;
       else outp[pos] = i;
     }
@@ -233,6 +229,138 @@ __global__ void __launch_bounds__(kSelThreads) select_topp_kernel(
       __syncthreads();
     }
   }
+  for (uint32_t i = tid; i < p; i += kSelThreads) outp[i] = static_cast<uint32_t>(sel[i] & 0xFFFFFFFFu);
+}
+
+__global__ void __launch_bounds__(kSelThreads) select_topp_kernel(
+    const float *__restrict__ dists, uint32_t n, uint32_t p, uint32_t *__restrict__ probed,
+    unsigned long long *__restrict__ tie_count) {
+  extern __shared__ unsigned long long sel[];  // up to kSortMax (key << 32 | id)
+  __shared__ uint32_t hist[256], scal[4];
+  const uint32_t q = blockIdx.x;
+  select_passes(reinterpret_cast<const uint32_t *>(dists) + static_cast<size_t>(q) * n, n, p,
+                probed + static_cast<size_t>(q) * p, tie_count, sel, hist, scal);
+}
+
+// In-shared-memory bitonic sort of n 64-bit keys, ascending.
+__device__ void sort_keys(unsigned long long *key, uint32_t n) {
+  uint32_t np2 = 1;
+  while (np2 < n) np2 <<= 1;
+  for (uint32_t i = n + threadIdx.x; i < np2; i += blockDim.x) key[i] = ~0ull;
+  __syncthreads();
+  for (uint32_t size = 2; size <= np2; size <<= 1)
+    for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+      for (uint32_t i = threadIdx.x; i < np2; i += blockDim.x) {
+        const uint32_t j = i ^ stride;
+        if (j > i) {
+          const bool up = (i & size) == 0;
+          const unsigned long long a = key[i], b = key[j];
+          if ((a > b) == up) {
+            key[i] = b;
+            key[j] = a;
+          }
+        }
+      }
+      __syncthreads();
+    }
+}
+
+// Smallest p of a row of n non-negative float distances by (distance, list),
+// ascending, for p <= kSortMax, in two passes over the row: a histogram of
+// the top 12 bits below the sign (distances cluster in a narrow range, so
+// these bits still spread them), then a gather that takes every key of a bin
+// below the boundary bin and collects the boundary bin's keys, of which the
+// first (p - below) by (key, index) complete the selection. A boundary bin
+// with more than kCand keys falls back to select_passes.
+constexpr uint32_t kHistBins = 4096;
+constexpr uint32_t kCand = 2048;
+
+__global__ void __launch_bounds__(kSelThreads) select_topp_hist_kernel(
+    const float *__restrict__ dists, uint32_t n, uint32_t p, uint32_t *__restrict__ probed,
+    unsigned long long *__restrict__ tie_count) {
+  extern __shared__ unsigned long long dyn[];
+  unsigned long long *cand = dyn;          // kCand
+  unsigned long long *sel = dyn + kCand;   // np2(p)
+  __shared__ uint32_t hist[kHistBins];
+  __shared__ uint32_t scal[8];
+  __shared__ uint32_t wsum[kSelThreads / 32];
+  const uint32_t q = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t *keys = reinterpret_cast<const uint32_t *>(dists) + static_cast<size_t>(q) * n;
+  uint32_t *outp = probed + static_cast<size_t>(q) * p;
+  for (uint32_t i = tid; i < kHistBins; i += kSelThreads) hist[i] = 0;
+  if (tid < 8) scal[tid] = 0;
+  __syncthreads();
+  const bool vec = (reinterpret_cast<uintptr_t>(keys) & 15) == 0;
+  const uint32_t n4 = vec ? n / 4 : 0;
+  auto bin_of = [](uint32_t k) { return (k >> 19) & (kHistBins - 1); };
+  // 1) histogram
+#pragma unroll 4
+  for (uint32_t i = tid; i < n4; i += kSelThreads) {
+    const uint4 v = reinterpret_cast<const uint4 *>(keys)[i];
+    atomicAdd(&hist[bin_of(v.x)], 1u);
+    atomicAdd(&hist[bin_of(v.y)], 1u);
+    atomicAdd(&hist[bin_of(v.z)], 1u);
+    atomicAdd(&hist[bin_of(v.w)], 1u);
+  }
+  for (uint32_t i = n4 * 4 + tid; i < n; i += kSelThreads) atomicAdd(&hist[bin_of(keys[i])], 1u);
+  __syncthreads();
+  // 2) the bin holding rank p - 1: each thread owns 16 consecutive bins
+  constexpr uint32_t kPer = kHistBins / kSelThreads;
+  uint32_t tsum = 0;
+#pragma unroll
+  for (uint32_t j = 0; j < kPer; ++j) tsum += hist[tid * kPer + j];
+  uint32_t incl = tsum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= static_cast<uint32_t>(o)) incl += y;
+  }
+  if (lane == 31) wsum[warp] = incl;
+  __syncthreads();
+  uint32_t wbase = 0;
+  for (uint32_t w = 0; w < warp; ++w) wbase += wsum[w];
+  const uint32_t excl = wbase + incl - tsum, rank = p - 1;
+  if (rank >= excl && rank < excl + tsum) {
+    uint32_t acc = excl, j = 0;
+    for (; j < kPer; ++j) {
+      const uint32_t h = hist[tid * kPer + j];
+      if (rank < acc + h) break;
+      acc += h;
+    }
+    scal[0] = tid * kPer + j;  // boundary bin
+    scal[1] = acc;             // keys below it
+  }
+  __syncthreads();
+  const uint32_t bstar = scal[0], below = scal[1], c = hist[bstar];
+  if (c > kCand) {  // a crowded boundary bin: the radix passes instead
+    select_passes(keys, n, p, outp, tie_count, sel, hist, scal + 4);
+    return;
+  }
+  // 3) gather: bins below the boundary are in; the boundary bin is a candidate
+  auto take = [&](uint32_t k, uint32_t i) {
+    const uint32_t b = bin_of(k);
+    if (b < bstar) sel[atomicAdd(&scal[2], 1u)] = (static_cast<unsigned long long>(k) << 32) | i;
+    else if (b == bstar) cand[atomicAdd(&scal[3], 1u)] = (static_cast<unsigned long long>(k) << 32) | i;
+  };
+#pragma unroll 4
+  for (uint32_t i = tid; i < n4; i += kSelThreads) {
+    const uint4 v = reinterpret_cast<const uint4 *>(keys)[i];
+    take(v.x, 4 * i);
+    take(v.y, 4 * i + 1);
+    take(v.z, 4 * i + 2);
+    take(v.w, 4 * i + 3);
+  }
+  for (uint32_t i = n4 * 4 + tid; i < n; i += kSelThreads) take(keys[i], i);
+  __syncthreads();
+  // 4) the boundary bin's keys in order; the first `need` complete the set
+  sort_keys(cand, c);
+  const uint32_t need = p - below;
+  for (uint32_t i = tid; i < need; i += kSelThreads) sel[below + i] = cand[i];
+  if (tid == 0 && tie_count && need < c && (cand[need] >> 32) == (cand[need - 1] >> 32))
+    atomicAdd(tie_count, 1ull);
+  __syncthreads();
+  // 5) the p selected in order
+  sort_keys(sel, p);
   for (uint32_t i = tid; i < p; i += kSelThreads) outp[i] = static_cast<uint32_t>(sel[i] & 0xFFFFFFFFu);
 }
 
@@ -265,14 +393,23 @@ int select_topp(const float *dists, uint32_t nq, uint32_t n, uint32_t p, uint32_
   if (p == 0 || p > n) return invalid("need 1 <= nprobe <= nlist");
   uint32_t np2 = 1;
   while (np2 < p) np2 <<= 1;
-  const size_t smem = p <= kSortMax ? np2 * sizeof(unsigned long long) : 0;
   static bool attr_set = false;
   if (!attr_set) {
     KATO_CUDA(cudaFuncSetAttribute(select_topp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    kSortMax * 8));
+    KATO_CUDA(cudaFuncSetAttribute(select_topp_hist_kernel,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (kCand + kSortMax) * 8));
     attr_set = true;
   }
-  select_topp_kernel<<<nq, kSelThreads, smem, st>>>(dists, n, p, probed, tie_count);
+  if (p <= kSortMax) {
+    // candidates and the sorted selection (the bitonic sort pads to a power of two)
+    const size_t smem = (kCand + std::max<uint32_t>(np2, 2)) * sizeof(unsigned long long);
+    select_topp_hist_kernel<<<nq, kSelThreads, smem, st>>>(dists, n, p, probed, tie_count);
+    KATO_LAUNCHED("select_topp_hist_kernel");
+    return KATO_OK;
+  }
+  select_topp_kernel<<<nq, kSelThreads, 0, st>>>(dists, n, p, probed, tie_count);
   KATO_LAUNCHED("select_topp_kernel");
   return KATO_OK;
 }
