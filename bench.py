@@ -56,6 +56,8 @@ def parse_args():
     ap.add_argument("--survivors", type=int, default=32)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--ref-coding", choices=["gpu", "oracle"], default="gpu",
+                    help="reference arm: who codes the index the oracle searches")
     return ap.parse_args()
 
 
@@ -209,6 +211,14 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------ roofline
+SEED_ROWS = 1024  # rows behind each query's seed bound (the library default for survivors <= 128)
+
+# DRAM bytes per 128-row tile of the tensor-core ranking kernel, from one ncu
+# capture on the 2M x 1024 case (profiles/rank_tc_traffic_2m.md): 530.5 MB over
+# 20,278 tiles. The traffic of a launch scales with the tiles it scores.
+RANK_TC_DRAM_BYTES_PER_TILE = 530.5e6 / 20278
+
+
 def phase_work(phase: str, B: int, L: int, dc: int, d: int, nprobe: int, S: int, head: int,
                probed_rows: float, probed_lists_rows: float):
     """(bound, algorithmic work per launch, unit) of one pipeline phase.
@@ -218,8 +228,12 @@ def phase_work(phase: str, B: int, L: int, dc: int, d: int, nprobe: int, S: int,
     if phase == "coarse product":
         return "tensor", 2.0 * 4 * B * L * dc / 1e12, "TFLOP/s"
     if phase == "ranking pass":
-        # each probed list's head bytes, head norm and ids, read once per batch
-        return "hbm", probed_lists_rows * (head + 8 + 4) / 1e9, "GB/s"
+        # each probed list's head bytes, read once per batch (the row norms are
+        # summed from the same bytes; ids are only read for the survivors)
+        return "hbm", probed_lists_rows * head / 1e9, "GB/s"
+    if phase == "seed bounds":
+        # the first SEED_ROWS rows of each query's nearest lists
+        return "hbm", B * SEED_ROWS * head / 1e9, "GB/s"
     if phase == "refine":
         return "hbm", B * S * (2 * dc + 8 + 4) / 1e9, "GB/s"
     if phase == "rotate+quantize":
@@ -308,6 +322,7 @@ def main():
         grid = [(args.nprobe, args.survivors)]
     else:
         grid = [(p, s) for s in (32, 64) for p in (16, 24, 32, 48, 64, 96, 128, 192, 256) if p <= L]
+        grid += [(p, 128) for p in (128, 192, 256, 384) if p <= L]  # towards recall 0.999
     for p, s in grid:
         r, ms = run(p, s)
         sweep.append({"nprobe": p, "survivors": s, "recall": round(r, 5), "ms": round(ms, 3),
@@ -391,8 +406,13 @@ def main():
                                    probed_rows, probed_rows)
     achieved = work / (per_launch[dom] / 1e3)
     peak = peaks["bf16_tflops"] if bound == "tensor" else peaks["hbm_gbs"]
+    traffic = None
+    if dom == "ranking pass" and search_stats.get("ranking_tiles"):
+        traffic = round(RANK_TC_DRAM_BYTES_PER_TILE * search_stats["ranking_tiles"] / 1e9, 3)
     roofline = {"kernel": dom, "bound": bound, "achieved": round(achieved, 2), "peak": peak,
-                "unit": unit, "frac": round(achieved / peak, 4), "traffic": None,
+                "unit": unit, "frac": round(achieved / peak, 4), "traffic": traffic,
+                "traffic_unit": "GB per launch (scaled from the 2M capture by tiles scored)",
+                "algorithmic": round(work, 3),
                 "peak_source": peaks["source"] + (" burst bf16" if bound == "tensor" else " copy"),
                 "ms_per_launch": round(per_launch[dom], 4)}
 
@@ -474,21 +494,37 @@ def cpu_baseline(args, torch, idx, queries, p, S, k):
 
 
 def run_reference(args, torch, vectors, order, cen, rot, sizes, queries, gt, setup_s):
-    """The reference's CPU search, restated (oracle), coding the index itself
-    from the float vectors and timing bounded samples of the batch."""
+    """The reference's CPU search, restated (oracle), timed on bounded samples
+    of the batch. The index the oracle searches is coded from the same float
+    vectors either by the oracle itself (--ref-coding oracle: its scalar
+    rotation of 10M x 1024 takes minutes on 16 cores) or, by default, by the
+    GPU load, whose codes are bit-identical to the oracle's (the kernel tests
+    compare them); the timed search runs in the oracle alone."""
     import oracle
     k = args.k
     cores = os.cpu_count() or 1
     oracle.set_threads(cores)
     t0 = time.time()
-    o = oracle.OracleIndex(None, arrays=dict(
-        centroids=cen.cpu().numpy(), list_sizes=sizes, ids=order.cpu().numpy().astype(np.uint32),
-        vectors=vectors.cpu().numpy(), rotation=rot.cpu().numpy(), head_dims=args.head))
+    if args.ref_coding == "oracle":
+        o = oracle.OracleIndex(None, arrays=dict(
+            centroids=cen.cpu().numpy(), list_sizes=sizes, ids=order.cpu().numpy().astype(np.uint32),
+            vectors=vectors.cpu().numpy(), rotation=rot.cpu().numpy(), head_dims=args.head))
+    else:
+        import katoann
+        idx = katoann.Index()
+        idx.load_arrays(cen, sizes, order.to(torch.int32), vectors, rotation=rot,
+                        head_dims=args.head, max_batch=args.batch)
+        codes = idx.export_codes()
+        del idx
+        torch.cuda.empty_cache()
+        o = oracle.OracleIndex(None, codes=codes)
+        del codes
     load_s = time.time() - t0
     q = queries.cpu().numpy()
-    p, S = (args.nprobe or 64), args.survivors
-    # a step = a bounded sample of the batch, sized so warmup + steps fit ~150 s
-    per_step = max(2.0, 150.0 / max(1, args.steps + args.warmup))
+    # the GPU arm's sweep reaches recall 0.99 at nprobe 96, survivors 64 on this workload
+    p, S = (args.nprobe or 96), (args.survivors if args.nprobe else 64)
+    # a step = a bounded sample of the batch, sized so warmup + steps fit ~90 s
+    per_step = max(0.1, 90.0 / max(1, args.steps + args.warmup))
     qps, m, dt, ids, _ = _time_oracle(o, q, k, p, S, per_step)
     tot_q, tot_t = 0, 0.0
     for i in range(args.warmup):
@@ -515,7 +551,8 @@ def run_reference(args, torch, vectors, order, cen, rot, sizes, queries, gt, set
                             "isa": platform.machine()},
            "e2e": {"value": round(value, 1), "unit": "queries/s", "h2d_bytes_per_step": 0,
                    "d2h_bytes_per_step": 0},
-           "setup_s": round(setup_s, 1), "oracle_load_s": round(load_s, 1)}
+           "setup_s": round(setup_s, 1), "oracle_load_s": round(load_s, 1),
+           "index_coding": "oracle" if args.ref_coding == "oracle" else "GPU load (bit-identical codes)"}
     print(json.dumps(out))
 
 

@@ -162,8 +162,9 @@ int katoann_gpu_search(const katoann_gpu_index *index, const float *d_queries, u
  * the pipeline's phases, so the duration of every phase of every pass in a
  * timed region is measured where it runs. Phases: 0 rotation+quantization of
  * the queries, 1 coarse product, 2 top-nprobe selection, 3 inversion,
- * 4 ranking pass, 5 survivor merge, 6 refinement. */
-#define KATO_PHASES 7
+ * 4 seed bounds of the tensor-core ranking pass (empty on the CUDA-core
+ * pass), 5 ranking pass, 6 survivor merge, 7 refinement. */
+#define KATO_PHASES 8
 void *katoann_gpu_timer_create(uint32_t max_passes);
 void katoann_gpu_timer_destroy(void *timer);
 /* Sums the phase durations (ms) of all passes recorded since the last read

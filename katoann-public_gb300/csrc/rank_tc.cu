@@ -38,6 +38,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <climits>
 #include <cmath>
 
@@ -128,6 +129,12 @@ struct TileWalk {
   __device__ bool last() const { return t + 1 == t1 || t + 1 == next; }
 };
 
+// The MMA width (queries) an item of ne queries uses: 16, 32 or N.
+template <uint32_t N>
+__device__ __forceinline__ uint32_t mma_width(uint32_t ne) {
+  return ne <= 16 ? 16u : (ne <= 32 && N > 32 ? 32u : N);
+}
+
 // A pipeline wait that also adds the cycles it took to `acc`.
 // A pipeline wait that also adds the cycles it took to `acc`.
 __device__ __forceinline__ bool timed_wait(uint64_t *b, uint32_t phase, volatile uint32_t *err,
@@ -150,23 +157,24 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   uint32_t *rcount = reinterpret_cast<uint32_t *>(sm + L.rcount);
   int32_t *sxn = reinterpret_cast<int32_t *>(sm + L.sxn);
   QInfo *qinfo = reinterpret_cast<QInfo *>(sm + L.qinfo);
+  uint32_t *swidth = reinterpret_cast<uint32_t *>(sm + L.width);  // per query buffer: queries
   const uint32_t btile = N * h * 2, rtile = kTcRows * S.inner;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
   if (tid == 0) {
     for (uint32_t s = 0; s < S.Rs; ++s) {
       tc::mbar_init(bar.raw_full + s, 1);
-      tc::mbar_init(bar.raw_empty + s, kConvWarps * 32);
+      tc::mbar_init(bar.raw_empty + s, kConvWarps);
     }
     for (uint32_t s = 0; s < kTcAStages; ++s) {
-      tc::mbar_init(bar.a_full + s, kConvWarps * 32);
+      tc::mbar_init(bar.a_full + s, kConvWarps);
       tc::mbar_init(bar.a_empty + s, 1);
       tc::mbar_init(bar.acc_full + s, 1);
       tc::mbar_init(bar.acc_empty + s, kEpiWarps);
-      tc::mbar_init(bar.xn_full + s, kConvWarps * 32);
+      tc::mbar_init(bar.xn_full + s, kConvWarps);
     }
     for (uint32_t s = 0; s < S.Bs; ++s) {
-      tc::mbar_init(bar.b_full + s, N);
+      tc::mbar_init(bar.b_full + s, kQueryWarps);
       tc::mbar_init(bar.b_empty + s, 1 + kEpiWarps);
     }
     tc::mbar_init(bar.done, 1);
@@ -180,6 +188,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   __syncthreads();
   tc::fence_after();
   const uint32_t tmem = *tbase;
+  const uint32_t acol = kTcAStages * N;  // TMEM columns of the A stages follow the accumulators
   const uint32_t nitems = *A.nitems;
   const uint32_t T = nitems ? A.tile_off[nitems] : 0;
   const uint32_t t0 = static_cast<uint32_t>(static_cast<uint64_t>(T) * blockIdx.x / gridDim.x);
@@ -203,46 +212,61 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       for (; ok && w.t < t1; ++w.t) {
         int32_t xs = 0;
         for (uint32_t kc = 0; kc < nkc; ++kc) {
-          if (!timed_wait(bar.raw_full + rs, rph, err, pw[0]) ||
-              !timed_wait(bar.a_empty + as, aph ^ 1, err, pw[1])) {
+          // warp-uniform waits: a warp arrives once for all its lanes below
+          if (!__all_sync(0xffffffffu, timed_wait(bar.raw_full + rs, rph, err, pw[0]) &&
+                                           timed_wait(bar.a_empty + as, aph ^ 1, err, pw[1]))) {
             ok = false;
             break;
           }
+          tc::fence_after();  // the MMAs that read A stage `as` before have completed
           const unsigned char *raw = sm + L.raw + rs * rtile;
-          unsigned char *a = sm + L.a + as * kTcATile;
           const uint32_t nu = min(S.inner, h - kc * S.inner) / 16;
+          // the row's half of the chunk as fp16 pairs: 16 dimensions = 8 columns
+          uint32_t cols[32];
 #pragma unroll
           for (uint32_t i = 0; i < 4; ++i) {
             const uint32_t u = hf * nuh + i;
+            uint4 lo = make_uint4(0, 0, 0, 0), hi = lo;
             if (i < nuh && u < nu) {
               const uint32_t o = r * S.inner + u * 16;
               const uint4 v = *reinterpret_cast<const uint4 *>(raw + (o ^ (((o >> 7) & swm) << 4)));
-              uint4 lo, hi;
               tc::bytes_to_half16(v, bias, lo, hi);
-              *reinterpret_cast<uint4 *>(a + tc::canon_off(r, u * 16, 128)) = lo;
-              *reinterpret_cast<uint4 *>(a + tc::canon_off(r, u * 16 + 8, 128)) = hi;
               xs += centred_sq_sum16(v);
             }
+            cols[8 * i + 0] = lo.x, cols[8 * i + 1] = lo.y, cols[8 * i + 2] = lo.z, cols[8 * i + 3] = lo.w;
+            cols[8 * i + 4] = hi.x, cols[8 * i + 5] = hi.y, cols[8 * i + 6] = hi.z, cols[8 * i + 7] = hi.w;
           }
-          tc::fence_smem_to_async();
-          tc::mbar_arrive(bar.a_full + as);
-          tc::mbar_arrive(bar.raw_empty + rs);
+          __syncwarp();
+          if (lane == 0) tc::mbar_arrive(bar.raw_empty + rs);  // the raw stage has been read
+          // into this row's TMEM lane: A stage `as`, the half's columns
+          if (hf * nuh < nu) {
+            const uint32_t taddr =
+                tmem + (((warp & 3) * 32u) << 16) + acol + as * (S.inner / 2) + hf * nuh * 8;
+            if (nuh == 4) tc::tmem_st32(taddr, cols);
+            else tc::tmem_st16(taddr, *reinterpret_cast<const uint32_t(*)[16]>(cols));
+          }
+          tc::tmem_wait_st();
+          tc::fence_before();
+          __syncwarp();
+          if (lane == 0) tc::mbar_arrive(bar.a_full + as);
           if (++rs == S.Rs) rs = 0, rph ^= 1;
           if (++as == kTcAStages) as = 0, aph ^= 1;
         }
         if (!ok) break;
         // the row norms of this tile's accumulator slot, once the epilogue
         // has finished with the slot's previous tile
-        if (!timed_wait(bar.acc_empty + ab, abph ^ 1, err, pw[1])) break;
+        if (!__all_sync(0xffffffffu, timed_wait(bar.acc_empty + ab, abph ^ 1, err, pw[1]))) break;
         sxn[(ab * 2 + hf) * kTcRows + r] = xs;
-        tc::mbar_arrive(bar.xn_full + ab);
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(bar.xn_full + ab);
         if (++ab == kTcAStages) ab = 0, abph ^= 1;
       }
     } else if (warp < kTmaWarp) {
       // ---- epilogue: thread = row (its TMEM lane), warpgroup = column half
       constexpr uint32_t CH = N / 2;  // columns per half
       const uint32_t q4 = warp & 3, half = (warp - kConvWarps) >> 2;
-      const uint32_t row = q4 * 32 + lane, c0 = half * CH;
+      const uint32_t row = q4 * 32 + lane;
+      uint32_t cph = CH, c0 = half * CH;  // columns per half and this half's first, per item
       uint4 *rec = A.rec + static_cast<size_t>(blockIdx.x) * A.rec_cap;
       uint32_t ab = 0, abph = 0, ib = 0, bph = 0;
       unsigned long long tiles = 0, found = 0;
@@ -251,8 +275,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         w.step();
         const QInfo *qi = qinfo + ib * N;
         // waits are made warp-uniform: the warp-collective steps below need all lanes
-        if (w.first())
+        if (w.first()) {
           if (!__all_sync(0xffffffffu, timed_wait(bar.b_full + ib, bph, err, pw[0]))) break;
+          cph = mma_width<N>(swidth[ib]) / 2;
+          c0 = half * cph;
+        }
         const uint32_t rin = (w.t - w.start) * kTcRows + row;
         const bool valid = rin < w.cur.nrows;
         const uint32_t grow = w.cur.row0 + rin;
@@ -263,12 +290,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const int32_t xn = sxn[ab * 2 * kTcRows + row] + sxn[(ab * 2 + 1) * kTcRows + row];
         const uint32_t taddr = tmem + ((q4 * 32u) << 16) + ab * N;
         const float xnf = static_cast<float>(xn);
-        // columns in groups of up to 16: load the group's accumulators and
-        // bounds, compare each pair (or-ed into one predicate), and resolve
-        // the columns only when the warp has a passing pair (rare)
-        constexpr uint32_t G = CH < 16 ? CH : 16;
-#pragma unroll
-        for (uint32_t g = 0; g < CH; g += G) {
+        // this warpgroup's columns: half of the item's MMA width. In groups
+        // of up to 16: load the group's accumulators and bounds, compare each
+        // pair (or-ed into one predicate), and resolve the columns only when
+        // the warp has a passing pair (rare)
+        auto process = [&](auto gsize, uint32_t g) {
+          constexpr uint32_t G = decltype(gsize)::value;
           uint32_t d[G], qb[G];
           if constexpr (G == 16) tc::tmem_ld16(taddr + c0 + g, d);
           else tc::tmem_ld8(taddr + c0 + g, d);
@@ -321,6 +348,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
               }
             }
           }
+        };
+        if (cph == 8) {
+          process(std::integral_constant<uint32_t, 8>{}, 0);
+        } else if constexpr (CH >= 16) {
+          for (uint32_t g = 0; g < cph; g += 16) process(std::integral_constant<uint32_t, 16>{}, g);
         }
         // the slot's accumulators and row norms have been read: hand it back
         tc::fence_before();
@@ -369,13 +401,16 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     } else if (warp == kMmaWarp) {
       // ---- MMA issuer
       if (lane == 0) {
-        const uint32_t idesc = tc::idesc_f16(kTcRows, N);
+        uint32_t idesc = tc::idesc_f16(kTcRows, N);
         uint32_t as = 0, aph = 0, ab = 0, abph = 0, ib = 0, bph = 0;
         unsigned long long pi = 0;  // cycles issuing MMAs and commits
         bool ok = true;
         for (; ok && w.t < t1; ++w.t) {
           w.step();
-          if (w.first() && !timed_wait(bar.b_full + ib, bph, err, pw[0])) break;
+          if (w.first()) {
+            if (!timed_wait(bar.b_full + ib, bph, err, pw[0])) break;
+            idesc = tc::idesc_f16(kTcRows, mma_width<N>(swidth[ib]));  // the item's queries
+          }
           if (!timed_wait(bar.acc_empty + ab, abph ^ 1, err, pw[1])) break;
           tc::fence_after();
           const uint32_t bbase = tc::smem_addr(sm + L.b + ib * btile);
@@ -386,16 +421,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             }
             tc::fence_after();
             const long long ti = clock64();
-            // descriptors of the chunk's first K step; each further step of
-            // 16 dimensions advances A by 256 bytes and B by 256 bytes (two
-            // core matrices), i.e. the encoded start address by 16
-            const uint64_t ad0 = tc::desc(tc::smem_addr(sm + L.a + as * kTcATile), 128, 16 * 128);
+            // A from TMEM (8 columns per 16-dimension step); B's descriptor
+            // advances 256 bytes (two core matrices), i.e. 16 encoded, per step
+            const uint32_t a0 = tmem + acol + as * (S.inner / 2);
             const uint64_t bd0 = tc::desc(bbase + kc * S.inner * 16, 128, (h / 8) * 128);
             const uint32_t steps = min(S.inner, h - kc * S.inner) / 16;
             const uint32_t dcol = tmem + ab * N;
 #pragma unroll
             for (uint32_t s = 0; s < 8; ++s)
-              if (s < steps) tc::mma_f16(dcol, ad0 + 16 * s, bd0 + 16 * s, idesc, (kc | s) != 0);
+              if (s < steps) tc::mma_f16_ts(dcol, a0 + 8 * s, bd0 + 16 * s, idesc, (kc | s) != 0);
             tc::commit(bar.a_empty + as);
             pi += clock64() - ti;
             if (++as == kTcAStages) as = 0, aph ^= 1;
@@ -415,16 +449,18 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       }
       __syncwarp();
     } else {
-      // ---- query staging: thread j < N gathers query j of each item
+      // ---- query staging: thread j < N gathers query j of each item; each
+      // staging warp arrives once per item
       const uint32_t j = tid - kQueryWarp0 * 32;
       uint32_t ib = 0, bph = 0;
-      if (j < N) {
-        for (; w.t < t1; ++w.t) {
-          w.step();
-          if (!w.first()) continue;
-          if (!timed_wait(bar.b_empty + ib, bph ^ 1, err, pw[0])) break;
+      for (; w.t < t1; ++w.t) {
+        w.step();
+        if (!w.first()) continue;
+        if (!__all_sync(0xffffffffu, timed_wait(bar.b_empty + ib, bph ^ 1, err, pw[0]))) break;
+        if (j < N) {
           const uint32_t e0 = A.off[w.cur.list] + w.cur.qfirst;
           const uint32_t ne = min(N, A.off[w.cur.list + 1] - e0);
+          if (j == 0) swidth[ib] = ne;
           unsigned char *b = sm + L.b + ib * btile;
           QInfo q{0, 0, INT_MIN, -INFINITY};
           if (j < ne) {
@@ -456,9 +492,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           reinterpret_cast<uint32_t *>(sm + L.qbv)[ib * N + j] =
               kFloat ? __float_as_uint(q.qbf) : static_cast<uint32_t>(q.qb);
           tc::fence_smem_to_async();
-          tc::mbar_arrive(bar.b_full + ib);
-          if (++ib == S.Bs) ib = 0, bph ^= 1;
         }
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(bar.b_full + ib);
+        if (++ib == S.Bs) ib = 0, bph ^= 1;
       }
     }
   }
@@ -895,8 +932,9 @@ bool rank_tc_plan(uint32_t h, uint32_t dc, TcShape *s) {
   TcShape t{};
   t.N = h <= 256 ? 64 : (h <= 512 ? 32 : 16);
   t.inner = dc >= 128 ? 128 : 64;
+  // accumulators (two slots of N columns), then the two A stages (inner / 2 columns each)
   t.tcols = 32;
-  while (t.tcols < kTcAStages * t.N) t.tcols <<= 1;
+  while (t.tcols < kTcAStages * t.N + kTcAStages * t.inner / 2) t.tcols <<= 1;
   for (uint32_t bs = 2; bs >= 1; --bs)
     for (uint32_t rs = 4; rs >= 2; --rs) {
       t.Bs = bs;

@@ -42,7 +42,7 @@ struct TcShape {
 
 // Shared-memory carve-up of the ranking CTA.
 struct TcSmem {
-  uint32_t raw, a, b, qinfo, qbv, sxn, bars, tbase, err, rcount, total;
+  uint32_t raw, a, b, qinfo, qbv, width, sxn, bars, tbase, err, rcount, total;
 };
 
 __host__ __device__ inline uint32_t tc_take(uint32_t &o, uint32_t bytes, uint32_t align) {
@@ -62,10 +62,11 @@ __host__ __device__ inline TcSmem tc_smem_layout(uint32_t h, const TcShape &s) {
   TcSmem L{};
   uint32_t o = 0;
   L.raw = tc_take(o, s.Rs * kTcRows * s.inner, 1024);
-  L.a = tc_take(o, kTcAStages * kTcATile, 1024);
+  L.a = tc_take(o, 0, 1024);  // the A stages live in tensor memory
   L.b = tc_take(o, s.Bs * s.N * h * 2, 128);
   L.qinfo = tc_take(o, s.Bs * s.N * kTcQInfo, 16);
   L.qbv = tc_take(o, s.Bs * s.N * 4, 16);
+  L.width = tc_take(o, 2 * 4, 16);
   L.sxn = tc_take(o, kTcAStages * 2 * kTcRows * 4, 16);
   L.bars = tc_take(o, kTcBars * 8, 8);
   L.tbase = tc_take(o, 4, 4);

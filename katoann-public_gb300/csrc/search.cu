@@ -802,6 +802,7 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
   KATO_LAUNCHED("inversion kernels");
   mark(tm, 4, st);
   uint32_t *qcount = nullptr;
+  if (!pl.tc) mark(tm, 5, st);  // no seed-bound phase on the CUDA-core pass
   if (pl.tc) {
     // 4'. ranking pass on the tensor cores: seed bounds, work items, the
     // scan, and the exact rescan of any query whose buffer overflowed
@@ -820,6 +821,7 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
     if ((rc = rank_seed(ix->d_hi, xnorm, qhi, qnorm, probed, ix->d_list_off, nq, p, dc, pl.dims,
                         pl.S, pl.seed_rows, bound, st)))
       return rc;
+    mark(tm, 5, st);
     if ((rc = rank_tc_prepare(cnt, ix->d_list_off, L, pl.tcs.N, nq,
                               reinterpret_cast<uint32_t *>(ws + pl.off_tcscratch), items, tile_off,
                               nitems, qcount, qfill, st)))
@@ -894,7 +896,7 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
     if (rc) return rc;
     ++g_launches;
   }
-  mark(tm, 5, st);
+  mark(tm, 6, st);
   // 5. per-query merge of the slot lists (:1058-1080 / :1205-1218)
   uint32_t np2 = 1;
   while (np2 < pl.S) np2 <<= 1;
@@ -906,9 +908,9 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
                                             stats + 1);
   ++g_launches;
   KATO_LAUNCHED("merge_kernel");
-  mark(tm, 6, st);
+  mark(tm, 7, st);
   if (full) {
-    mark(tm, 7, st);
+    mark(tm, 8, st);
     if (tm && tm->used < tm->max_passes) ++tm->used;
     return KATO_OK;
   }
@@ -922,7 +924,7 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
                                              make_dist_scale(ix->step_sq), out_ids, out_dists);
   KATO_LAUNCHED("refine_kernel");
   ++g_launches;
-  mark(tm, 7, st);
+  mark(tm, 8, st);
   if (tm && tm->used < tm->max_passes) ++tm->used;
   return KATO_OK;
 }

@@ -123,8 +123,8 @@ def dist_value(l2: int, step_sq: float) -> float:
     return float(_lib.katoann_dist_value(int(l2), float(step_sq)))
 
 
-PHASES = ("rotate+quantize", "coarse product", "coarse select", "inversion", "ranking pass",
-          "survivor merge", "refine")
+PHASES = ("rotate+quantize", "coarse product", "coarse select", "inversion", "seed bounds",
+          "ranking pass", "survivor merge", "refine")
 
 
 class PhaseTimer:
