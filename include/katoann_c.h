@@ -33,6 +33,17 @@ void katoann_index_free(void *index);
 int katoann_index_load(void *index, const char *prefix, int precision, int use_amx,
                        uint32_t prefix_dims, int batched_coarse, uint32_t max_batch);
 
+/* katoann_index_load through the device-code cache PREFIX.gpucodes
+ * (LoadOptions::code_cache): loads the codes when they were made from the
+ * same files with the same prefix_dims, else loads the files and writes them. */
+int katoann_index_load_cached(void *index, const char *prefix, uint32_t prefix_dims,
+                              uint32_t max_batch);
+
+/* Index::save_codes / Index::load_codes: the loaded index as it lives on the
+ * device, to and from one file (no counterpart in the reference). */
+int katoann_index_save_codes(void *index, const char *path);
+int katoann_index_load_codes(void *index, const char *path, uint32_t max_batch);
+
 /* An index from arrays (lists concatenated in list order); on_device selects
  * device pointers for ids, vectors, centroids and rotation. */
 int katoann_index_load_arrays(void *index, uint32_t dim, uint32_t nlist, uint32_t npts,

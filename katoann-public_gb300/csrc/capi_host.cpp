@@ -82,6 +82,29 @@ int katoann_index_load(void *index, const char *prefix, int precision, int use_a
   });
 }
 
+int katoann_index_load_cached(void *index, const char *prefix, uint32_t prefix_dims,
+                              uint32_t max_batch) {
+  return guarded([&] {
+    katoann::LoadOptions o;
+    o.prefix_dims = prefix_dims;
+    o.code_cache = true;
+    if (max_batch) o.max_batch = max_batch;
+    I(index)->load(prefix, o);
+  });
+}
+
+int katoann_index_save_codes(void *index, const char *path) {
+  return guarded([&] { I(index)->save_codes(path); });
+}
+
+int katoann_index_load_codes(void *index, const char *path, uint32_t max_batch) {
+  return guarded([&] {
+    katoann::LoadOptions o;
+    if (max_batch) o.max_batch = max_batch;
+    I(index)->load_codes(path, o);
+  });
+}
+
 int katoann_index_load_arrays(void *index, uint32_t dim, uint32_t nlist, uint32_t npts,
                               int normalized, const float *centroids, const uint32_t *list_sizes,
                               const uint32_t *ids, const float *vectors, const float *rotation,

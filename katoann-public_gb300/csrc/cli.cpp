@@ -9,6 +9,7 @@
 //                  [--prefix-dims D] [--selection threshold|local] [--batch 4096]
 //                  [--precision sq16] [--engine gpu|amx|avx512] [--coarse batched]
 //                  [--repeat 3] [--threads T] [--query-ids FILE] [--out PREFIX]
+//                  [--code-cache]
 //   katoann load   --index PREFIX --queries Q.fbin --rate QPS [--requests 10000]
 //                  [--nprobe 64] [--max-batch 4096] [--seed 42] and the search flags
 //
@@ -70,7 +71,7 @@ struct Args {
 };
 
 Args parse(int argc, char **argv, int first) {
-  static const std::set<std::string> kSwitches = {"normalize", "normalized"};
+  static const std::set<std::string> kSwitches = {"normalize", "normalized", "code-cache"};
   Args a;
   for (int i = first; i < argc; ++i) {
     std::string s = argv[i];
@@ -131,6 +132,7 @@ katoann::LoadOptions load_options(const Args &a) {
   if (coarse == "flat") o.batched_coarse = false;
   else if (coarse != "batched") throw std::invalid_argument("--coarse is batched or flat");
   o.max_batch = std::max(a.u32("batch", 4096), a.u32("max-batch", 4096));
+  o.code_cache = a.has("code-cache");  // PREFIX.gpucodes (an addition to the reference's flags)
   return o;
 }
 
@@ -354,6 +356,7 @@ void usage() {
                "                      [--prefix-dims D] [--selection threshold|local] [--batch 4096]\n"
                "                      [--precision sq16] [--engine gpu] [--coarse batched]\n"
                "                      [--repeat 3] [--threads T] [--query-ids FILE] [--out PREFIX]\n"
+               "                      [--code-cache]\n"
                "       katoann load   --index PREFIX --queries Q.fbin --rate QPS [--requests 10000]\n"
                "                      [--nprobe 64] [--max-batch 4096] [--seed 42] and the search\n"
                "                      flags\n");

@@ -10,6 +10,7 @@
 
 #include <algorithm>
 #include <cfloat>
+#include <cstdio>
 #include <cmath>
 #include <cstring>
 #include <fstream>
@@ -76,6 +77,8 @@ struct Index::State {
   float lo = 0;
   double inv_step = 0, step = 0, step_sq = 0;
   std::vector<uint32_t> sizes;
+  uint64_t source[4] = {0, 0, 0, 0};  // the index files the codes came from (code cache)
+  uint32_t req_prefix = 0;            // the prefix_dims the load was asked for
   DevBuf rot, hi, lop, norm, hinorm, headnorm, ids, list_off, chi, clo, cnorm, chi16, clo16, cterm;
   katoann_gpu_index view{};
   cudaStream_t stream = nullptr;
@@ -109,7 +112,199 @@ Index::~Index() = default;
 Index::Index(Index &&) noexcept = default;
 Index &Index::operator=(Index &&) noexcept = default;
 
+// ------------------------------------------------------------ code cache
+// File: a CodeHeader, then the arrays below in order, each as a uint64 byte
+// count and the bytes.
+namespace {
+
+constexpr uint32_t kCodeMagic = 0x4443474Bu;  // "KGCD"
+constexpr uint32_t kCodeVersion = 1;
+
+struct CodeHeader {
+  uint32_t magic, version, dim, nlist, npts, dc, head, max_list, rotated, normalized, req_prefix,
+      pad;
+  float lo, pad2;
+  double inv_step, step, step_sq;
+  uint64_t source[4];
+};
+
+uint64_t fnv1a(uint64_t h, const char *p, size_t n) {
+  for (size_t i = 0; i < n; ++i) h = (h ^ static_cast<unsigned char>(p[i])) * 0x100000001B3ull;
+  return h;
+}
+
+// Sizes and content hashes of the index files: .meta, .centroids and .dimc
+// whole; .invlist by its size and its first and last MiB.
+void file_signature(const std::string &prefix, uint64_t out[4]) {
+  uint64_t h = 0xCBF29CE484222325ull, sizes = 0;
+  std::vector<char> buf;
+  for (const char *ext : {".meta", ".centroids", ".dimc", ".invlist"}) {
+    std::ifstream f(prefix + ext, std::ios::binary | std::ios::ate);
+    const uint64_t n = f ? static_cast<uint64_t>(f.tellg()) : 0;
+    sizes = sizes * 0x9E3779B97F4A7C15ull + n + 1;
+    if (!f || n == 0) continue;
+    const bool whole = std::string(ext) != ".invlist";
+    const uint64_t part = whole ? n : std::min<uint64_t>(n, 1u << 20);
+    buf.resize(part);
+    f.seekg(0);
+    f.read(buf.data(), static_cast<std::streamsize>(part));
+    h = fnv1a(h, buf.data(), part);
+    if (!whole && n > part) {
+      f.seekg(static_cast<std::streamoff>(n - part));
+      f.read(buf.data(), static_cast<std::streamsize>(part));
+      h = fnv1a(h, buf.data(), part);
+    }
+  }
+  out[0] = sizes;
+  out[1] = h;
+  out[2] = out[3] = 0;
+}
+
+// Device <-> file through one pinned bounce buffer.
+struct Pinned {
+  void *p = nullptr;
+  size_t n = 0;
+  explicit Pinned(size_t bytes) : n(bytes) { cuda_check(cudaMallocHost(&p, bytes), "cudaMallocHost"); }
+  ~Pinned() { cudaFreeHost(p); }
+};
+
+void put(std::ofstream &f, const void *dev, uint64_t bytes, Pinned &pin) {
+  f.write(reinterpret_cast<const char *>(&bytes), 8);
+  for (uint64_t o = 0; o < bytes; o += pin.n) {
+    const size_t c = static_cast<size_t>(std::min<uint64_t>(pin.n, bytes - o));
+    cuda_check(cudaMemcpy(pin.p, static_cast<const char *>(dev) + o, c, cudaMemcpyDeviceToHost), "save codes");
+    f.write(static_cast<const char *>(pin.p), static_cast<std::streamsize>(c));
+  }
+  if (!f) throw std::runtime_error("cannot write the code cache");
+}
+
+void get(std::ifstream &f, DevBuf &b, uint64_t expect, Pinned &pin, const std::string &path) {
+  uint64_t bytes = 0;
+  f.read(reinterpret_cast<char *>(&bytes), 8);
+  if (!f || bytes != expect) throw std::runtime_error("bad array in " + path);
+  b.alloc(static_cast<size_t>(bytes));
+  for (uint64_t o = 0; o < bytes; o += pin.n) {
+    const size_t c = static_cast<size_t>(std::min<uint64_t>(pin.n, bytes - o));
+    f.read(static_cast<char *>(pin.p), static_cast<std::streamsize>(c));
+    if (!f) throw std::runtime_error("truncated " + path);
+    cuda_check(cudaMemcpy(static_cast<char *>(b.p) + o, pin.p, c, cudaMemcpyHostToDevice), "load codes");
+  }
+}
+
+}  // namespace
+
+void Index::save_codes(const std::string &path) const {
+  if (!s_) throw std::logic_error("save_codes before load");
+  const State &s = *s_;
+  cuda_check(cudaStreamSynchronize(s.stream), "save codes");
+  std::ofstream f(path, std::ios::binary | std::ios::trunc);
+  if (!f) throw std::runtime_error("cannot open " + path);
+  CodeHeader h{};
+  h.magic = kCodeMagic;
+  h.version = kCodeVersion;
+  h.dim = s.dim, h.nlist = s.nlist, h.npts = s.npts, h.dc = s.dc, h.head = s.head;
+  h.max_list = s.max_list, h.rotated = s.rotated, h.normalized = s.normalized;
+  h.req_prefix = s.req_prefix;
+  h.lo = s.lo, h.inv_step = s.inv_step, h.step = s.step, h.step_sq = s.step_sq;
+  std::memcpy(h.source, s.source, sizeof(h.source));
+  f.write(reinterpret_cast<const char *>(&h), sizeof(h));
+  const uint64_t L = s.nlist;
+  f.write(reinterpret_cast<const char *>(s.sizes.data()), static_cast<std::streamsize>(L * 4));
+  Pinned pin(64u << 20);
+  const uint64_t n = s.npts, dc = s.dc;
+  put(f, s.ids.p, n * 4, pin);
+  put(f, s.hi.p, n * dc, pin);
+  put(f, s.lop.p, n * dc, pin);
+  put(f, s.norm.p, n * 8, pin);
+  put(f, s.hinorm.p, n * 8, pin);
+  if (s.head) put(f, s.headnorm.p, n * 8, pin);
+  if (s.rotated) put(f, s.rot.p, static_cast<uint64_t>(s.dim) * s.dim * 4, pin);
+  put(f, s.chi.p, L * dc, pin);
+  put(f, s.clo.p, L * dc, pin);
+  put(f, s.cnorm.p, L * 8, pin);
+  put(f, s.chi16.p, L * dc * 2, pin);
+  put(f, s.clo16.p, L * dc * 2, pin);
+  put(f, s.cterm.p, L * 8, pin);
+  f.flush();
+  if (!f) throw std::runtime_error("cannot write " + path);
+}
+
+void Index::load_codes(const std::string &path, const LoadOptions &opt) {
+  std::ifstream f(path, std::ios::binary);
+  if (!f) throw std::runtime_error("cannot open " + path);
+  CodeHeader h{};
+  f.read(reinterpret_cast<char *>(&h), sizeof(h));
+  if (!f || h.magic != kCodeMagic || h.version != kCodeVersion || h.dim == 0 || h.dim > kMaxDim ||
+      h.nlist == 0 || h.dc != round_up(h.dim, 64u) || h.head > h.dc)
+    throw std::runtime_error("bad header in " + path);
+  s_.reset();
+  auto st = std::make_unique<State>();
+  State &s = *st;
+  s.dim = h.dim, s.nlist = h.nlist, s.npts = h.npts, s.dc = h.dc, s.head = h.head;
+  s.rotated = h.rotated != 0, s.normalized = h.normalized != 0, s.req_prefix = h.req_prefix;
+  s.lo = h.lo, s.inv_step = h.inv_step, s.step = h.step, s.step_sq = h.step_sq;
+  std::memcpy(s.source, h.source, sizeof(s.source));
+  s.max_batch = std::max(1u, opt.max_batch);
+  const uint64_t L = s.nlist, n = s.npts, dc = s.dc;
+  s.sizes.assign(L, 0);
+  f.read(reinterpret_cast<char *>(s.sizes.data()), static_cast<std::streamsize>(L * 4));
+  if (!f) throw std::runtime_error("truncated " + path);
+  std::vector<uint32_t> off(L + 1, 0);
+  for (uint64_t c = 0; c < L; ++c) {
+    off[c + 1] = off[c] + s.sizes[c];
+    s.max_list = std::max(s.max_list, s.sizes[c]);
+  }
+  if (off[L] != n || s.max_list != h.max_list) throw std::runtime_error("bad list sizes in " + path);
+  cuda_check(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  cuda_check(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming), "cudaEventCreate");
+  s.list_off.alloc((L + 1) * 4);
+  cuda_check(cudaMemcpy(s.list_off.p, off.data(), (L + 1) * 4, cudaMemcpyHostToDevice), "upload");
+  Pinned pin(64u << 20);
+  get(f, s.ids, n * 4, pin, path);
+  get(f, s.hi, n * dc, pin, path);
+  get(f, s.lop, n * dc, pin, path);
+  get(f, s.norm, n * 8, pin, path);
+  get(f, s.hinorm, n * 8, pin, path);
+  if (s.head) get(f, s.headnorm, n * 8, pin, path);
+  if (s.rotated) get(f, s.rot, static_cast<uint64_t>(s.dim) * s.dim * 4, pin, path);
+  get(f, s.chi, L * dc, pin, path);
+  get(f, s.clo, L * dc, pin, path);
+  get(f, s.cnorm, L * 8, pin, path);
+  get(f, s.chi16, L * dc * 2, pin, path);
+  get(f, s.clo16, L * dc * 2, pin, path);
+  get(f, s.cterm, L * 8, pin, path);
+  set_view(s);
+  s_ = std::move(st);
+}
+
 void Index::load(const std::string &prefix, const LoadOptions &opt) {
+  uint64_t sig[4] = {0, 0, 0, 0};
+  if (opt.code_cache) {
+    file_signature(prefix, sig);
+    const std::string path = prefix + ".gpucodes";
+    std::ifstream f(path, std::ios::binary);
+    CodeHeader h{};
+    if (f && f.read(reinterpret_cast<char *>(&h), sizeof(h)) && h.magic == kCodeMagic &&
+        h.version == kCodeVersion && std::memcmp(h.source, sig, sizeof(sig)) == 0 &&
+        h.req_prefix == opt.prefix_dims && opt.precision == Precision::kSq16 && opt.batched_coarse) {
+      f.close();
+      load_codes(path, opt);
+      return;
+    }
+  }
+  load_files(prefix, opt);
+  if (opt.code_cache) {
+    std::memcpy(s_->source, sig, sizeof(sig));
+    s_->req_prefix = opt.prefix_dims;
+    try {
+      save_codes(prefix + ".gpucodes");
+    } catch (const std::runtime_error &) {
+      std::remove((prefix + ".gpucodes").c_str());  // a read-only place: no cache, same index
+    }
+  }
+}
+
+void Index::load_files(const std::string &prefix, const LoadOptions &opt) {
   IndexArrays a;
   std::vector<float> centroids, vectors, rotation;
   std::vector<uint32_t> sizes, ids;
@@ -300,7 +495,12 @@ void Index::load_arrays(const IndexArrays &a, const LoadOptions &opt) {
   }
   cuda_check(cudaStreamSynchronize(s.stream), "load");
   rotd.reset();
+  set_view(s);
+  s_ = std::move(st);
+}
 
+void Index::set_view(State &s) {
+  const uint32_t d = s.dim, dc = s.dc, n = s.npts, L = s.nlist;
   katoann_gpu_index &v = s.view;
   v.dim = d;
   v.dc = dc;
@@ -326,7 +526,6 @@ void Index::load_arrays(const IndexArrays &a, const LoadOptions &opt) {
   v.d_chi16 = s.chi16.as<uint16_t>();
   v.d_clo16 = s.clo16.as<uint16_t>();
   v.d_cterm = s.cterm.as<int64_t>();
-  s_ = std::move(st);
 }
 
 namespace {

@@ -45,6 +45,9 @@ def _load():
     lib.katoann_index_new.restype = P
     lib.katoann_index_free.argtypes = [P]
     lib.katoann_index_load.argtypes = [P, C.c_char_p, I32, I32, U32, I32, U32]
+    lib.katoann_index_load_cached.argtypes = [P, C.c_char_p, U32, U32]
+    lib.katoann_index_save_codes.argtypes = [P, C.c_char_p]
+    lib.katoann_index_load_codes.argtypes = [P, C.c_char_p, U32]
     lib.katoann_index_load_arrays.argtypes = [P, U32, U32, U32, I32, P, P, P, P, P, I32, U32, I32,
                                               U32, U32]
     lib.katoann_index_search.argtypes = [P, P, U32, U32, U32, I32, U32, I32, P, P]
@@ -185,11 +188,26 @@ class Index:
             self._h = None
 
     def load(self, prefix: str, precision: str = "sq16", use_amx: bool = True, prefix_dims: int = 0,
-             batched_coarse: bool = True, max_batch: int = 4096) -> None:
+             batched_coarse: bool = True, max_batch: int = 4096, code_cache: bool = False) -> None:
+        """The reference's Index.load; code_cache=True goes through PREFIX.gpucodes
+        (see save_codes)."""
         if precision not in ("sq16", "bf16"):
             raise ValueError("precision is 'sq16' or 'bf16'")
+        if code_cache and precision == "sq16" and batched_coarse:
+            _check(_lib.katoann_index_load_cached(self._h, prefix.encode(), prefix_dims, max_batch))
+            return
         _check(_lib.katoann_index_load(self._h, prefix.encode(), 1 if precision == "bf16" else 0,
                                        int(use_amx), prefix_dims, int(batched_coarse), max_batch))
+
+    def save_codes(self, path: str) -> None:
+        """The loaded index as it lives on the device, to one file (the
+        device-code cache; no counterpart in the reference)."""
+        _check(_lib.katoann_index_save_codes(self._h, path.encode()))
+
+    def load_codes(self, path: str, max_batch: int = 4096) -> None:
+        """An index from a file written by save_codes: no float vectors are read
+        and nothing is re-coded."""
+        _check(_lib.katoann_index_load_codes(self._h, path.encode(), max_batch))
 
     def load_arrays(self, centroids, list_sizes, ids, vectors, rotation=None, head_dims: int = 0,
                     has_dimc: bool | None = None, normalized: bool = False, prefix_dims: int = 0,
