@@ -67,12 +67,22 @@ enum class Selection {
   kLocal,      // a top-S per (query, list), merged after the scan
 };
 
+class ProbeModel;  // include/katoann/probe.h
+
 struct SearchParams {
   uint32_t k = 10;
   uint32_t nprobe = 64;
   Ranking ranking = Ranking::kPrefix;
   uint32_t survivors = 32;      // candidates refined per query (at least k)
   Selection selection = Selection::kThreshold;
+  // Additions: a per-query nprobe, capped at nprobe. Either given
+  // (nprobe_per_query, nq values) or chosen by a learned model (budget, with
+  // its cumulative-probability threshold); nprobe_used receives every query's
+  // nprobe. Host memory in search(), device memory in search_device().
+  const ProbeModel *budget = nullptr;
+  float budget_threshold = 0.95f;
+  const uint32_t *nprobe_per_query = nullptr;
+  uint32_t *nprobe_used = nullptr;
 };
 
 // An index given as arrays (lists concatenated in list order). Pointers are

@@ -65,6 +65,57 @@ int katoann_index_search_device(void *index, const float *d_queries, uint32_t nq
                                 uint32_t nprobe, int ranking, uint32_t survivors, int selection,
                                 uint32_t *d_ids, float *d_dists, void *stream, void *timer);
 
+/* Index.search with a per-query nprobe (SearchParams::budget /
+ * nprobe_per_query / nprobe_used; no counterpart in the reference): model is
+ * a katoann_probe_* handle or NULL, nprobe_in (nq values, capped at nprobe)
+ * or NULL, nprobe_out (nq values) or NULL. */
+int katoann_index_search_budget(void *index, const float *queries, uint32_t nq, uint32_t k,
+                                uint32_t nprobe, int ranking, uint32_t survivors, int selection,
+                                const void *model, float threshold, const uint32_t *nprobe_in,
+                                uint32_t *nprobe_out, uint32_t *ids, float *dists);
+
+/* katoann_index_search_device with the per-query nprobe of
+ * katoann_index_search_budget (d_nprobe_in / d_nprobe_out: device memory). */
+int katoann_index_search_device_budget(void *index, const float *d_queries, uint32_t nq,
+                                       uint32_t k, uint32_t nprobe, int ranking,
+                                       uint32_t survivors, int selection, const void *model,
+                                       float threshold, const uint32_t *d_nprobe_in,
+                                       uint32_t *d_nprobe_out, uint32_t *d_ids, float *d_dists,
+                                       void *stream, void *timer);
+
+/* ------------------------------------------------ learned probe budget
+ * katoann::ProbeModel (include/katoann/probe.h). train: labels nq queries by
+ * searching the index and trains on the device; options as in
+ * ProbeTrainOptions (ranking 0 full, 1 high, 2 prefix). */
+int katoann_probe_train(void *index, const float *queries, uint32_t nq, const uint32_t *ladder,
+                        uint32_t nladder, uint32_t depth, uint32_t k, uint32_t label_nprobe,
+                        int ranking, uint32_t survivors, uint32_t epochs, uint32_t batch,
+                        float lr, float weight_decay, uint64_t seed, void **model);
+/* ProbeModel::fit on given raw features (n x 64) and class labels. */
+int katoann_probe_fit(const float *z, const uint8_t *labels, uint32_t n, const uint32_t *ladder,
+                      uint32_t nladder, uint32_t depth, uint32_t epochs, uint32_t batch,
+                      float lr, float weight_decay, uint64_t seed, void **model);
+int katoann_probe_load(const char *path, void **model);
+int katoann_probe_save(const void *model, const char *path);
+void katoann_probe_free(void *model);
+/* info[2] = {classes, depth}; ladder and ranks (64) may be NULL. */
+int katoann_probe_info(const void *model, uint32_t *info, uint32_t *ladder, uint32_t *ranks);
+/* Training record: labels (n values) and per-epoch loss (epochs values);
+ * *n and *epochs receive the counts when the arrays are NULL. */
+int katoann_probe_record(const void *model, uint8_t *labels, uint32_t *n, float *loss,
+                         uint32_t *epochs);
+/* The weights as the device uses them: shift, scale (64 each), w1 (64 x 256
+ * bf16), b1 (256), w2 (256 x 256 bf16), b2 (256), w3 (256 x classes bf16),
+ * b3 (classes). */
+int katoann_probe_weights(const void *model, float *shift, float *scale, uint16_t *w1, float *b1,
+                          uint16_t *w2, float *b2, uint16_t *w3, float *b3);
+/* Raw features of nq queries at `depth` (nq x 64) and the model's output on
+ * feature rows (probs n x classes and nprobe n, either may be NULL). */
+int katoann_probe_features(void *index, const float *queries, uint32_t nq, uint32_t depth,
+                           float *z);
+int katoann_probe_predict(const void *model, const float *z, uint32_t n, float threshold,
+                          uint32_t cap, float *probs, uint32_t *nprobe);
+
 /* info[8] = {dim, nlist, size, prefix_dims, rotated, normalized, batched_coarse, engine=2} */
 int katoann_index_info(void *index, uint32_t *info);
 size_t katoann_index_memory_bytes(void *index);

@@ -161,10 +161,11 @@ int katoann_gpu_search(const katoann_gpu_index *index, const float *d_queries, u
 /* Phase timer: CUDA events recorded on the search stream at the boundaries of
  * the pipeline's phases, so the duration of every phase of every pass in a
  * timed region is measured where it runs. Phases: 0 rotation+quantization of
- * the queries, 1 coarse product, 2 top-nprobe selection, 3 inversion,
- * 4 seed bounds of the tensor-core ranking pass (empty on the CUDA-core
- * pass), 5 ranking pass, 6 survivor merge, 7 refinement. */
-#define KATO_PHASES 8
+ * the queries, 1 coarse product, 2 top-nprobe selection, 3 per-query probe
+ * budget (empty without one), 4 inversion, 5 seed bounds of the tensor-core
+ * ranking pass (empty on the CUDA-core pass), 6 ranking pass, 7 survivor
+ * merge, 8 refinement. */
+#define KATO_PHASES 9
 void *katoann_gpu_timer_create(uint32_t max_passes);
 void katoann_gpu_timer_destroy(void *timer);
 /* Sums the phase durations (ms) of all passes recorded since the last read
@@ -232,6 +233,105 @@ int katoann_gpu_copy_to_host(void *h_dst, const void *d_src, size_t n);
  * the exact conversion every kernel uses). */
 int katoann_gpu_dist_values(const int64_t *d_l2, uint32_t n, double step_sq, float *d_out,
                             katoann_stream_t stream);
+
+/* ------------------------------------------------- learned probe budget
+ * No counterpart in the reference, whose nprobe is one value for a whole
+ * batch (SearchParams::nprobe, include/katoann/index.h:53). Here every query
+ * may probe its own number of lists: the p_q nearest by (coarse distance,
+ * list id), so a query's result is exactly the fixed-nprobe result at
+ * nprobe = p_q. The budget comes either from the caller or from a small MLP
+ * over the query's sorted coarse distances.
+ *
+ * Features: with d_r the r-th smallest coarse distance of the query (r from
+ * 0), r_j the model's 64 ranks (r_0 = 0, ascending) and
+ * e = 1e-4 d_{r_63} + 1e-30,
+ *   z_0 = log(d_0 + e),   z_j = log(d_{r_j} + e) - log(d_0 + e)  (j >= 1),
+ * standardized as x_j = (z_j - shift_j) * scale_j. The MLP is
+ * 64 -> 256 (ReLU) -> 256 (ReLU) -> nclass: bf16 weights stored input-major
+ * (w[i * outputs + o]), fp32 biases, fp32 accumulation. Its budget is
+ * ladder[c] for the smallest class c whose cumulative softmax probability
+ * reaches `threshold` (the last class if none does), capped at the search's
+ * nprobe. */
+#define KATO_PROBE_FEATURES 64
+#define KATO_PROBE_HIDDEN 256
+#define KATO_PROBE_MAX_CLASSES 32
+
+typedef struct {
+  uint32_t nclass;          /* 2 .. KATO_PROBE_MAX_CLASSES */
+  uint32_t depth;           /* d_rank[63] + 1: how many coarse ranks the features read */
+  float threshold;          /* cumulative probability the budget must reach */
+  uint32_t reserved;
+  const uint32_t *d_rank;   /* 64 */
+  const float *d_shift;     /* 64 */
+  const float *d_scale;     /* 64 */
+  const uint16_t *d_w1;     /* 64 x 256 bf16 */
+  const float *d_b1;        /* 256 */
+  const uint16_t *d_w2;     /* 256 x 256 bf16 */
+  const float *d_b2;        /* 256 */
+  const uint16_t *d_w3;     /* 256 x nclass bf16 */
+  const float *d_b3;        /* nclass */
+  const uint32_t *d_ladder; /* nclass nprobe values, ascending */
+} katoann_gpu_probe_model;
+
+/* katoann_gpu_search_timed with a per-query nprobe. `nprobe` caps every
+ * query's budget. The budget is d_nprobe_in[q] (device, nq values, each
+ * clamped to [1, nprobe]) when given, else the model's choice when `model` is
+ * given, else nprobe. The coarse selection takes P = max(nprobe,
+ * model->depth) lists per query (P <= 4096 when a budget applies); size the
+ * workspace with katoann_gpu_search_workspace(..., nprobe = P, ...).
+ * d_nprobe_out (device, nq values, may be NULL) receives every query's
+ * budget. */
+int katoann_gpu_search_budget(const katoann_gpu_index *index, const float *d_queries,
+                              uint32_t nq, uint32_t k, uint32_t nprobe, int ranking,
+                              uint32_t survivors, uint32_t max_batch,
+                              const uint32_t *d_nprobe_in, const katoann_gpu_probe_model *model,
+                              void *d_ws, size_t ws_bytes, uint32_t *d_ids, float *d_dists,
+                              uint32_t *d_nprobe_out, katoann_stream_t stream, void *timer);
+
+/* The 64 raw features z (before standardization) of nq queries into d_z
+ * (nq x 64, device): rotation, quantization, coarse product and selection of
+ * the `depth` nearest lists, as in the search. The workspace is sized with
+ * katoann_gpu_search_workspace(index, max_batch, 1, depth, KATO_RANK_FULL, 1). */
+int katoann_gpu_probe_features(const katoann_gpu_index *index, const float *d_queries,
+                               uint32_t nq, const uint32_t *d_rank, uint32_t depth,
+                               uint32_t max_batch, void *d_ws, size_t ws_bytes, float *d_z,
+                               katoann_stream_t stream);
+
+/* The model on n raw feature rows d_z: class probabilities into d_probs
+ * (n x nclass, may be NULL) and budgets, capped at `cap`, into d_nprobe (n,
+ * may be NULL). */
+int katoann_gpu_probe_predict(const katoann_gpu_probe_model *model, const float *d_z, uint32_t n,
+                              uint32_t cap, float *d_probs, uint32_t *d_nprobe,
+                              katoann_stream_t stream);
+
+typedef struct {
+  uint32_t epochs;     /* passes over the data */
+  uint32_t batch;      /* rows per step */
+  float lr;            /* Adam step size */
+  float weight_decay;  /* decoupled, on the weights only */
+  uint64_t seed;       /* initial weights and the order of the rows */
+} katoann_gpu_probe_train_options;
+
+/* Trains the MLP with softmax cross-entropy and Adam on n rows of raw
+ * features d_z (n x 64) and classes d_label (n values < nclass), on the
+ * device (synchronous; allocates its own device memory). The forward pass
+ * uses bf16 copies of fp32 master weights. Outputs (host): the
+ * standardization (h_shift, h_scale: the features' mean and 1 / standard
+ * deviation), the trained weights in fp32 (h_w1 64 x 256, h_b1 256, h_w2
+ * 256 x 256, h_b2 256, h_w3 256 x nclass, h_b3 nclass; round them to bf16 for
+ * a model) and the mean loss of every epoch (h_loss, `epochs` values). */
+int katoann_gpu_probe_train(const float *d_z, const uint8_t *d_label, uint32_t n,
+                            uint32_t nclass, const katoann_gpu_probe_train_options *options,
+                            float *h_shift, float *h_scale, float *h_w1, float *h_b1, float *h_w2,
+                            float *h_b2, float *h_w3, float *h_b3, float *h_loss);
+
+/* Mean cross-entropy loss of the model on n rows and its gradients with
+ * respect to the weights (as fp32; test hook of the training kernels):
+ * d_g = {w1, b1, w2, b2, w3, b3}, each sized like the parameter (device).
+ * Synchronous. */
+int katoann_gpu_probe_grads(const katoann_gpu_probe_model *model, const float *d_z,
+                            const uint8_t *d_label, uint32_t n, float *h_loss, float *d_gw1,
+                            float *d_gb1, float *d_gw2, float *d_gb2, float *d_gw3, float *d_gb3);
 
 #ifdef __cplusplus
 }

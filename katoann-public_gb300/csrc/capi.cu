@@ -8,6 +8,7 @@
 #include <cuda_fp16.h>
 
 #include "kcommon.cuh"
+#include "probe.cuh"
 
 namespace kato {
 
@@ -37,7 +38,11 @@ int select_topp(const float *dists, uint32_t nq, uint32_t n, uint32_t p, uint32_
 int dist_values(const int64_t *l2, uint32_t n, double step_sq, float *out, cudaStream_t st);
 int search(const katoann_gpu_index *ix, const float *queries, uint32_t nq, uint32_t k, uint32_t p,
            int ranking, uint32_t survivors, uint32_t max_batch, void *ws, size_t ws_bytes,
-           uint32_t *out_ids, float *out_dists, cudaStream_t st, void *timer);
+           uint32_t *out_ids, float *out_dists, const Budget &budget, cudaStream_t st,
+           void *timer);
+int probe_features_search(const katoann_gpu_index *ix, const float *queries, uint32_t nq,
+                          const uint32_t *rank, uint32_t depth, uint32_t max_batch, void *ws,
+                          size_t ws_bytes, float *z, cudaStream_t st);
 void *timer_create(uint32_t max_passes);
 uint32_t last_launches();
 int centre_planes(const uint8_t *hi, const uint8_t *lo, const int64_t *norm, uint32_t rows,
@@ -154,7 +159,7 @@ int katoann_gpu_search(const katoann_gpu_index *ix, const float *d_queries, uint
     return KATO_ELOGIC;
   }
   return kato::search(ix, d_queries, nq, k, nprobe, ranking, survivors, max_batch, d_ws, ws_bytes,
-                      d_ids, d_dists, as_stream(stream), nullptr);
+                      d_ids, d_dists, kato::Budget{}, as_stream(stream), nullptr);
 }
 
 int katoann_gpu_search_timed(const katoann_gpu_index *ix, const float *d_queries, uint32_t nq,
@@ -167,7 +172,38 @@ int katoann_gpu_search_timed(const katoann_gpu_index *ix, const float *d_queries
     return KATO_ELOGIC;
   }
   return kato::search(ix, d_queries, nq, k, nprobe, ranking, survivors, max_batch, d_ws, ws_bytes,
-                      d_ids, d_dists, as_stream(stream), timer);
+                      d_ids, d_dists, kato::Budget{}, as_stream(stream), timer);
+}
+
+int katoann_gpu_search_budget(const katoann_gpu_index *ix, const float *d_queries, uint32_t nq,
+                              uint32_t k, uint32_t nprobe, int ranking, uint32_t survivors,
+                              uint32_t max_batch, const uint32_t *d_nprobe_in,
+                              const katoann_gpu_probe_model *model, void *d_ws, size_t ws_bytes,
+                              uint32_t *d_ids, float *d_dists, uint32_t *d_nprobe_out,
+                              katoann_stream_t stream, void *timer) {
+  if (!ix) return kato::invalid("null index");
+  if (ix->nlist == 0) {
+    kato::set_error("search before load");
+    return KATO_ELOGIC;
+  }
+  kato::Budget b;
+  b.nprobe_in = d_nprobe_in;
+  b.model = d_nprobe_in ? nullptr : model;
+  b.nprobe_out = d_nprobe_out;
+  return kato::search(ix, d_queries, nq, k, nprobe, ranking, survivors, max_batch, d_ws, ws_bytes,
+                      d_ids, d_dists, b, as_stream(stream), timer);
+}
+
+int katoann_gpu_probe_features(const katoann_gpu_index *ix, const float *d_queries, uint32_t nq,
+                               const uint32_t *d_rank, uint32_t depth, uint32_t max_batch,
+                               void *d_ws, size_t ws_bytes, float *d_z, katoann_stream_t stream) {
+  if (!ix) return kato::invalid("null index");
+  if (ix->nlist == 0) {
+    kato::set_error("features before load");
+    return KATO_ELOGIC;
+  }
+  return kato::probe_features_search(ix, d_queries, nq, d_rank, depth, max_batch, d_ws, ws_bytes,
+                                     d_z, as_stream(stream));
 }
 
 void *katoann_gpu_timer_create(uint32_t max_passes) { return kato::timer_create(max_passes); }

@@ -1,9 +1,11 @@
 // extern "C" surface of libkatoann.so (include/katoann_c.h).
+#include <algorithm>
 #include <stdexcept>
 #include <string>
 
 #include "dist_value.h"
 #include "katoann/index.h"
+#include "katoann/probe.h"
 #include "katoann_c.h"
 
 namespace {
@@ -28,6 +30,27 @@ int guarded(F &&f) {
 }
 
 katoann::Index *I(void *p) { return static_cast<katoann::Index *>(p); }
+const katoann::ProbeModel *M(const void *p) { return static_cast<const katoann::ProbeModel *>(p); }
+
+katoann::Ranking ranking_of(int r) {
+  return r == 0 ? katoann::Ranking::kFull
+         : r == 1 ? katoann::Ranking::kHighBytes
+                  : katoann::Ranking::kPrefix;
+}
+
+katoann::ProbeTrainOptions train_options(const uint32_t *ladder, uint32_t nladder, uint32_t depth,
+                                         uint32_t epochs, uint32_t batch, float lr, float wd,
+                                         uint64_t seed) {
+  katoann::ProbeTrainOptions o;
+  if (ladder) o.ladder.assign(ladder, ladder + nladder);
+  if (depth) o.depth = depth;
+  if (epochs) o.epochs = epochs;
+  if (batch) o.batch = batch;
+  if (lr > 0) o.lr = lr;
+  if (wd >= 0) o.weight_decay = wd;
+  o.seed = seed;
+  return o;
+}
 
 katoann::SearchParams params(uint32_t k, uint32_t nprobe, int ranking, uint32_t survivors,
                              int selection) {
@@ -177,6 +200,107 @@ int katoann_index_stats(void *index, uint64_t *stats, uint32_t n) {
 }
 
 const void *katoann_index_device_view(void *index) { return I(index)->device_view(); }
+
+int katoann_index_search_budget(void *index, const float *queries, uint32_t nq, uint32_t k,
+                                uint32_t nprobe, int ranking, uint32_t survivors, int selection,
+                                const void *model, float threshold, const uint32_t *nprobe_in,
+                                uint32_t *nprobe_out, uint32_t *ids, float *dists) {
+  return guarded([&] {
+    katoann::SearchParams p = params(k, nprobe, ranking, survivors, selection);
+    p.budget = M(model);
+    p.budget_threshold = threshold;
+    p.nprobe_per_query = nprobe_in;
+    p.nprobe_used = nprobe_out;
+    I(index)->search(queries, nq, p, ids, dists);
+  });
+}
+
+int katoann_index_search_device_budget(void *index, const float *d_queries, uint32_t nq,
+                                       uint32_t k, uint32_t nprobe, int ranking,
+                                       uint32_t survivors, int selection, const void *model,
+                                       float threshold, const uint32_t *d_nprobe_in,
+                                       uint32_t *d_nprobe_out, uint32_t *d_ids, float *d_dists,
+                                       void *stream, void *timer) {
+  return guarded([&] {
+    katoann::SearchParams p = params(k, nprobe, ranking, survivors, selection);
+    p.budget = M(model);
+    p.budget_threshold = threshold;
+    p.nprobe_per_query = d_nprobe_in;
+    p.nprobe_used = d_nprobe_out;
+    I(index)->search_device(d_queries, nq, p, d_ids, d_dists, stream, timer);
+  });
+}
+
+int katoann_probe_train(void *index, const float *queries, uint32_t nq, const uint32_t *ladder,
+                        uint32_t nladder, uint32_t depth, uint32_t k, uint32_t label_nprobe,
+                        int ranking, uint32_t survivors, uint32_t epochs, uint32_t batch,
+                        float lr, float weight_decay, uint64_t seed, void **model) {
+  return guarded([&] {
+    katoann::ProbeTrainOptions o =
+        train_options(ladder, nladder, depth, epochs, batch, lr, weight_decay, seed);
+    if (k) o.k = k;
+    o.label_nprobe = label_nprobe;
+    o.ranking = ranking_of(ranking);
+    if (survivors) o.survivors = survivors;
+    *model = new katoann::ProbeModel(katoann::ProbeModel::train(*I(index), queries, nq, o));
+  });
+}
+
+int katoann_probe_fit(const float *z, const uint8_t *labels, uint32_t n, const uint32_t *ladder,
+                      uint32_t nladder, uint32_t depth, uint32_t epochs, uint32_t batch,
+                      float lr, float weight_decay, uint64_t seed, void **model) {
+  return guarded([&] {
+    const katoann::ProbeTrainOptions o =
+        train_options(ladder, nladder, depth, epochs, batch, lr, weight_decay, seed);
+    *model = new katoann::ProbeModel(katoann::ProbeModel::fit(z, labels, n, o));
+  });
+}
+
+int katoann_probe_load(const char *path, void **model) {
+  return guarded([&] { *model = new katoann::ProbeModel(katoann::ProbeModel::load(path)); });
+}
+
+int katoann_probe_save(const void *model, const char *path) {
+  return guarded([&] { M(model)->save(path); });
+}
+
+void katoann_probe_free(void *model) { delete static_cast<katoann::ProbeModel *>(model); }
+
+int katoann_probe_info(const void *model, uint32_t *info, uint32_t *ladder, uint32_t *ranks) {
+  return guarded([&] {
+    const katoann::ProbeModel &m = *M(model);
+    info[0] = m.classes();
+    info[1] = m.depth();
+    if (ladder) std::copy(m.ladder().begin(), m.ladder().end(), ladder);
+    if (ranks) std::copy(m.feature_ranks().begin(), m.feature_ranks().end(), ranks);
+  });
+}
+
+int katoann_probe_record(const void *model, uint8_t *labels, uint32_t *n, float *loss,
+                         uint32_t *epochs) {
+  return guarded([&] {
+    const katoann::ProbeModel &m = *M(model);
+    if (labels) std::copy(m.labels().begin(), m.labels().end(), labels);
+    if (n) *n = static_cast<uint32_t>(m.labels().size());
+    if (loss) std::copy(m.loss().begin(), m.loss().end(), loss);
+    if (epochs) *epochs = static_cast<uint32_t>(m.loss().size());
+  });
+}
+
+int katoann_probe_weights(const void *model, float *shift, float *scale, uint16_t *w1, float *b1,
+                          uint16_t *w2, float *b2, uint16_t *w3, float *b3) {
+  return guarded([&] { M(model)->weights(shift, scale, w1, b1, w2, b2, w3, b3); });
+}
+
+int katoann_probe_features(void *index, const float *queries, uint32_t nq, uint32_t depth,
+                           float *z) {
+  return guarded([&] { katoann::ProbeModel::features(*I(index), queries, nq, depth, z); });
+}
+
+int katoann_probe_predict(const void *model, const float *z, uint32_t n, float threshold,
+                          uint32_t cap, float *probs, uint32_t *nprobe) {
+  return guarded([&] { M(model)->predict(z, n, threshold, cap, probs, nprobe); });
+}
 
 void katoann_normalize_rows(float *rows, size_t n, uint32_t dim) {
   katoann::normalize_rows(rows, n, dim);

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "katoann/index.h"
+#include "katoann/probe.h"
 #include "katoann_gpu.h"
 
 namespace katoann {
@@ -84,7 +85,7 @@ struct Index::State {
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
   mutable std::mutex mu;
-  mutable DevBuf ws, dq, dids, ddists;
+  mutable DevBuf ws, dq, dids, ddists, dnp_in, dnp_out;
   mutable void *last_stream = nullptr;
 
   ~State() {
@@ -543,6 +544,29 @@ void validate(const void *state, uint32_t nlist, uint32_t head, const SearchPara
     throw std::invalid_argument("prefix ranking needs the rotation file (.dimc)");
 }
 
+// The per-query budget of a search: the device model (when the params carry
+// one and no explicit budgets) and the selection depth the workspace needs.
+struct BudgetPlan {
+  bool active = false;
+  bool use_model = false;
+  katoann_gpu_probe_model model{};
+  uint32_t depth = 0;
+};
+
+BudgetPlan budget_plan(const SearchParams &p, uint32_t nlist) {
+  BudgetPlan b;
+  b.depth = p.nprobe;
+  b.active = p.budget || p.nprobe_per_query;
+  if (p.budget && !p.nprobe_per_query) {
+    if (p.budget->empty()) throw std::invalid_argument("empty probe model");
+    p.budget->device_model(p.budget_threshold, &b.model);
+    b.use_model = true;
+    b.depth = std::max(b.depth, b.model.depth);
+    if (b.depth > nlist) throw std::invalid_argument("the probe model's depth exceeds nlist");
+  }
+  return b;
+}
+
 }  // namespace
 
 void Index::search(const float *queries, uint32_t nq, const SearchParams &p, uint32_t *ids,
@@ -550,15 +574,18 @@ void Index::search(const float *queries, uint32_t nq, const SearchParams &p, uin
   if (nq == 0) return;
   validate(s_.get(), s_ ? s_->nlist : 0, s_ ? s_->head : 0, p);
   State &s = *s_;
+  const BudgetPlan bp = budget_plan(p, s.nlist);
   std::lock_guard<std::mutex> lock(s.mu);
   const uint32_t mb = s.max_batch, b = std::min(nq, mb);
   const int rk = ranking_code(p.ranking);
-  const size_t need = katoann_gpu_search_workspace(&s.view, b, p.k, p.nprobe, rk, p.survivors);
+  const size_t need = katoann_gpu_search_workspace(&s.view, b, p.k, bp.depth, rk, p.survivors);
   if (need == 0) gpu_check(KATO_EINVAL);
   s.ws.ensure(need);
   s.dq.ensure(static_cast<size_t>(b) * s.dim * 4);
   s.dids.ensure(static_cast<size_t>(b) * p.k * 4);
   s.ddists.ensure(static_cast<size_t>(b) * p.k * 4);
+  if (p.nprobe_per_query) s.dnp_in.ensure(static_cast<size_t>(b) * 4);
+  if (p.nprobe_used) s.dnp_out.ensure(static_cast<size_t>(b) * 4);
   if (s.last_stream && s.last_stream != s.stream)
     cuda_check(cudaStreamWaitEvent(s.stream, s.done, 0), "cudaStreamWaitEvent");
   for (uint32_t q0 = 0; q0 < nq; q0 += mb) {
@@ -566,9 +593,26 @@ void Index::search(const float *queries, uint32_t nq, const SearchParams &p, uin
     cuda_check(cudaMemcpyAsync(s.dq.p, queries + static_cast<size_t>(q0) * s.dim,
                                static_cast<size_t>(nb) * s.dim * 4, cudaMemcpyHostToDevice, s.stream),
                "copy queries");
-    gpu_check(katoann_gpu_search(&s.view, s.dq.as<float>(), nb, p.k, p.nprobe, rk, p.survivors, mb,
-                                 s.ws.p, s.ws.n, s.dids.as<uint32_t>(), s.ddists.as<float>(),
-                                 reinterpret_cast<katoann_stream_t>(s.stream)));
+    if (bp.active || p.nprobe_used) {
+      if (p.nprobe_per_query)
+        cuda_check(cudaMemcpyAsync(s.dnp_in.p, p.nprobe_per_query + q0, static_cast<size_t>(nb) * 4,
+                                   cudaMemcpyHostToDevice, s.stream),
+                   "copy budgets");
+      gpu_check(katoann_gpu_search_budget(
+          &s.view, s.dq.as<float>(), nb, p.k, p.nprobe, rk, p.survivors, mb,
+          p.nprobe_per_query ? s.dnp_in.as<uint32_t>() : nullptr,
+          bp.use_model ? &bp.model : nullptr, s.ws.p, s.ws.n, s.dids.as<uint32_t>(),
+          s.ddists.as<float>(), p.nprobe_used ? s.dnp_out.as<uint32_t>() : nullptr,
+          reinterpret_cast<katoann_stream_t>(s.stream), nullptr));
+      if (p.nprobe_used)
+        cuda_check(cudaMemcpyAsync(p.nprobe_used + q0, s.dnp_out.p, static_cast<size_t>(nb) * 4,
+                                   cudaMemcpyDeviceToHost, s.stream),
+                   "copy budgets");
+    } else {
+      gpu_check(katoann_gpu_search(&s.view, s.dq.as<float>(), nb, p.k, p.nprobe, rk, p.survivors,
+                                   mb, s.ws.p, s.ws.n, s.dids.as<uint32_t>(),
+                                   s.ddists.as<float>(), reinterpret_cast<katoann_stream_t>(s.stream)));
+    }
     cuda_check(cudaMemcpyAsync(ids + static_cast<size_t>(q0) * p.k, s.dids.p,
                                static_cast<size_t>(nb) * p.k * 4, cudaMemcpyDeviceToHost, s.stream),
                "copy ids");
@@ -589,8 +633,9 @@ void Index::search_device(const float *d_queries, uint32_t nq, const SearchParam
   std::lock_guard<std::mutex> lock(s.mu);
   cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : s.stream;
   const int rk = ranking_code(p.ranking);
+  const BudgetPlan bp = budget_plan(p, s.nlist);
   const size_t need =
-      katoann_gpu_search_workspace(&s.view, std::min(nq, s.max_batch), p.k, p.nprobe, rk, p.survivors);
+      katoann_gpu_search_workspace(&s.view, std::min(nq, s.max_batch), p.k, bp.depth, rk, p.survivors);
   if (need == 0) gpu_check(KATO_EINVAL);
   if (need > s.ws.n) {
     cuda_check(cudaDeviceSynchronize(), "workspace resize");
@@ -598,9 +643,16 @@ void Index::search_device(const float *d_queries, uint32_t nq, const SearchParam
   }
   if (s.last_stream && s.last_stream != st)
     cuda_check(cudaStreamWaitEvent(st, s.done, 0), "cudaStreamWaitEvent");
-  gpu_check(katoann_gpu_search_timed(&s.view, d_queries, nq, p.k, p.nprobe, rk, p.survivors,
-                                     s.max_batch, s.ws.p, s.ws.n, d_ids, d_dists,
-                                     reinterpret_cast<katoann_stream_t>(st), timer));
+  if (bp.active || p.nprobe_used)
+    gpu_check(katoann_gpu_search_budget(&s.view, d_queries, nq, p.k, p.nprobe, rk, p.survivors,
+                                        s.max_batch, p.nprobe_per_query,
+                                        bp.use_model ? &bp.model : nullptr, s.ws.p, s.ws.n, d_ids,
+                                        d_dists, p.nprobe_used,
+                                        reinterpret_cast<katoann_stream_t>(st), timer));
+  else
+    gpu_check(katoann_gpu_search_timed(&s.view, d_queries, nq, p.k, p.nprobe, rk, p.survivors,
+                                       s.max_batch, s.ws.p, s.ws.n, d_ids, d_dists,
+                                       reinterpret_cast<katoann_stream_t>(st), timer));
   cuda_check(cudaEventRecord(s.done, st), "cudaEventRecord");
   s.last_stream = st;
 }

@@ -632,8 +632,9 @@ __device__ __forceinline__ void for_rows_split(const uint8_t *__restrict__ x, ui
 __global__ void __launch_bounds__(256) rank_seed_kernel(
     const uint8_t *__restrict__ xhi, const int64_t *__restrict__ xnorm,
     const uint8_t *__restrict__ qhi, const int64_t *__restrict__ qnorm,
-    const uint32_t *__restrict__ probed, const uint32_t *__restrict__ list_off, uint32_t p,
-    uint32_t dc, uint32_t h, uint32_t S, uint32_t want, int32_t *__restrict__ bound) {
+    const uint32_t *__restrict__ probed, const uint32_t *__restrict__ qprobes,
+    const uint32_t *__restrict__ list_off, uint32_t p, uint32_t dc, uint32_t h, uint32_t S,
+    uint32_t want, int32_t *__restrict__ bound) {
   __shared__ int32_t l2s[kSeedCap];
   __shared__ uint32_t qw[2048 / 4];
   __shared__ uint32_t hist[256], sel[2];
@@ -642,8 +643,9 @@ __global__ void __launch_bounds__(256) rank_seed_kernel(
     qw[i] = reinterpret_cast<const uint32_t *>(qhi + static_cast<size_t>(q) * dc)[i];
   __syncthreads();
   const int64_t qn = qnorm[q];
+  const uint32_t pq = qprobes ? qprobes[q] : p;  // the query's own budget
   uint32_t count = 0;
-  for (uint32_t r = 0; r < p && count < want; ++r) {
+  for (uint32_t r = 0; r < pq && count < want; ++r) {
     const uint32_t c = probed[static_cast<size_t>(q) * p + r];
     const uint32_t r0 = list_off[c], n = min(list_off[c + 1] - r0, kSeedCap - count);
     for_rows_split(xhi, dc, h, qw, r0, n, [&](uint32_t i, uint32_t dot) {
@@ -774,14 +776,15 @@ __global__ void __launch_bounds__(256) rescan_bound_kernel(
 
 __global__ void __launch_bounds__(256) rescan_rows_kernel(
     RowKey key, const uint8_t *__restrict__ qhi, const int64_t *__restrict__ qnorm,
-    const uint32_t *__restrict__ probed, const uint32_t *__restrict__ list_off, uint32_t p,
-    uint32_t *__restrict__ qcount, uint2 *__restrict__ qbuf, uint32_t cap,
-    const uint32_t *__restrict__ list, const unsigned long long *__restrict__ kbound,
-    const uint32_t *__restrict__ nlisted) {
+    const uint32_t *__restrict__ probed, const uint32_t *__restrict__ qprobes,
+    const uint32_t *__restrict__ list_off, uint32_t p, uint32_t *__restrict__ qcount,
+    uint2 *__restrict__ qbuf, uint32_t cap, const uint32_t *__restrict__ list,
+    const unsigned long long *__restrict__ kbound, const uint32_t *__restrict__ nlisted) {
   __shared__ uint32_t qw[2048 / 4];
   const size_t pairs = static_cast<size_t>(*nlisted) * p;
   for (size_t pair = blockIdx.x; pair < pairs; pair += gridDim.x) {
     const uint32_t q = list[pair / p];
+    if (qprobes && pair % p >= qprobes[q]) continue;  // beyond the query's budget
     const uint32_t c = probed[static_cast<size_t>(q) * p + pair % p];
     __syncthreads();
     load_query_words(qhi, q, key.dc, key.h, qw);
@@ -806,8 +809,9 @@ __global__ void __launch_bounds__(256) rescan_rows_kernel(
 
 __global__ void __launch_bounds__(256) rescan_exact_kernel(
     RowKey key, const uint8_t *__restrict__ qhi, const int64_t *__restrict__ qnorm,
-    const uint32_t *__restrict__ probed, const uint32_t *__restrict__ list_off, uint32_t p,
-    uint32_t S, uint32_t *__restrict__ qcount, uint2 *__restrict__ qbuf, uint32_t cap) {
+    const uint32_t *__restrict__ probed, const uint32_t *__restrict__ qprobes,
+    const uint32_t *__restrict__ list_off, uint32_t p, uint32_t S, uint32_t *__restrict__ qcount,
+    uint2 *__restrict__ qbuf, uint32_t cap) {
   const uint32_t q = blockIdx.x, tid = threadIdx.x;
   if (qcount[q] <= cap) return;
   __shared__ uint32_t qw[2048 / 4];
@@ -817,8 +821,9 @@ __global__ void __launch_bounds__(256) rescan_exact_kernel(
   __syncthreads();
   const int64_t qn = qnorm[q];
   const uint32_t *pq = probed + static_cast<size_t>(q) * p;
+  const uint32_t np = qprobes ? qprobes[q] : p;  // the query's own budget
   uint32_t total = 0;
-  for (uint32_t r = 0; r < p; ++r) total += list_off[pq[r] + 1] - list_off[pq[r]];
+  for (uint32_t r = 0; r < np; ++r) total += list_off[pq[r] + 1] - list_off[pq[r]];
   // more than cap >= S candidates, so the S-th smallest key exists
   const unsigned long long K = block_select64(
       total, S - 1,
@@ -834,7 +839,7 @@ __global__ void __launch_bounds__(256) rescan_exact_kernel(
       },
       hist, sel);
   uint2 *buf = qbuf + static_cast<size_t>(q) * cap;
-  for (uint32_t r = 0; r < p; ++r)
+  for (uint32_t r = 0; r < np; ++r)
     for (uint32_t row = list_off[pq[r]] + tid; row < list_off[pq[r] + 1]; row += blockDim.x) {
       const unsigned long long k = key(row, qw, qn);
       if (k <= K) {
@@ -997,11 +1002,12 @@ int rank_tc_bucket(const uint4 *rec, const uint32_t *rec_n, uint32_t rec_cap, ui
 }
 
 int rank_seed(const uint8_t *xhi, const int64_t *xnorm, const uint8_t *qhi, const int64_t *qnorm,
-              const uint32_t *probed, const uint32_t *list_off, uint32_t B, uint32_t p,
+              const uint32_t *probed, const uint32_t *qprobes, const uint32_t *list_off,
+              uint32_t B, uint32_t p,
               uint32_t dc, uint32_t h, uint32_t S, uint32_t rows, int32_t *bound, cudaStream_t st) {
   if (h > 2048 || h % 16) return invalid("seed bounds need h <= 2048, a multiple of 16");
   if (B == 0) return KATO_OK;
-  rank_seed_kernel<<<B, 256, 0, st>>>(xhi, xnorm, qhi, qnorm, probed, list_off, p, dc, h, S,
+  rank_seed_kernel<<<B, 256, 0, st>>>(xhi, xnorm, qhi, qnorm, probed, qprobes, list_off, p, dc, h, S,
                                       std::min(std::max(rows, S), kSeedCap), bound);
   KATO_LAUNCHED("rank_seed_kernel");
   return KATO_OK;
@@ -1020,7 +1026,8 @@ int rank_tc_prepare(const uint32_t *cnt, const uint32_t *list_off, uint32_t L, u
 
 int rank_overflow(const uint8_t *xhi, const int64_t *xnorm, const uint32_t *ids,
                   const uint8_t *qhi, const int64_t *qnorm, const uint32_t *probed,
-                  const uint32_t *list_off, uint32_t B, uint32_t p, uint32_t dc, uint32_t h,
+                  const uint32_t *qprobes, const uint32_t *list_off, uint32_t B, uint32_t p,
+                  uint32_t dc, uint32_t h,
                   uint32_t S, DistScale scale, uint32_t *qcount, uint2 *qbuf, uint32_t cap,
                   const RescanBufs &rb, unsigned long long *stats, cudaStream_t st) {
   if (S > cap) return invalid("candidate buffer smaller than the survivor count");
@@ -1031,10 +1038,12 @@ int rank_overflow(const uint8_t *xhi, const int64_t *xnorm, const uint32_t *ids,
   for (int r = 0; r < kRescanRounds; ++r) {
     rescan_bound_kernel<<<B, 256, 0, st>>>(ids, qcount, rb.qfill, qbuf, cap, S, r, rb.list,
                                            rb.kbound, rb.nlisted + r, stats);
-    rescan_rows_kernel<<<4 * sms, 256, 0, st>>>(key, qhi, qnorm, probed, list_off, p, qcount, qbuf,
-                                                cap, rb.list, rb.kbound, rb.nlisted + r);
+    rescan_rows_kernel<<<4 * sms, 256, 0, st>>>(key, qhi, qnorm, probed, qprobes, list_off, p,
+                                                qcount, qbuf, cap, rb.list, rb.kbound,
+                                                rb.nlisted + r);
   }
-  rescan_exact_kernel<<<B, 256, 0, st>>>(key, qhi, qnorm, probed, list_off, p, S, qcount, qbuf, cap);
+  rescan_exact_kernel<<<B, 256, 0, st>>>(key, qhi, qnorm, probed, qprobes, list_off, p, S, qcount,
+                                         qbuf, cap);
   KATO_LAUNCHED("overflow rescan kernels");
   return KATO_OK;
 }

@@ -85,7 +85,8 @@ int rank_tc(const RankTcArgs &A, const uint8_t *xhi, uint32_t npts, const TcShap
 // Per query, an upper bound on its final S-th ranking l2 from the first
 // `rows` rows (at most 4096) of its probed lists in probe order.
 int rank_seed(const uint8_t *xhi, const int64_t *xnorm, const uint8_t *qhi, const int64_t *qnorm,
-              const uint32_t *probed, const uint32_t *list_off, uint32_t B, uint32_t p,
+              const uint32_t *probed, const uint32_t *qprobes, const uint32_t *list_off,
+              uint32_t B, uint32_t p,
               uint32_t dc, uint32_t h, uint32_t S, uint32_t rows, int32_t *bound, cudaStream_t st);
 // Work items of the pass (per list: groups of N queries) and their tile
 // offsets; also zeroes the B candidate counts and buffer fills. scratch:
@@ -115,7 +116,8 @@ constexpr uint32_t kRescanCounters = 4;
 // stats[0] counts them, stats[1] is the largest candidate count of a query.
 int rank_overflow(const uint8_t *xhi, const int64_t *xnorm, const uint32_t *ids,
                   const uint8_t *qhi, const int64_t *qnorm, const uint32_t *probed,
-                  const uint32_t *list_off, uint32_t B, uint32_t p, uint32_t dc, uint32_t h,
+                  const uint32_t *qprobes, const uint32_t *list_off, uint32_t B, uint32_t p,
+                  uint32_t dc, uint32_t h,
                   uint32_t S, DistScale scale, uint32_t *qcount, uint2 *qbuf, uint32_t cap,
                   const RescanBufs &rb, unsigned long long *stats, cudaStream_t st);
 

@@ -18,6 +18,7 @@
 #include <cuda_fp16.h>
 
 #include "kcommon.cuh"
+#include "probe.cuh"
 #include "rank_tc.cuh"
 #include "scan.cuh"
 
@@ -44,10 +45,18 @@ struct Work {
 };
 
 // ---------------------------------------------------------------- inversion
-__global__ void count_kernel(const uint32_t *__restrict__ probed, uint32_t total,
-                             uint32_t *__restrict__ cnt) {
+// A (query, rank) pair i = query * p + rank is probed when the query's
+// budget (if any) exceeds the rank: its p nearest lists are in order, so a
+// budget of b probes exactly the lists a fixed nprobe of b would.
+__device__ __forceinline__ bool probed_pair(uint32_t i, uint32_t p,
+                                            const uint32_t *__restrict__ qprobes) {
+  return !qprobes || i % p < qprobes[i / p];
+}
+
+__global__ void count_kernel(const uint32_t *__restrict__ probed, uint32_t total, uint32_t p,
+                             const uint32_t *__restrict__ qprobes, uint32_t *__restrict__ cnt) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < total) atomicAdd(&cnt[probed[i]], 1u);
+  if (i < total && probed_pair(i, p, qprobes)) atomicAdd(&cnt[probed[i]], 1u);
 }
 
 // One CTA: exclusive scans of the per-list query counts (off) and of the
@@ -73,11 +82,12 @@ __global__ void __launch_bounds__(1024) scan_kernel(const uint32_t *__restrict__
   }
 }
 
-__global__ void scatter_kernel(const uint32_t *__restrict__ probed, uint32_t total,
+__global__ void scatter_kernel(const uint32_t *__restrict__ probed, uint32_t total, uint32_t p,
+                               const uint32_t *__restrict__ qprobes,
                                const uint32_t *__restrict__ off, uint32_t *__restrict__ cursor,
                                uint32_t *__restrict__ entries) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= total) return;
+  if (i >= total || !probed_pair(i, p, qprobes)) return;
   const uint32_t c = probed[i];
   entries[off[c] + atomicAdd(&cursor[c], 1u)] = i;  // i = query * nprobe + rank
 }
@@ -462,7 +472,7 @@ __device__ void block_sort_pairs(unsigned long long *key, uint32_t *val, uint32_
 // (:1088-1112). The full mode writes the final top-k, ascending, padded.
 __global__ void __launch_bounds__(kThreads) merge_kernel(
     const uint2 *__restrict__ slots, uint32_t per_query, const uint32_t *__restrict__ qcount,
-    const uint32_t *__restrict__ ids,
+    const uint32_t *__restrict__ qprobes, uint32_t per_probe, const uint32_t *__restrict__ ids,
     uint32_t S, bool final_topk, uint32_t k, uint2 *__restrict__ surv, uint32_t *__restrict__ nsurv,
     uint32_t *__restrict__ out_ids, float *__restrict__ out_dists,
     unsigned long long *__restrict__ tie_count) {
@@ -475,7 +485,12 @@ __global__ void __launch_bounds__(kThreads) merge_kernel(
   uint32_t *pos = reinterpret_cast<uint32_t *>(sel + np2);
   const uint32_t q = blockIdx.x;
   const uint2 *e = slots + static_cast<size_t>(q) * per_query;
-  const uint32_t n = qcount ? min(qcount[q], per_query) : per_query;
+  // the tensor-core pass counts each query's candidates; on the CUDA-core
+  // pass a query's slots are its probes' (rank-major), of which the first
+  // budget ones were written
+  const uint32_t n = qcount    ? min(qcount[q], per_query)
+                     : qprobes ? min(per_query, qprobes[q] * per_probe)
+                               : per_query;
   auto K = [&](uint32_t i) { return e[i].x; };
   auto I = [&](uint32_t i) { return ids[e[i].y]; };
   const uint32_t got = block_select(n, S, K, I, sel, pos, hist, scratch, &tie);
@@ -641,7 +656,7 @@ struct Plan {
       off_woff, off_cur, off_work, off_ent, off_slots, off_surv, off_nsurv, off_stats,
       off_tcscratch, off_tcitems, off_tileoff, off_nitems, off_qcount, off_qfill, off_bound,
       off_rec, off_recn, off_rlist, off_rkey, off_rcount, off_qh16, off_ql16, off_qterm, off_rot,
-      total;
+      off_qprobes, off_z, total;
 };
 
 static size_t align256(size_t x) { return (x + 255) / 256 * 256; }
@@ -725,15 +740,19 @@ int make_plan(const katoann_gpu_index *ix, uint32_t B, uint32_t k, uint32_t p, i
   pl.off_rlist = take(static_cast<size_t>(B) * 4);
   pl.off_rkey = take(static_cast<size_t>(B) * 8);
   pl.off_rcount = take(kRescanCounters * 4);
+  pl.off_qprobes = take(static_cast<size_t>(B) * 4);
+  pl.off_z = take(static_cast<size_t>(B) * KATO_PROBE_FEATURES * 4);
   pl.off_surv = take(static_cast<size_t>(B) * pl.S * sizeof(uint2));
   pl.off_nsurv = take(static_cast<size_t>(B) * 4);
   pl.total = o;
   return KATO_OK;
 }
 
-int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *queries, uint32_t nq,
-                unsigned char *ws, uint32_t *out_ids, float *out_dists, cudaStream_t st,
-                PhaseTimer *tm) {
+// Rotation, quantization, coarse product and top-p selection of nq queries
+// (phases 0-2): leaves the query planes, the coarse distances (cd) and each
+// query's p nearest lists in order (probed) in the workspace.
+int coarse_pass(const katoann_gpu_index *ix, const Plan &pl, const float *queries, uint32_t nq,
+                unsigned char *ws, cudaStream_t st, PhaseTimer *tm) {
   int rc;
   const uint32_t L = ix->nlist, p = pl.p, dc = ix->dc;
   float *fq = reinterpret_cast<float *>(ws + pl.off_fq);
@@ -743,15 +762,6 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
   int64_t *qh0 = reinterpret_cast<int64_t *>(ws + pl.off_qh0);
   float *cd = reinterpret_cast<float *>(ws + pl.off_cd);
   uint32_t *probed = reinterpret_cast<uint32_t *>(ws + pl.off_probed);
-  uint32_t *cnt = reinterpret_cast<uint32_t *>(ws + pl.off_cnt);
-  uint32_t *off = reinterpret_cast<uint32_t *>(ws + pl.off_off);
-  uint32_t *woff = reinterpret_cast<uint32_t *>(ws + pl.off_woff);
-  uint32_t *cur = reinterpret_cast<uint32_t *>(ws + pl.off_cur);
-  Work *work = reinterpret_cast<Work *>(ws + pl.off_work);
-  uint32_t *ent = reinterpret_cast<uint32_t *>(ws + pl.off_ent);
-  uint2 *slots = reinterpret_cast<uint2 *>(ws + pl.off_slots);
-  uint2 *surv = reinterpret_cast<uint2 *>(ws + pl.off_surv);
-  uint32_t *nsurv = reinterpret_cast<uint32_t *>(ws + pl.off_nsurv);
   unsigned long long *stats = reinterpret_cast<unsigned long long *>(ws + pl.off_stats);
 
   mark(tm, 0, st);
@@ -788,21 +798,68 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
   mark(tm, 2, st);
   if ((rc = select_topp(cd, nq, L, p, probed, stats + 0, st))) return rc;
   mark(tm, 3, st);
+  return KATO_OK;
+}
+
+int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *queries, uint32_t nq,
+                unsigned char *ws, uint32_t *out_ids, float *out_dists, const Budget &bud,
+                cudaStream_t st, PhaseTimer *tm) {
+  int rc;
+  const uint32_t L = ix->nlist, p = pl.p, dc = ix->dc;
+  uint8_t *qhi = ws + pl.off_qhi, *qlo = ws + pl.off_qlo;
+  int64_t *qn = reinterpret_cast<int64_t *>(ws + pl.off_qn);
+  int64_t *qhn = reinterpret_cast<int64_t *>(ws + pl.off_qhn);
+  int64_t *qh0 = reinterpret_cast<int64_t *>(ws + pl.off_qh0);
+  float *cd = reinterpret_cast<float *>(ws + pl.off_cd);
+  uint32_t *probed = reinterpret_cast<uint32_t *>(ws + pl.off_probed);
+  uint32_t *cnt = reinterpret_cast<uint32_t *>(ws + pl.off_cnt);
+  uint32_t *off = reinterpret_cast<uint32_t *>(ws + pl.off_off);
+  uint32_t *woff = reinterpret_cast<uint32_t *>(ws + pl.off_woff);
+  uint32_t *cur = reinterpret_cast<uint32_t *>(ws + pl.off_cur);
+  Work *work = reinterpret_cast<Work *>(ws + pl.off_work);
+  uint32_t *ent = reinterpret_cast<uint32_t *>(ws + pl.off_ent);
+  uint2 *slots = reinterpret_cast<uint2 *>(ws + pl.off_slots);
+  uint2 *surv = reinterpret_cast<uint2 *>(ws + pl.off_surv);
+  uint32_t *nsurv = reinterpret_cast<uint32_t *>(ws + pl.off_nsurv);
+  unsigned long long *stats = reinterpret_cast<unsigned long long *>(ws + pl.off_stats);
+
+  if ((rc = coarse_pass(ix, pl, queries, nq, ws, st, tm))) return rc;
+  // 2'. per-query budgets: given, or from the model over the coarse distances
+  uint32_t *qprobes = nullptr;
+  if (bud.active()) {
+    qprobes = reinterpret_cast<uint32_t *>(ws + pl.off_qprobes);
+    if (bud.nprobe_in) {
+      if ((rc = clamp_budget(bud.nprobe_in, nq, bud.cap, qprobes, st))) return rc;
+      ++g_launches;
+    } else {
+      float *z = reinterpret_cast<float *>(ws + pl.off_z);
+      if ((rc = probe_features(cd, L, probed, p, bud.model->d_rank, nq, z, st))) return rc;
+      if ((rc = probe_budget(*bud.model, z, nq, bud.cap, nullptr, qprobes, st))) return rc;
+      g_launches += 2;
+    }
+    if (bud.nprobe_out)
+      KATO_CUDA(cudaMemcpyAsync(bud.nprobe_out, qprobes, static_cast<size_t>(nq) * 4,
+                                cudaMemcpyDeviceToDevice, st));
+  } else if (bud.nprobe_out) {
+    if ((rc = clamp_budget(nullptr, nq, p, bud.nprobe_out, st))) return rc;  // all p
+    ++g_launches;
+  }
+  mark(tm, 4, st);
   // 3. inversion (:403-412)
   const uint32_t total = nq * p;
   KATO_CUDA(cudaMemsetAsync(cnt, 0, static_cast<size_t>(L) * 4, st));
-  count_kernel<<<div_up(total, 256), 256, 0, st>>>(probed, total, cnt);
+  count_kernel<<<div_up(total, 256), 256, 0, st>>>(probed, total, p, qprobes, cnt);
   scan_kernel<<<1, 1024, 0, st>>>(cnt, L, off, woff, cur);
-  scatter_kernel<<<div_up(total, 256), 256, 0, st>>>(probed, total, off, cur, ent);
+  scatter_kernel<<<div_up(total, 256), 256, 0, st>>>(probed, total, p, qprobes, off, cur, ent);
   g_launches += 3;
   if (!pl.tc) {
     work_kernel<<<div_up(L, 256), 256, 0, st>>>(cnt, woff, L, work);
     ++g_launches;
   }
   KATO_LAUNCHED("inversion kernels");
-  mark(tm, 4, st);
+  mark(tm, 5, st);
   uint32_t *qcount = nullptr;
-  if (!pl.tc) mark(tm, 5, st);  // no seed-bound phase on the CUDA-core pass
+  if (!pl.tc) mark(tm, 6, st);  // no seed-bound phase on the CUDA-core pass
   if (pl.tc) {
     // 4'. ranking pass on the tensor cores: seed bounds, work items, the
     // scan, and the exact rescan of any query whose buffer overflowed
@@ -818,10 +875,10 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
     const int64_t *xnorm = prefix_mode ? ix->d_headnorm : ix->d_hinorm;
     const int64_t *qnorm = prefix_mode ? qh0 : qhn;
     const DistScale scale = make_dist_scale(ix->step_sq);
-    if ((rc = rank_seed(ix->d_hi, xnorm, qhi, qnorm, probed, ix->d_list_off, nq, p, dc, pl.dims,
-                        pl.S, pl.seed_rows, bound, st)))
+    if ((rc = rank_seed(ix->d_hi, xnorm, qhi, qnorm, probed, qprobes, ix->d_list_off, nq, p, dc,
+                        pl.dims, pl.S, pl.seed_rows, bound, st)))
       return rc;
-    mark(tm, 5, st);
+    mark(tm, 6, st);
     if ((rc = rank_tc_prepare(cnt, ix->d_list_off, L, pl.tcs.N, nq,
                               reinterpret_cast<uint32_t *>(ws + pl.off_tcscratch), items, tile_off,
                               nitems, qcount, qfill, st)))
@@ -852,7 +909,7 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
     const RescanBufs rb{reinterpret_cast<uint32_t *>(ws + pl.off_rlist),
                         reinterpret_cast<unsigned long long *>(ws + pl.off_rkey),
                         reinterpret_cast<uint32_t *>(ws + pl.off_rcount), qfill};
-    if ((rc = rank_overflow(ix->d_hi, xnorm, ix->d_ids, qhi, qnorm, probed, ix->d_list_off, nq, p,
+    if ((rc = rank_overflow(ix->d_hi, xnorm, ix->d_ids, qhi, qnorm, probed, qprobes, ix->d_list_off, nq, p,
                             dc, pl.dims, pl.S, scale, qcount, slots, pl.cap, rb, stats + 6, st)))
       return rc;
     g_launches += 11;  // seed, 3 preparation, scan, bucket, 2 x 2 rescan rounds, exact rescan
@@ -896,21 +953,21 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
     if (rc) return rc;
     ++g_launches;
   }
-  mark(tm, 6, st);
+  mark(tm, 7, st);
   // 5. per-query merge of the slot lists (:1058-1080 / :1205-1218)
   uint32_t np2 = 1;
   while (np2 < pl.S) np2 <<= 1;
   const size_t msmem = static_cast<size_t>(np2) * 12;
   KATO_CUDA(cudaFuncSetAttribute(merge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(msmem)));
-  merge_kernel<<<nq, kThreads, msmem, st>>>(slots, pl.tc ? pl.cap : p * pl.SC, qcount, ix->d_ids,
-                                            pl.S, full, pl.k, surv, nsurv, out_ids, out_dists,
-                                            stats + 1);
+  merge_kernel<<<nq, kThreads, msmem, st>>>(slots, pl.tc ? pl.cap : p * pl.SC, qcount, qprobes,
+                                            pl.SC, ix->d_ids, pl.S, full, pl.k, surv, nsurv,
+                                            out_ids, out_dists, stats + 1);
   ++g_launches;
   KATO_LAUNCHED("merge_kernel");
-  mark(tm, 7, st);
+  mark(tm, 8, st);
   if (full) {
-    mark(tm, 8, st);
+    mark(tm, 9, st);
     if (tm && tm->used < tm->max_passes) ++tm->used;
     return KATO_OK;
   }
@@ -924,18 +981,28 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
                                              make_dist_scale(ix->step_sq), out_ids, out_dists);
   KATO_LAUNCHED("refine_kernel");
   ++g_launches;
-  mark(tm, 8, st);
+  mark(tm, 9, st);
   if (tm && tm->used < tm->max_passes) ++tm->used;
   return KATO_OK;
 }
 
 int search(const katoann_gpu_index *ix, const float *queries, uint32_t nq, uint32_t k, uint32_t p,
            int ranking, uint32_t survivors, uint32_t max_batch, void *ws, size_t ws_bytes,
-           uint32_t *out_ids, float *out_dists, cudaStream_t st, void *timer) {
+           uint32_t *out_ids, float *out_dists, const Budget &budget, cudaStream_t st,
+           void *timer) {
   if (nq == 0) return KATO_OK;
   if (max_batch == 0) return invalid("max_batch must be positive");
+  // with a budget, the selection depth covers the cap and the model's features
+  uint32_t depth = p;
+  if (budget.active()) {
+    if (budget.model) {
+      if (int rc = check_probe_model(*budget.model)) return rc;
+      depth = std::max(depth, budget.model->depth);
+    }
+    if (depth > kSortMax) return invalid("a per-query nprobe needs nprobe (and model depth) <= 4096");
+  }
   Plan pl{};
-  int rc = make_plan(ix, std::min(nq, max_batch), k, p, ranking, survivors, &pl);
+  int rc = make_plan(ix, std::min(nq, max_batch), k, depth, ranking, survivors, &pl);
   if (rc) return rc;
   if (ws_bytes < pl.total) {
     set_error("search workspace too small");
@@ -946,10 +1013,45 @@ int search(const katoann_gpu_index *ix, const float *queries, uint32_t nq, uint3
   g_launches = 0;
   for (uint32_t q0 = 0; q0 < nq; q0 += max_batch) {
     const uint32_t b = std::min(max_batch, nq - q0);
+    Budget bud = budget;
+    bud.cap = p;
+    if (bud.nprobe_in) bud.nprobe_in += q0;
+    if (bud.nprobe_out) bud.nprobe_out += q0;
     if ((rc = search_pass(ix, pl, queries + static_cast<size_t>(q0) * ix->dim, b, w,
                           out_ids + static_cast<size_t>(q0) * k,
-                          out_dists + static_cast<size_t>(q0) * k, st,
+                          out_dists + static_cast<size_t>(q0) * k, bud, st,
                           static_cast<PhaseTimer *>(timer))))
+      return rc;
+  }
+  return KATO_OK;
+}
+
+// The probe-budget features of nq queries (phases 0-2, then the feature
+// kernel), max_batch at a time.
+int probe_features_search(const katoann_gpu_index *ix, const float *queries, uint32_t nq,
+                          const uint32_t *rank, uint32_t depth, uint32_t max_batch, void *ws,
+                          size_t ws_bytes, float *z, cudaStream_t st) {
+  if (nq == 0) return KATO_OK;
+  if (max_batch == 0) return invalid("max_batch must be positive");
+  if (!rank) return invalid("null feature ranks");
+  if (depth == 0 || depth > ix->nlist || depth > kSortMax)
+    return invalid("feature depth must be 1 to min(nlist, 4096)");
+  Plan pl{};
+  int rc = make_plan(ix, std::min(nq, max_batch), 1, depth, KATO_RANK_FULL, 1, &pl);
+  if (rc) return rc;
+  if (ws_bytes < pl.total) {
+    set_error("feature workspace too small");
+    return KATO_ENOMEM;
+  }
+  unsigned char *w = static_cast<unsigned char *>(ws);
+  g_launches = 0;
+  for (uint32_t q0 = 0; q0 < nq; q0 += max_batch) {
+    const uint32_t b = std::min(max_batch, nq - q0);
+    if ((rc = coarse_pass(ix, pl, queries + static_cast<size_t>(q0) * ix->dim, b, w, st, nullptr)))
+      return rc;
+    if ((rc = probe_features(reinterpret_cast<float *>(w + pl.off_cd), ix->nlist,
+                             reinterpret_cast<uint32_t *>(w + pl.off_probed), depth, rank, b,
+                             z + static_cast<size_t>(q0) * KATO_PROBE_FEATURES, st)))
       return rc;
   }
   return KATO_OK;

@@ -8,8 +8,10 @@ GIL during each call, as the reference's module does). There is no CPU
 fallback: importing fails loudly when the libraries are missing.
 
 Additions: ``Index.load_arrays`` (an index from numpy arrays or CUDA tensors),
-``Index.search_device`` (CUDA tensors in and out, no host copies) and
-``Index.search_stats``.
+``Index.search_device`` (CUDA tensors in and out, no host copies),
+``Index.search_stats``, the device-code cache (``save_codes`` / ``load_codes``)
+and the learned per-query probe budget (``ProbeModel``; ``search(...,
+budget=model)`` or ``nprobe_per_query=``).
 """
 from __future__ import annotations
 
@@ -62,6 +64,21 @@ def _load():
     lib.katoann_normalize_rows.argtypes = [P, S, U32]
     lib.katoann_dist_value.argtypes = [C.c_int64, D]
     lib.katoann_dist_value.restype = C.c_float
+    F = C.c_float
+    lib.katoann_index_search_budget.argtypes = [P, P, U32, U32, U32, I32, U32, I32, P, F, P, P, P, P]
+    lib.katoann_index_search_device_budget.argtypes = [P, P, U32, U32, U32, I32, U32, I32, P, F, P,
+                                                       P, P, P, P, P]
+    lib.katoann_probe_train.argtypes = [P, P, U32, P, U32, U32, U32, U32, I32, U32, U32, U32, F, F,
+                                        U64, C.POINTER(P)]
+    lib.katoann_probe_fit.argtypes = [P, P, U32, P, U32, U32, U32, U32, F, F, U64, C.POINTER(P)]
+    lib.katoann_probe_load.argtypes = [C.c_char_p, C.POINTER(P)]
+    lib.katoann_probe_save.argtypes = [P, C.c_char_p]
+    lib.katoann_probe_free.argtypes = [P]
+    lib.katoann_probe_info.argtypes = [P, P, P, P]
+    lib.katoann_probe_record.argtypes = [P, P, P, P, P]
+    lib.katoann_probe_weights.argtypes = [P, P, P, P, P, P, P, P, P]
+    lib.katoann_probe_features.argtypes = [P, P, U32, U32, P]
+    lib.katoann_probe_predict.argtypes = [P, P, U32, F, U32, P, P]
     return lib
 
 
@@ -126,8 +143,8 @@ def dist_value(l2: int, step_sq: float) -> float:
     return float(_lib.katoann_dist_value(int(l2), float(step_sq)))
 
 
-PHASES = ("rotate+quantize", "coarse product", "coarse select", "inversion", "seed bounds",
-          "ranking pass", "survivor merge", "refine")
+PHASES = ("rotate+quantize", "coarse product", "coarse select", "probe budget", "inversion",
+          "seed bounds", "ranking pass", "survivor merge", "refine")
 
 
 class PhaseTimer:
@@ -241,10 +258,16 @@ class Index:
             head_dims, int(on_device), prefix_dims, max_batch))
 
     def search(self, queries, k: int = 10, nprobe: int = 64, ranking: str = "prefix",
-               survivors: int = 32, selection: str = "threshold"):
+               survivors: int = 32, selection: str = "threshold", budget: "ProbeModel | None" = None,
+               threshold: float = 0.95, nprobe_per_query=None, return_nprobe: bool = False):
         """Search all queries together; returns (ids uint32 [nq, k], squared
         L2 distances float32 [nq, k]), nearest first. Queries are normalized
-        when the index was built with normalized=True."""
+        when the index was built with normalized=True.
+
+        Additions: a per-query nprobe, capped at `nprobe`: given
+        (nprobe_per_query, nq values) or chosen by a ProbeModel (`budget`, at
+        cumulative probability `threshold`). return_nprobe=True also returns
+        every query's nprobe (uint32 [nq])."""
         if ranking not in _RANKING:
             raise ValueError("ranking is 'prefix', 'high' or 'full'")
         if selection not in _SELECTION:
@@ -257,30 +280,63 @@ class Index:
         nq = q.shape[0]
         ids = np.zeros((nq, k), np.uint32)
         dists = np.zeros((nq, k), np.float32)
-        _check(_lib.katoann_index_search(self._h, _ptr(q), nq, k, nprobe, _RANKING[ranking],
-                                         survivors, _SELECTION[selection], _ptr(ids), _ptr(dists)))
-        return ids, dists
+        if budget is None and nprobe_per_query is None and not return_nprobe:
+            _check(_lib.katoann_index_search(self._h, _ptr(q), nq, k, nprobe, _RANKING[ranking],
+                                             survivors, _SELECTION[selection], _ptr(ids),
+                                             _ptr(dists)))
+            return ids, dists
+        npq = None
+        if nprobe_per_query is not None:
+            npq = np.ascontiguousarray(nprobe_per_query, dtype=np.uint32)
+            if npq.shape != (nq,):
+                raise ValueError("nprobe_per_query needs one value per query")
+        used = np.zeros(nq, np.uint32)
+        _check(_lib.katoann_index_search_budget(
+            self._h, _ptr(q), nq, k, nprobe, _RANKING[ranking], survivors, _SELECTION[selection],
+            budget._h if budget is not None else None, float(threshold),
+            _ptr(npq) if npq is not None else None, _ptr(used), _ptr(ids), _ptr(dists)))
+        return (ids, dists, used) if return_nprobe else (ids, dists)
 
     def search_into(self, q_ptr: int, nq: int, ids_ptr: int, dists_ptr: int, k: int = 10,
                     nprobe: int = 64, ranking: str = "prefix", survivors: int = 32,
-                    selection: str = "threshold") -> None:
+                    selection: str = "threshold", budget: "ProbeModel | None" = None,
+                    threshold: float = 0.95, nprobe_out_ptr: int = 0) -> None:
         """search() on raw host pointers (e.g. pinned buffers); no normalisation."""
-        _check(_lib.katoann_index_search(self._h, C.c_void_p(q_ptr), nq, k, nprobe,
-                                         _RANKING[ranking], survivors, _SELECTION[selection],
-                                         C.c_void_p(ids_ptr), C.c_void_p(dists_ptr)))
+        if budget is None and not nprobe_out_ptr:
+            _check(_lib.katoann_index_search(self._h, C.c_void_p(q_ptr), nq, k, nprobe,
+                                             _RANKING[ranking], survivors, _SELECTION[selection],
+                                             C.c_void_p(ids_ptr), C.c_void_p(dists_ptr)))
+            return
+        _check(_lib.katoann_index_search_budget(
+            self._h, C.c_void_p(q_ptr), nq, k, nprobe, _RANKING[ranking], survivors,
+            _SELECTION[selection], budget._h if budget is not None else None, float(threshold),
+            None, C.c_void_p(nprobe_out_ptr) if nprobe_out_ptr else None, C.c_void_p(ids_ptr),
+            C.c_void_p(dists_ptr)))
 
     def search_device(self, queries, ids, dists, k: int = 10, nprobe: int = 64,
                       ranking: str = "prefix", survivors: int = 32, selection: str = "threshold",
-                      stream: int | None = None, timer: "PhaseTimer | None" = None) -> None:
+                      stream: int | None = None, timer: "PhaseTimer | None" = None,
+                      budget: "ProbeModel | None" = None, threshold: float = 0.95,
+                      nprobe_per_query=None, nprobe_out=None) -> None:
         """CUDA tensors in (nq x dim float32) and out (nq x k uint32/int32,
         float32) on `stream` (a cudaStream_t as int, e.g. torch's
         ``Stream.cuda_stream``; 0 is the legacy default stream; None = the
-        index's own stream). Asynchronous."""
+        index's own stream). Asynchronous. nprobe_per_query / nprobe_out are
+        CUDA int32 tensors of nq values."""
         nq = int(queries.shape[0])
-        _check(_lib.katoann_index_search_device(
+        tm = C.c_void_p(timer.handle) if timer else None
+        if budget is None and nprobe_per_query is None and nprobe_out is None:
+            _check(_lib.katoann_index_search_device(
+                self._h, C.c_void_p(queries.data_ptr()), nq, k, nprobe, _RANKING[ranking],
+                survivors, _SELECTION[selection], C.c_void_p(ids.data_ptr()),
+                C.c_void_p(dists.data_ptr()), _stream_arg(stream), tm))
+            return
+        _check(_lib.katoann_index_search_device_budget(
             self._h, C.c_void_p(queries.data_ptr()), nq, k, nprobe, _RANKING[ranking], survivors,
-            _SELECTION[selection], C.c_void_p(ids.data_ptr()), C.c_void_p(dists.data_ptr()),
-            _stream_arg(stream), C.c_void_p(timer.handle) if timer else None))
+            _SELECTION[selection], budget._h if budget is not None else None, float(threshold),
+            C.c_void_p(nprobe_per_query.data_ptr()) if nprobe_per_query is not None else None,
+            C.c_void_p(nprobe_out.data_ptr()) if nprobe_out is not None else None,
+            C.c_void_p(ids.data_ptr()), C.c_void_p(dists.data_ptr()), _stream_arg(stream), tm))
 
     def search_stats(self) -> dict:
         """Diagnostics of the last search (see katoann_gpu_workspace_stats)."""
@@ -370,3 +426,139 @@ class Index:
             "clo": h(v.d_clo, L * dc, np.uint8).reshape(L, dc),
             "cnorm": h(v.d_cnorm, L * 8, np.int64),
         }
+
+
+class ProbeModel:
+    """Learned per-query probe budget (include/katoann/probe.h): a
+    64 -> 256 -> 256 -> C MLP with bf16 weights over 64 features of a query's
+    sorted coarse distances, choosing nprobe from a ladder. Use it as
+    ``index.search(q, nprobe=cap, budget=model, threshold=t)``."""
+
+    LADDER = (8, 12, 16, 24, 32, 48, 64, 96, 128, 192, 256, 384, 512)
+
+    def __init__(self, handle):
+        self._h = handle
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            _lib.katoann_probe_free(h)
+            self._h = None
+
+    @classmethod
+    def train(cls, index: Index, queries, ladder=LADDER, depth: int = 256, k: int = 10,
+              label_nprobe: int = 0, ranking: str = "prefix", survivors: int = 64,
+              epochs: int = 24, batch: int = 1024, lr: float = 1e-3, weight_decay: float = 1e-4,
+              seed: int = 0) -> "ProbeModel":
+        """Labels the training queries by searching `index` (the smallest
+        ladder value whose fixed-nprobe search recovers as much of the exact
+        top-k, from the exact search at label_nprobe lists, as any ladder
+        value does) and trains the model on the device."""
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        if q.ndim != 2 or q.shape[1] != index.dim:
+            raise ValueError("queries must be (n, dim) float32")
+        if index.normalized:
+            q = normalize_rows(q)
+        lad = np.ascontiguousarray(ladder, dtype=np.uint32)
+        h = C.c_void_p()
+        _check(_lib.katoann_probe_train(index._h, _ptr(q), q.shape[0], _ptr(lad), lad.size, depth,
+                                        k, label_nprobe, _RANKING[ranking], survivors, epochs,
+                                        batch, lr, weight_decay, seed, C.byref(h)))
+        return cls(h.value)
+
+    @classmethod
+    def fit(cls, z, labels, ladder=LADDER, depth: int = 256, epochs: int = 24, batch: int = 1024,
+            lr: float = 1e-3, weight_decay: float = 1e-4, seed: int = 0) -> "ProbeModel":
+        """Trains on raw features (n x 64, from features()) and class labels."""
+        z = np.ascontiguousarray(z, dtype=np.float32)
+        y = np.ascontiguousarray(labels, dtype=np.uint8)
+        if z.ndim != 2 or z.shape[1] != 64 or y.shape != (z.shape[0],):
+            raise ValueError("features must be (n, 64) with n labels")
+        lad = np.ascontiguousarray(ladder, dtype=np.uint32)
+        h = C.c_void_p()
+        _check(_lib.katoann_probe_fit(_ptr(z), _ptr(y), z.shape[0], _ptr(lad), lad.size, depth,
+                                      epochs, batch, lr, weight_decay, seed, C.byref(h)))
+        return cls(h.value)
+
+    @classmethod
+    def load(cls, path: str) -> "ProbeModel":
+        h = C.c_void_p()
+        _check(_lib.katoann_probe_load(path.encode(), C.byref(h)))
+        return cls(h.value)
+
+    def save(self, path: str) -> None:
+        _check(_lib.katoann_probe_save(self._h, path.encode()))
+
+    def _info(self):
+        info = np.zeros(2, np.uint32)
+        _check(_lib.katoann_probe_info(self._h, _ptr(info), None, None))
+        return info
+
+    @property
+    def classes(self) -> int:
+        return int(self._info()[0])
+
+    @property
+    def depth(self) -> int:
+        return int(self._info()[1])
+
+    @property
+    def ladder(self) -> np.ndarray:
+        lad = np.zeros(self.classes, np.uint32)
+        _check(_lib.katoann_probe_info(self._h, _ptr(np.zeros(2, np.uint32)), _ptr(lad), None))
+        return lad
+
+    @property
+    def feature_ranks(self) -> np.ndarray:
+        r = np.zeros(64, np.uint32)
+        _check(_lib.katoann_probe_info(self._h, _ptr(np.zeros(2, np.uint32)), None, _ptr(r)))
+        return r
+
+    @property
+    def labels(self) -> np.ndarray:
+        n = np.zeros(1, np.uint32)
+        _check(_lib.katoann_probe_record(self._h, None, _ptr(n), None, None))
+        out = np.zeros(int(n[0]), np.uint8)
+        _check(_lib.katoann_probe_record(self._h, _ptr(out), None, None, None))
+        return out
+
+    @property
+    def loss(self) -> np.ndarray:
+        e = np.zeros(1, np.uint32)
+        _check(_lib.katoann_probe_record(self._h, None, None, None, _ptr(e)))
+        out = np.zeros(int(e[0]), np.float32)
+        _check(_lib.katoann_probe_record(self._h, None, None, _ptr(out), None))
+        return out
+
+    def weights(self) -> dict:
+        """The weights as the device uses them (bf16 as uint16 bit patterns)."""
+        c = self.classes
+        w = dict(shift=np.zeros(64, np.float32), scale=np.zeros(64, np.float32),
+                 w1=np.zeros((64, 256), np.uint16), b1=np.zeros(256, np.float32),
+                 w2=np.zeros((256, 256), np.uint16), b2=np.zeros(256, np.float32),
+                 w3=np.zeros((256, c), np.uint16), b3=np.zeros(c, np.float32))
+        _check(_lib.katoann_probe_weights(self._h, *(_ptr(w[n]) for n in
+                                                     ("shift", "scale", "w1", "b1", "w2", "b2",
+                                                      "w3", "b3"))))
+        return w
+
+    @staticmethod
+    def features(index: Index, queries, depth: int = 256) -> np.ndarray:
+        """The 64 raw features of each query (n x 64) at `depth`."""
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        if index.normalized:
+            q = normalize_rows(q)
+        z = np.zeros((q.shape[0], 64), np.float32)
+        _check(_lib.katoann_probe_features(index._h, _ptr(q), q.shape[0], depth, _ptr(z)))
+        return z
+
+    def predict(self, z, threshold: float = 0.95, cap: int = 4096):
+        """Class probabilities (n x classes) and budgets (n, capped at cap) of
+        raw feature rows."""
+        z = np.ascontiguousarray(z, dtype=np.float32)
+        n = z.shape[0]
+        probs = np.zeros((n, self.classes), np.float32)
+        nprobe = np.zeros(n, np.uint32)
+        _check(_lib.katoann_probe_predict(self._h, _ptr(z), n, threshold, cap, _ptr(probs),
+                                          _ptr(nprobe)))
+        return probs, nprobe
