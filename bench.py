@@ -34,6 +34,8 @@ for _p in (os.path.join(ROOT, "katoann-public_gb300"), os.path.join(ROOT, "oracl
         sys.path.insert(0, _p)
 
 PUBLISHED_QPS_099 = 6294.0  # README.md:84 (BioASQ-1024-10M, 28-core Xeon, nlist 8192)
+LADDER = (8, 12, 16, 24, 32, 48, 64, 96, 128, 192, 256, 384, 512)  # learned nprobe choices
+THRESHOLDS = (0.3, 0.5, 0.7, 0.8, 0.9, 0.95, 0.98, 0.99, 0.995, 0.999)
 
 
 def parse_args():
@@ -58,14 +60,23 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-coding", choices=["gpu", "oracle"], default="gpu",
                     help="reference arm: who codes the index the oracle searches")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned probe budget")
+    ap.add_argument("--train-queries", type=int, default=200000,
+                    help="training queries of the probe-budget model")
+    ap.add_argument("--label-nprobe", type=int, default=1024,
+                    help="lists of the search that gives the training labels' exact top-k")
+    ap.add_argument("--label-survivors", type=int, default=256,
+                    help="survivors of that search (prefix ranking, exact refinement)")
     return ap.parse_args()
 
 
 # ----------------------------------------------------------------- data
-def make_data(torch, n, d, ncomp, seed, queries):
+def make_data(torch, n, d, ncomp, seed, queries, train_queries=0):
     """Unit vectors: mixture centres and per-point noise share an anisotropic
     spectrum (eigenvalue_i ~ i^-1.2) in a random orthogonal basis; component
-    weights follow Zipf(1.1), so the inverted lists come out skewed."""
+    weights follow Zipf(1.1), so the inverted lists come out skewed. Returns
+    the base, the evaluation queries and (another stream of the same
+    distribution) the probe-budget training queries."""
     dev = "cuda"
     g = torch.Generator(device=dev).manual_seed(seed)
     # random orthogonal basis (QR on the host: torch's linear-algebra library is
@@ -92,7 +103,9 @@ def make_data(torch, n, d, ncomp, seed, queries):
     base = sample(n, g)
     gq = torch.Generator(device=dev).manual_seed(seed + 7919)
     q = sample(queries, gq)
-    return base, q
+    gt_ = torch.Generator(device=dev).manual_seed(seed + 104729)
+    tq = sample(train_queries, gt_) if train_queries else None
+    return base, q, tq
 
 
 def assign(torch, x, c, chunk=65536):
@@ -274,7 +287,8 @@ def main():
     torch.backends.cuda.matmul.allow_tf32 = True
     t0 = time.time()
     n, d, L, B, k = args.n, args.dim, args.nlist, args.batch, args.k
-    base, queries = make_data(torch, n, d, args.ncomp, args.seed + rank, B)
+    ntrain = 0 if (args.no_learned or args.nprobe or args.impl == "reference") else args.train_queries
+    base, queries, train_q = make_data(torch, n, d, args.ncomp, args.seed + rank, B, ntrain)
     cen = kmeans(torch, base, L, args.kmeans_iters, min(args.train, n), args.seed)
     rot = pca_rotation(torch, base, min(100000, n), args.seed)
     a = assign(torch, base, cen)
@@ -305,40 +319,108 @@ def main():
     ids_d = torch.empty((B, k), dtype=torch.int32, device="cuda")
     dists_d = torch.empty((B, k), dtype=torch.float32, device="cuda")
 
-    def run(nprobe, S, reps=3):
-        idx.search_device(queries, ids_d, dists_d, k=k, nprobe=nprobe, survivors=S, stream=stream)
+    np_d = torch.empty(B, dtype=torch.int32, device="cuda")
+
+    def search(cfg, timer=None, nprobe_out=None):
+        """One device search of the batch: fixed {nprobe, survivors}, or learned
+        {model, threshold, nprobe (the cap), survivors}."""
+        idx.search_device(queries, ids_d, dists_d, k=k, nprobe=cfg["nprobe"],
+                          survivors=cfg["survivors"], stream=stream, timer=timer,
+                          budget=cfg.get("model"), threshold=cfg.get("threshold", 0.95),
+                          nprobe_out=nprobe_out)
+
+    def run(cfg, reps=3):
+        search(cfg, nprobe_out=np_d if cfg.get("model") else None)
         torch.cuda.synchronize()
         r = recall(ids_d.cpu().numpy().view(np.uint32), gt, k)
+        mean_np = float(np_d.float().mean()) if cfg.get("model") else float(cfg["nprobe"])
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         for _ in range(reps):
-            idx.search_device(queries, ids_d, dists_d, k=k, nprobe=nprobe, survivors=S, stream=stream)
+            search(cfg)
         e1.record()
         torch.cuda.synchronize()
-        return r, e0.elapsed_time(e1) / reps
+        return r, e0.elapsed_time(e1) / reps, mean_np
 
     sweep = []
     if args.nprobe:
         grid = [(args.nprobe, args.survivors)]
     else:
         grid = [(p, s) for s in (32, 64) for p in (16, 24, 32, 48, 64, 96, 128, 192, 256) if p <= L]
-        grid += [(p, 128) for p in (128, 192, 256, 384) if p <= L]  # towards recall 0.999
+        grid += [(p, 128) for p in (128, 192, 256, 384, 512) if p <= L]  # towards recall 0.999
     for p, s in grid:
-        r, ms = run(p, s)
-        sweep.append({"nprobe": p, "survivors": s, "recall": round(r, 5), "ms": round(ms, 3),
-                      "qps": round(B / ms * 1e3, 1)})
+        r, ms, _ = run(dict(nprobe=p, survivors=s))
+        sweep.append({"path": "fixed", "nprobe": p, "survivors": s, "recall": round(r, 5),
+                      "ms": round(ms, 3), "qps": round(B / ms * 1e3, 1)})
 
-    def best(target):
-        ok = [x for x in sweep if x["recall"] >= target]
+    # ---- the learned per-query probe budget: train on its own query stream,
+    # then sweep the threshold (every query's result is the fixed-nprobe
+    # result at its own nprobe; the model only chooses the nprobe)
+    models, learned_info = {}, None
+    if train_q is not None:
+        tq = train_q.cpu().numpy()
+        del train_q
+        torch.cuda.empty_cache()
+        cap = min(LADDER[-1], L)
+        ladder = tuple(v for v in LADDER if v <= L)
+        lab_p = min(L, args.label_nprobe)
+        learned_info = {"train_queries": len(tq), "ladder": list(ladder), "depth": min(256, L),
+                        "label_search": {"nprobe": lab_p, "ranking": "prefix",
+                                         "survivors": args.label_survivors},
+                        "models": {}}
+        for s_l in (64, 128):
+            t_l = time.time()
+            m = katoann.ProbeModel.train(idx, tq, ladder=ladder, depth=min(256, L), k=k,
+                                         label_nprobe=lab_p, label_ranking="prefix",
+                                         label_survivors=args.label_survivors, ranking="prefix",
+                                         survivors=s_l, epochs=24, batch=1024, seed=args.seed)
+            models[s_l] = m
+            hist = np.bincount(m.labels, minlength=len(ladder))
+            learned_info["models"][s_l] = {"train_s": round(time.time() - t_l, 1),
+                                           "loss_first_last": [round(float(m.loss[0]), 4),
+                                                               round(float(m.loss[-1]), 4)],
+                                           "label_histogram": hist.tolist()}
+        # how close the labels' top-k is to the exact-distance search's (a sample)
+        t_c = time.time()
+        smp = tq[:256]
+        ex, _ = idx.search(smp, k=k, nprobe=lab_p, ranking="full", survivors=k)
+        lb, _ = idx.search(smp, k=k, nprobe=lab_p, ranking="prefix", survivors=args.label_survivors)
+        learned_info["label_check"] = {
+            "queries": len(smp), "same_top_k_as_exact_search": float(np.mean(
+                [set(a) == set(b) for a, b in zip(ex, lb)])), "seconds": round(time.time() - t_c, 1)}
+        del tq
+        for s_l, m in models.items():
+            for thr in THRESHOLDS:
+                r, ms, mnp = run(dict(nprobe=cap, survivors=s_l, model=m, threshold=thr))
+                sweep.append({"path": "learned", "survivors": s_l, "threshold": thr, "cap": cap,
+                              "mean_nprobe": round(mnp, 2), "recall": round(r, 5),
+                              "ms": round(ms, 3), "qps": round(B / ms * 1e3, 1)})
+
+    def best(target, path=None):
+        ok = [x for x in sweep if x["recall"] >= target and path in (None, x["path"])]
         return min(ok, key=lambda x: x["ms"]) if ok else None
+
+    def summary(x):
+        if x is None:
+            return None
+        keys = ("nprobe", "survivors") if x["path"] == "fixed" else \
+            ("survivors", "threshold", "cap", "mean_nprobe")
+        return {"qps": x["qps"], "recall": x["recall"], **{kk: x[kk] for kk in keys}}
 
     b99, b999 = best(0.99), best(0.999)
     chosen = b99 or max(sweep, key=lambda x: x["recall"])
-    p, S = chosen["nprobe"], chosen["survivors"]
+    if chosen["path"] == "learned":
+        cfg = dict(nprobe=chosen["cap"], survivors=chosen["survivors"],
+                   model=models[chosen["survivors"]], threshold=chosen["threshold"])
+    else:
+        cfg = dict(nprobe=chosen["nprobe"], survivors=chosen["survivors"])
+    S = cfg["survivors"]
+    fixed99 = best(0.99, "fixed") or max((x for x in sweep if x["path"] == "fixed"),
+                                         key=lambda x: x["recall"])
 
     # ---- timed region: K steps on device-resident queries
     for _ in range(max(3, args.warmup)):
-        idx.search_device(queries, ids_d, dists_d, k=k, nprobe=p, survivors=S, stream=stream)
+        search(cfg)
     timer = katoann.PhaseTimer(args.steps + 4)
     timer.read()
     torch.cuda.synchronize()
@@ -349,8 +431,7 @@ def main():
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         for _ in range(args.steps):
-            idx.search_device(queries, ids_d, dists_d, k=k, nprobe=p, survivors=S, stream=stream,
-                              timer=timer)
+            search(cfg, timer=timer)
         e1.record()
         torch.cuda.synchronize()
         elapsed_ms = e0.elapsed_time(e1)
@@ -363,24 +444,30 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = world * B * args.steps / (ms / 1e3)
-    idx.search_device(queries, ids_d, dists_d, k=k, nprobe=p, survivors=S, stream=stream)
+    search(cfg, nprobe_out=np_d)
     torch.cuda.synchronize()
     search_stats = idx.search_stats()
     launches_per_search = katoann.last_launches()
+    per_query_np = np_d.cpu().numpy().astype(np.int64)
 
     # ---- end to end through the public host API (pinned host buffers)
     qh = torch.empty((B, d), dtype=torch.float32).pin_memory()
     qh.copy_(queries.cpu())
     ih = torch.empty((B, k), dtype=torch.int32).pin_memory()
     dh = torch.empty((B, k), dtype=torch.float32).pin_memory()
+
+    def host_search():
+        idx.search_into(qh.data_ptr(), B, ih.data_ptr(), dh.data_ptr(), k=k, nprobe=cfg["nprobe"],
+                        survivors=S, budget=cfg.get("model"), threshold=cfg.get("threshold", 0.95))
+
     for _ in range(3):
-        idx.search_into(qh.data_ptr(), B, ih.data_ptr(), dh.data_ptr(), k=k, nprobe=p, survivors=S)
+        host_search()
     e2e_steps = max(10, min(args.steps, 100))
     if dist:
         dist.barrier()
     t2 = time.perf_counter()
     for _ in range(e2e_steps):
-        idx.search_into(qh.data_ptr(), B, ih.data_ptr(), dh.data_ptr(), k=k, nprobe=p, survivors=S)
+        host_search()
     e2e_s = time.perf_counter() - t2
     e2e_qps = world * B * e2e_steps / e2e_s
     e2e_recall = recall(ih.numpy().view(np.uint32), gt, k)
@@ -396,8 +483,11 @@ def main():
     cq = queries @ (rot.T)
     cc = cen @ (rot.T)
     dd = torch.cdist(cq, cc)
-    top = torch.topk(dd, p, dim=1, largest=False).indices.unique().cpu().numpy()
-    probed[top] = True
+    pmax = int(per_query_np.max())
+    top = torch.topk(dd, pmax, dim=1, largest=False).indices.cpu().numpy()
+    keep = np.arange(pmax)[None, :] < per_query_np[:, None]  # each query's own nprobe
+    probed[np.unique(top[keep])] = True
+    p = int(round(float(per_query_np.mean())))
     probed_rows = float(list_sizes[probed].sum())
     skew = {"max_list": int(sizes.max()), "mean_list": round(float(sizes.mean()), 1),
             "p99_list": int(np.percentile(sizes, 99)), "empty_lists": int((sizes == 0).sum()),
@@ -421,11 +511,11 @@ def main():
     cpu = None
     parity = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu, parity = cpu_baseline(args, torch, idx, queries, p, S, k)
+        cpu, parity = cpu_baseline(args, torch, idx, queries, fixed99, cfg, k)
 
     clk = clocks.summary()
     out = {
-        "metric": "QPS at recall@10 >= 0.99 (fixed nprobe), 10M x 1024 IVF, batch 4096, 1 GB300",
+        "metric": "QPS at recall@10 >= 0.99, 10M x 1024 IVF, learned vs fixed nprobe, batch 4096, 1 GB300",
         "value": round(value, 1), "unit": "queries/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
         "scaling": "weak",
@@ -436,12 +526,20 @@ def main():
         "data": "synthetic: seeded power-law spectrum (i^-1.2) + 10,000-component Zipf(1.1) mixture, "
                 "unit norm; stands in for BioASQ-1024-10M",
         "config": {"workload": f"{n // 1000000}M x {d} IVF, nlist {L}, batch {B}, k {k}",
-                   "nprobe": p, "survivors": S, "prefix_dims": args.head, "ranking": "prefix",
+                   "nprobe_path": chosen["path"],
+                   **{kk: v for kk, v in summary(chosen).items() if kk not in ("qps", "recall")},
+                   "prefix_dims": args.head,
+                   "ranking": "prefix",
                    "l2_policy": "inputs larger than L2 (index codes 20.5 GB per pass)"},
         "recall": chosen["recall"],
         "qps_at_recall_0.999": (round(b999["qps"], 1) if b999 else None),
-        "setting_at_recall_0.999": ({"nprobe": b999["nprobe"], "survivors": b999["survivors"]}
-                                    if b999 else None),
+        "setting_at_recall_0.999": ({"path": b999["path"], **summary(b999)} if b999 else None),
+        "learned_vs_fixed": {
+            "recall_0.99": {"fixed": summary(best(0.99, "fixed")),
+                            "learned": summary(best(0.99, "learned"))},
+            "recall_0.999": {"fixed": summary(best(0.999, "fixed")),
+                             "learned": summary(best(0.999, "learned"))}},
+        "probe_model": learned_info,
         "sweep": sweep,
         "phases_ms_per_step": {k2: round(v, 4) for k2, v in per_launch.items()},
         "roofline": roofline,
@@ -475,7 +573,11 @@ def _time_oracle(o, qs, k, p, S, budget_s):
     return m / dt, m, dt, ids, dists
 
 
-def cpu_baseline(args, torch, idx, queries, p, S, k):
+def cpu_baseline(args, torch, idx, queries, fixed, cfg, k):
+    """The oracle (the reference's algorithm, all host cores) on a bounded
+    sample of the batch at the fixed setting that reaches the recall target,
+    and a bit-exactness check of the timed path on the same sample: fixed, or
+    learned (then every query against the oracle at its own nprobe)."""
     import oracle
     codes = idx.export_codes()
     o = oracle.OracleIndex(None, codes=codes)
@@ -483,14 +585,25 @@ def cpu_baseline(args, torch, idx, queries, p, S, k):
     cores = os.cpu_count() or 1
     oracle.set_threads(cores)
     q = queries.cpu().numpy()
+    p, S = fixed["nprobe"], fixed["survivors"]
     qps, m, dt, oids, odists = _time_oracle(o, q, k, p, S, args.cpu_seconds)
-    gids, gd = idx.search(q[:m], k=k, nprobe=p, survivors=S)
-    exact = bool(np.array_equal(gids, oids) and np.array_equal(gd, odists))
     cpu = {"value": round(qps, 1), "unit": "queries/s", "cores": cores, "kind": "port",
-           "sample": f"{m} of the {len(q)} batch queries, same index and settings, {dt:.1f} s",
-           "isa": platform.machine()}
-    parity = {"queries": m, "bit_exact_vs_oracle": exact}
-    return cpu, parity
+           "sample": f"{m} of the {len(q)} batch queries, same index, fixed nprobe {p}, "
+                     f"survivors {S}, {dt:.1f} s", "isa": platform.machine()}
+    if cfg.get("model") is None and cfg["nprobe"] == p and cfg["survivors"] == S:
+        gids, gd = idx.search(q[:m], k=k, nprobe=p, survivors=S)
+        exact = bool(np.array_equal(gids, oids) and np.array_equal(gd, odists))
+        return cpu, {"queries": m, "path": "fixed", "bit_exact_vs_oracle": exact}
+    gids, gd, used = idx.search(q[:m], k=k, nprobe=cfg["nprobe"], survivors=cfg["survivors"],
+                                budget=cfg.get("model"), threshold=cfg.get("threshold", 0.95),
+                                return_nprobe=True)
+    exact = True
+    for v in np.unique(used):
+        sel = np.nonzero(used == v)[0]
+        rid, rd = o.search(q[:m][sel], k=k, nprobe=int(v), survivors=cfg["survivors"])
+        exact &= bool(np.array_equal(gids[sel], rid) and np.array_equal(gd[sel], rd))
+    return cpu, {"queries": m, "path": "learned (each query at its own nprobe)",
+                 "bit_exact_vs_oracle": exact}
 
 
 def run_reference(args, torch, vectors, order, cen, rot, sizes, queries, gt, setup_s):

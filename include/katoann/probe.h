@@ -15,8 +15,11 @@
 // a query's label is the smallest ladder value whose fixed-nprobe search
 // (the ranking and survivors the budget is for) recovers as much of the
 // query's exact top-k as any ladder value does. The exact top-k comes from
-// the exact-distance search (Ranking::kFull) at label_nprobe lists. Training
-// runs on the device (softmax cross-entropy, Adam).
+// the exact-distance search (Ranking::kFull) at label_nprobe lists, or, to
+// label many queries faster, from a search with label_ranking and
+// label_survivors (its refinement gives exact distances of the survivors, so
+// it equals the exact top-k whenever those rank within the survivors).
+// Training runs on the device (softmax cross-entropy, Adam).
 #pragma once
 
 #include <cstdint>
@@ -34,6 +37,8 @@ struct ProbeTrainOptions {
   uint32_t depth = 256;          // coarse ranks the features read (<= nlist, <= 4096)
   uint32_t k = 10;               // the exact top-k the labels recover
   uint32_t label_nprobe = 0;     // lists of the exact search; 0: min(nlist, 2 x the top of the ladder)
+  Ranking label_ranking = Ranking::kFull;  // the search that gives the exact top-k
+  uint32_t label_survivors = 0;  // its survivors (0: k)
   Ranking ranking = Ranking::kPrefix;  // the search the budget is for
   uint32_t survivors = 64;
   uint32_t epochs = 24;

@@ -86,11 +86,12 @@ int katoann_index_search_device_budget(void *index, const float *d_queries, uint
 /* ------------------------------------------------ learned probe budget
  * katoann::ProbeModel (include/katoann/probe.h). train: labels nq queries by
  * searching the index and trains on the device; options as in
- * ProbeTrainOptions (ranking 0 full, 1 high, 2 prefix). */
+ * ProbeTrainOptions (rankings 0 full, 1 high, 2 prefix). */
 int katoann_probe_train(void *index, const float *queries, uint32_t nq, const uint32_t *ladder,
                         uint32_t nladder, uint32_t depth, uint32_t k, uint32_t label_nprobe,
-                        int ranking, uint32_t survivors, uint32_t epochs, uint32_t batch,
-                        float lr, float weight_decay, uint64_t seed, void **model);
+                        int label_ranking, uint32_t label_survivors, int ranking,
+                        uint32_t survivors, uint32_t epochs, uint32_t batch, float lr,
+                        float weight_decay, uint64_t seed, void **model);
 /* ProbeModel::fit on given raw features (n x 64) and class labels. */
 int katoann_probe_fit(const float *z, const uint8_t *labels, uint32_t n, const uint32_t *ladder,
                       uint32_t nladder, uint32_t depth, uint32_t epochs, uint32_t batch,

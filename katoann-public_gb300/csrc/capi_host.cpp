@@ -233,13 +233,16 @@ int katoann_index_search_device_budget(void *index, const float *d_queries, uint
 
 int katoann_probe_train(void *index, const float *queries, uint32_t nq, const uint32_t *ladder,
                         uint32_t nladder, uint32_t depth, uint32_t k, uint32_t label_nprobe,
-                        int ranking, uint32_t survivors, uint32_t epochs, uint32_t batch,
-                        float lr, float weight_decay, uint64_t seed, void **model) {
+                        int label_ranking, uint32_t label_survivors, int ranking,
+                        uint32_t survivors, uint32_t epochs, uint32_t batch, float lr,
+                        float weight_decay, uint64_t seed, void **model) {
   return guarded([&] {
     katoann::ProbeTrainOptions o =
         train_options(ladder, nladder, depth, epochs, batch, lr, weight_decay, seed);
     if (k) o.k = k;
     o.label_nprobe = label_nprobe;
+    o.label_ranking = ranking_of(label_ranking);
+    o.label_survivors = label_survivors;
     o.ranking = ranking_of(ranking);
     if (survivors) o.survivors = survivors;
     *model = new katoann::ProbeModel(katoann::ProbeModel::train(*I(index), queries, nq, o));

@@ -285,8 +285,8 @@ ProbeModel ProbeModel::train(const Index &index, const float *queries, uint32_t 
   SearchParams sp;
   sp.k = k;
   sp.nprobe = ref_p;
-  sp.ranking = Ranking::kFull;
-  sp.survivors = k;
+  sp.ranking = opt.label_ranking;
+  sp.survivors = std::max(opt.label_survivors, k);
   index.search(queries, nq, sp, ref.data(), dd.data());
   // per query: how much of it each ladder value's search recovers
   const uint32_t C = static_cast<uint32_t>(opt.ladder.size());

@@ -68,8 +68,8 @@ def _load():
     lib.katoann_index_search_budget.argtypes = [P, P, U32, U32, U32, I32, U32, I32, P, F, P, P, P, P]
     lib.katoann_index_search_device_budget.argtypes = [P, P, U32, U32, U32, I32, U32, I32, P, F, P,
                                                        P, P, P, P, P]
-    lib.katoann_probe_train.argtypes = [P, P, U32, P, U32, U32, U32, U32, I32, U32, U32, U32, F, F,
-                                        U64, C.POINTER(P)]
+    lib.katoann_probe_train.argtypes = [P, P, U32, P, U32, U32, U32, U32, I32, U32, I32, U32, U32,
+                                        U32, F, F, U64, C.POINTER(P)]
     lib.katoann_probe_fit.argtypes = [P, P, U32, P, U32, U32, U32, U32, F, F, U64, C.POINTER(P)]
     lib.katoann_probe_load.argtypes = [C.c_char_p, C.POINTER(P)]
     lib.katoann_probe_save.argtypes = [P, C.c_char_p]
@@ -447,13 +447,14 @@ class ProbeModel:
 
     @classmethod
     def train(cls, index: Index, queries, ladder=LADDER, depth: int = 256, k: int = 10,
-              label_nprobe: int = 0, ranking: str = "prefix", survivors: int = 64,
-              epochs: int = 24, batch: int = 1024, lr: float = 1e-3, weight_decay: float = 1e-4,
-              seed: int = 0) -> "ProbeModel":
+              label_nprobe: int = 0, label_ranking: str = "full", label_survivors: int = 0,
+              ranking: str = "prefix", survivors: int = 64, epochs: int = 24, batch: int = 1024,
+              lr: float = 1e-3, weight_decay: float = 1e-4, seed: int = 0) -> "ProbeModel":
         """Labels the training queries by searching `index` (the smallest
         ladder value whose fixed-nprobe search recovers as much of the exact
-        top-k, from the exact search at label_nprobe lists, as any ladder
-        value does) and trains the model on the device."""
+        top-k as any ladder value does; the exact top-k comes from the
+        label_ranking search at label_nprobe lists, by default the exact-
+        distance one) and trains the model on the device."""
         q = np.ascontiguousarray(queries, dtype=np.float32)
         if q.ndim != 2 or q.shape[1] != index.dim:
             raise ValueError("queries must be (n, dim) float32")
@@ -462,8 +463,9 @@ class ProbeModel:
         lad = np.ascontiguousarray(ladder, dtype=np.uint32)
         h = C.c_void_p()
         _check(_lib.katoann_probe_train(index._h, _ptr(q), q.shape[0], _ptr(lad), lad.size, depth,
-                                        k, label_nprobe, _RANKING[ranking], survivors, epochs,
-                                        batch, lr, weight_decay, seed, C.byref(h)))
+                                        k, label_nprobe, _RANKING[label_ranking], label_survivors,
+                                        _RANKING[ranking], survivors, epochs, batch, lr,
+                                        weight_decay, seed, C.byref(h)))
         return cls(h.value)
 
     @classmethod
