@@ -450,6 +450,25 @@ def main():
     launches_per_search = katoann.last_launches()
     per_query_np = np_d.cpu().numpy().astype(np.int64)
 
+    # ---- the same search captured as a CUDA graph and replayed (one launch
+    # per step instead of one per kernel)
+    def search_graph():
+        idx.search_device(queries, ids_d, dists_d, k=k, nprobe=cfg["nprobe"], survivors=S,
+                          stream=stream, budget=cfg.get("model"),
+                          threshold=cfg.get("threshold", 0.95), graph=True)
+
+    for _ in range(max(3, args.warmup)):
+        search_graph()
+    torch.cuda.synchronize()
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g0.record()
+    for _ in range(args.steps):
+        search_graph()
+    g1.record()
+    torch.cuda.synchronize()
+    graph_ms = g0.elapsed_time(g1) / args.steps
+    graph_recall = recall(ids_d.cpu().numpy().view(np.uint32), gt, k)
+
     # ---- end to end through the public host API (pinned host buffers)
     qh = torch.empty((B, d), dtype=torch.float32).pin_memory()
     qh.copy_(queries.cpu())
@@ -543,6 +562,10 @@ def main():
         "sweep": sweep,
         "phases_ms_per_step": {k2: round(v, 4) for k2, v in per_launch.items()},
         "roofline": roofline,
+        "graph_replay": {"ms_per_step": round(graph_ms, 4),
+                         "qps": round(world * B / graph_ms * 1e3, 1),
+                         "recall": round(graph_recall, 5),
+                         "api": "katoann.Index.search_device(graph=True)"},
         "e2e": {"value": round(e2e_qps, 1), "unit": "queries/s", "recall": round(e2e_recall, 5),
                 "h2d_bytes_per_step": B * d * 4, "d2h_bytes_per_step": B * k * 8,
                 "api": "katoann.Index.search_into (pinned host buffers)"},

@@ -83,6 +83,10 @@ struct SearchParams {
   float budget_threshold = 0.95f;
   const uint32_t *nprobe_per_query = nullptr;
   uint32_t *nprobe_used = nullptr;
+  // search_device only: run the call as a CUDA graph, captured the first time
+  // these pointers and parameters are seen (the index keeps the last 16) and
+  // replayed in one launch after that.
+  bool graph = false;
 };
 
 // An index given as arrays (lists concatenated in list order). Pointers are

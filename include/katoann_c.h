@@ -75,13 +75,14 @@ int katoann_index_search_budget(void *index, const float *queries, uint32_t nq, 
                                 uint32_t *nprobe_out, uint32_t *ids, float *dists);
 
 /* katoann_index_search_device with the per-query nprobe of
- * katoann_index_search_budget (d_nprobe_in / d_nprobe_out: device memory). */
+ * katoann_index_search_budget (d_nprobe_in / d_nprobe_out: device memory);
+ * graph != 0 replays a captured CUDA graph of the call (SearchParams::graph). */
 int katoann_index_search_device_budget(void *index, const float *d_queries, uint32_t nq,
                                        uint32_t k, uint32_t nprobe, int ranking,
                                        uint32_t survivors, int selection, const void *model,
                                        float threshold, const uint32_t *d_nprobe_in,
                                        uint32_t *d_nprobe_out, uint32_t *d_ids, float *d_dists,
-                                       void *stream, void *timer);
+                                       void *stream, void *timer, int graph);
 
 /* ------------------------------------------------ learned probe budget
  * katoann::ProbeModel (include/katoann/probe.h). train: labels nq queries by

@@ -264,7 +264,7 @@ typedef struct {
   const uint32_t *d_rank;   /* 64 */
   const float *d_shift;     /* 64 */
   const float *d_scale;     /* 64 */
-  const uint16_t *d_w1;     /* 64 x 256 bf16 */
+  const uint16_t *d_w1;     /* 64 x 256 bf16, 16-byte aligned */
   const float *d_b1;        /* 256 */
   const uint16_t *d_w2;     /* 256 x 256 bf16 */
   const float *d_b2;        /* 256 */
@@ -287,6 +287,25 @@ int katoann_gpu_search_budget(const katoann_gpu_index *index, const float *d_que
                               const uint32_t *d_nprobe_in, const katoann_gpu_probe_model *model,
                               void *d_ws, size_t ws_bytes, uint32_t *d_ids, float *d_dists,
                               uint32_t *d_nprobe_out, katoann_stream_t stream, void *timer);
+
+/* A search captured as a CUDA graph (no counterpart in the reference): the
+ * whole pipeline of one katoann_gpu_search_budget call - every kernel, memset
+ * and copy of every batch pass - recorded on `stream` (a created stream, not
+ * the legacy default one) and instantiated. Nothing runs at capture.
+ * katoann_gpu_graph_launch replays it on any stream: the same pointers and
+ * sizes, with whatever the buffers hold at replay, in one launch instead of
+ * some thirty. The workspace, index, model and buffers must stay allocated
+ * while the graph lives. */
+int katoann_gpu_search_capture(const katoann_gpu_index *index, const float *d_queries,
+                               uint32_t nq, uint32_t k, uint32_t nprobe, int ranking,
+                               uint32_t survivors, uint32_t max_batch,
+                               const uint32_t *d_nprobe_in, const katoann_gpu_probe_model *model,
+                               void *d_ws, size_t ws_bytes, uint32_t *d_ids, float *d_dists,
+                               uint32_t *d_nprobe_out, katoann_stream_t stream, void **graph);
+int katoann_gpu_graph_launch(void *graph, katoann_stream_t stream);
+/* Kernel launches one replay of the graph makes. */
+uint32_t katoann_gpu_graph_launches(const void *graph);
+void katoann_gpu_graph_destroy(void *graph);
 
 /* The 64 raw features z (before standardization) of nq queries into d_z
  * (nq x 64, device): rotation, quantization, coarse product and selection of

@@ -43,6 +43,13 @@ int search(const katoann_gpu_index *ix, const float *queries, uint32_t nq, uint3
 int probe_features_search(const katoann_gpu_index *ix, const float *queries, uint32_t nq,
                           const uint32_t *rank, uint32_t depth, uint32_t max_batch, void *ws,
                           size_t ws_bytes, float *z, cudaStream_t st);
+int search_capture(const katoann_gpu_index *ix, const float *queries, uint32_t nq, uint32_t k,
+                   uint32_t p, int ranking, uint32_t survivors, uint32_t max_batch, void *ws,
+                   size_t ws_bytes, uint32_t *out_ids, float *out_dists, const Budget &budget,
+                   cudaStream_t st, void **out);
+int graph_launch(void *h, cudaStream_t st);
+uint32_t graph_launches(const void *h);
+void graph_destroy(void *h);
 void *timer_create(uint32_t max_passes);
 uint32_t last_launches();
 int centre_planes(const uint8_t *hi, const uint8_t *lo, const int64_t *norm, uint32_t rows,
@@ -193,6 +200,35 @@ int katoann_gpu_search_budget(const katoann_gpu_index *ix, const float *d_querie
   return kato::search(ix, d_queries, nq, k, nprobe, ranking, survivors, max_batch, d_ws, ws_bytes,
                       d_ids, d_dists, b, as_stream(stream), timer);
 }
+
+int katoann_gpu_search_capture(const katoann_gpu_index *ix, const float *d_queries, uint32_t nq,
+                               uint32_t k, uint32_t nprobe, int ranking, uint32_t survivors,
+                               uint32_t max_batch, const uint32_t *d_nprobe_in,
+                               const katoann_gpu_probe_model *model, void *d_ws, size_t ws_bytes,
+                               uint32_t *d_ids, float *d_dists, uint32_t *d_nprobe_out,
+                               katoann_stream_t stream, void **graph) {
+  if (!graph) return kato::invalid("null graph handle");
+  *graph = nullptr;
+  if (!ix) return kato::invalid("null index");
+  if (ix->nlist == 0) {
+    kato::set_error("search before load");
+    return KATO_ELOGIC;
+  }
+  kato::Budget b;
+  b.nprobe_in = d_nprobe_in;
+  b.model = d_nprobe_in ? nullptr : model;
+  b.nprobe_out = d_nprobe_out;
+  return kato::search_capture(ix, d_queries, nq, k, nprobe, ranking, survivors, max_batch, d_ws,
+                              ws_bytes, d_ids, d_dists, b, as_stream(stream), graph);
+}
+
+int katoann_gpu_graph_launch(void *graph, katoann_stream_t stream) {
+  return kato::graph_launch(graph, as_stream(stream));
+}
+
+uint32_t katoann_gpu_graph_launches(const void *graph) { return kato::graph_launches(graph); }
+
+void katoann_gpu_graph_destroy(void *graph) { kato::graph_destroy(graph); }
 
 int katoann_gpu_probe_features(const katoann_gpu_index *ix, const float *d_queries, uint32_t nq,
                                const uint32_t *d_rank, uint32_t depth, uint32_t max_batch,

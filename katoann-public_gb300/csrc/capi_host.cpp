@@ -220,13 +220,14 @@ int katoann_index_search_device_budget(void *index, const float *d_queries, uint
                                        uint32_t survivors, int selection, const void *model,
                                        float threshold, const uint32_t *d_nprobe_in,
                                        uint32_t *d_nprobe_out, uint32_t *d_ids, float *d_dists,
-                                       void *stream, void *timer) {
+                                       void *stream, void *timer, int graph) {
   return guarded([&] {
     katoann::SearchParams p = params(k, nprobe, ranking, survivors, selection);
     p.budget = M(model);
     p.budget_threshold = threshold;
     p.nprobe_per_query = d_nprobe_in;
     p.nprobe_used = d_nprobe_out;
+    p.graph = graph != 0;
     I(index)->search_device(d_queries, nq, p, d_ids, d_dists, stream, timer);
   });
 }

@@ -86,9 +86,20 @@ struct Index::State {
   cudaEvent_t done = nullptr;
   mutable std::mutex mu;
   mutable DevBuf ws, dq, dids, ddists, dnp_in, dnp_out;
+  // captured searches of search_device (SearchParams::graph), most recent last
+  struct Graph {
+    std::vector<uint64_t> key;
+    void *handle;
+  };
+  mutable std::vector<Graph> graphs;
+  void drop_graphs() const {
+    for (auto &g : graphs) katoann_gpu_graph_destroy(g.handle);
+    graphs.clear();
+  }
   mutable void *last_stream = nullptr;
 
   ~State() {
+    drop_graphs();
     if (done) cudaEventDestroy(done);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -639,11 +650,43 @@ void Index::search_device(const float *d_queries, uint32_t nq, const SearchParam
   if (need == 0) gpu_check(KATO_EINVAL);
   if (need > s.ws.n) {
     cuda_check(cudaDeviceSynchronize(), "workspace resize");
+    s.drop_graphs();  // they hold the old workspace
     s.ws.ensure(need);
   }
   if (s.last_stream && s.last_stream != st)
     cuda_check(cudaStreamWaitEvent(st, s.done, 0), "cudaStreamWaitEvent");
-  if (bp.active || p.nprobe_used)
+  if (p.graph) {
+    if (timer) throw std::invalid_argument("a graph search records no phase events");
+    // the call's identity: every pointer and size it captures
+    const std::vector<uint64_t> key = {
+        reinterpret_cast<uint64_t>(d_queries), nq, reinterpret_cast<uint64_t>(d_ids),
+        reinterpret_cast<uint64_t>(d_dists), p.k, p.nprobe, static_cast<uint64_t>(rk),
+        p.survivors, reinterpret_cast<uint64_t>(p.nprobe_per_query),
+        reinterpret_cast<uint64_t>(p.nprobe_used),
+        bp.use_model ? reinterpret_cast<uint64_t>(bp.model.d_w1) : 0,
+        bp.use_model ? (uint64_t(bp.model.nclass) << 32 | bp.model.depth) : 0,
+        bp.use_model ? static_cast<uint64_t>(std::llround(double(p.budget_threshold) * 1e9)) : 0,
+        reinterpret_cast<uint64_t>(st), reinterpret_cast<uint64_t>(s.ws.p)};
+    void *h = nullptr;
+    for (size_t i = 0; i < s.graphs.size(); ++i)
+      if (s.graphs[i].key == key) {
+        h = s.graphs[i].handle;
+        std::rotate(s.graphs.begin() + i, s.graphs.begin() + i + 1, s.graphs.end());
+        break;
+      }
+    if (!h) {
+      gpu_check(katoann_gpu_search_capture(
+          &s.view, d_queries, nq, p.k, p.nprobe, rk, p.survivors, s.max_batch,
+          p.nprobe_per_query, bp.use_model ? &bp.model : nullptr, s.ws.p, s.ws.n, d_ids, d_dists,
+          p.nprobe_used, reinterpret_cast<katoann_stream_t>(st), &h));
+      if (s.graphs.size() >= 16) {
+        katoann_gpu_graph_destroy(s.graphs.front().handle);
+        s.graphs.erase(s.graphs.begin());
+      }
+      s.graphs.push_back({key, h});
+    }
+    gpu_check(katoann_gpu_graph_launch(h, reinterpret_cast<katoann_stream_t>(st)));
+  } else if (bp.active || p.nprobe_used)
     gpu_check(katoann_gpu_search_budget(&s.view, d_queries, nq, p.k, p.nprobe, rk, p.survivors,
                                         s.max_batch, p.nprobe_per_query,
                                         bp.use_model ? &bp.model : nullptr, s.ws.p, s.ws.n, d_ids,

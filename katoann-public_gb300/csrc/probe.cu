@@ -82,7 +82,8 @@ struct MlpArgs {
 };
 
 // One dense ReLU layer over the CTA's 32 queries: thread j owns output unit j.
-// in: [K][kAS] (unit-major, query fastest), out: [kH][kAS].
+// in: [K][kAS] (unit-major, query fastest), out: [kH][kAS]; w is K x kH bf16
+// (global memory through L2, or shared memory).
 template <uint32_t K>
 __device__ __forceinline__ void dense_relu(const float *in, const uint16_t *__restrict__ w,
                                            const float *__restrict__ b, float *out) {
@@ -91,7 +92,7 @@ __device__ __forceinline__ void dense_relu(const float *in, const uint16_t *__re
   const float bj = b[j];
 #pragma unroll
   for (uint32_t i = 0; i < kQB; ++i) acc[i] = bj;
-#pragma unroll 4
+#pragma unroll 8
   for (uint32_t k = 0; k < K; ++k) {
     const float wk = bf16_value(w[k * kH + j]);
     const float4 *x = reinterpret_cast<const float4 *>(in + k * kAS);
@@ -111,7 +112,9 @@ __device__ __forceinline__ void dense_relu(const float *in, const uint16_t *__re
                        fmaxf(acc[4 * v + 2], 0.f), fmaxf(acc[4 * v + 3], 0.f));
 }
 
-constexpr size_t kMlpSmem = (static_cast<size_t>(kF) + 2 * kH) * kAS * 4 + kQB * (kCMax + 1) * 4;
+// activations (x0, h1, h2), logits, then w1 and w3 staged as bf16
+constexpr size_t kMlpAct = (static_cast<size_t>(kF) + 2 * kH) * kAS * 4 + kQB * (kCMax + 1) * 4;
+constexpr size_t kMlpSmem = kMlpAct + (static_cast<size_t>(kF) * kH + kH * kCMax) * 2;
 
 __global__ void __launch_bounds__(kH) probe_mlp_kernel(const float *__restrict__ z, uint32_t B,
                                                         MlpArgs m, uint32_t cap,
@@ -122,7 +125,17 @@ __global__ void __launch_bounds__(kH) probe_mlp_kernel(const float *__restrict__
   float *h1 = x0 + kF * kAS;      // [kH][kAS]
   float *h2 = h1 + kH * kAS;      // [kH][kAS]
   float *lg = h2 + kH * kAS;      // [kQB][kCMax + 1]
+  uint16_t *sw1 = reinterpret_cast<uint16_t *>(reinterpret_cast<unsigned char *>(sm) + kMlpAct);
+  uint16_t *sw3 = sw1 + kF * kH;  // [kH][C]
   const uint32_t q0 = blockIdx.x * kQB, t = threadIdx.x;
+  // the first and last layers' weights into shared memory (16-byte copies;
+  // w1 is 32 KB, w3 at most 16 KB); the middle layer's 128 KB stream from L2
+  {
+    const uint4 *g1 = reinterpret_cast<const uint4 *>(m.w1);
+    uint4 *s1 = reinterpret_cast<uint4 *>(sw1);
+    for (uint32_t i = t; i < kF * kH / 8; i += blockDim.x) s1[i] = g1[i];
+    for (uint32_t i = t; i < kH * m.C; i += blockDim.x) sw3[i] = m.w3[i];
+  }
   for (uint32_t idx = t; idx < kQB * kF; idx += blockDim.x) {
     const uint32_t i = idx / kF, f = idx % kF;
     float v = 0.f;
@@ -130,7 +143,7 @@ __global__ void __launch_bounds__(kH) probe_mlp_kernel(const float *__restrict__
     x0[f * kAS + i] = v;
   }
   __syncthreads();
-  dense_relu<kF>(x0, m.w1, m.b1, h1);
+  dense_relu<kF>(x0, sw1, m.b1, h1);
   __syncthreads();
   dense_relu<kH>(h1, m.w2, m.b2, h2);
   __syncthreads();
@@ -143,12 +156,13 @@ __global__ void __launch_bounds__(kH) probe_mlp_kernel(const float *__restrict__
       const uint32_t c = part + 8 * u;
       acc[u] = c < m.C ? m.b3[c] : 0.f;
     }
+#pragma unroll 4
     for (uint32_t k = 0; k < kH; ++k) {
       const float x = h2[k * kAS + qi];
 #pragma unroll
       for (uint32_t u = 0; u < kCMax / 8; ++u) {
         const uint32_t c = part + 8 * u;
-        if (c < m.C) acc[u] = fmaf(bf16_value(m.w3[k * m.C + c]), x, acc[u]);
+        if (c < m.C) acc[u] = fmaf(bf16_value(sw3[k * m.C + c]), x, acc[u]);
       }
     }
 #pragma unroll
@@ -445,6 +459,8 @@ int check_probe_model(const katoann_gpu_probe_model &m) {
   if (!m.d_rank || !m.d_shift || !m.d_scale || !m.d_w1 || !m.d_b1 || !m.d_w2 || !m.d_b2 ||
       !m.d_w3 || !m.d_b3 || !m.d_ladder)
     return invalid("probe model: null array");
+  if (reinterpret_cast<uintptr_t>(m.d_w1) % 16)
+    return invalid("probe model: d_w1 must be 16-byte aligned");
   return KATO_OK;
 }
 

@@ -1059,6 +1059,57 @@ int probe_features_search(const katoann_gpu_index *ix, const float *queries, uin
 
 uint32_t last_launches() { return g_launches; }
 
+// ------------------------------------------------------------ CUDA graphs
+struct SearchGraph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  uint32_t launches = 0;
+};
+
+int search_capture(const katoann_gpu_index *ix, const float *queries, uint32_t nq, uint32_t k,
+                   uint32_t p, int ranking, uint32_t survivors, uint32_t max_batch, void *ws,
+                   size_t ws_bytes, uint32_t *out_ids, float *out_dists, const Budget &budget,
+                   cudaStream_t st, void **out) {
+  *out = nullptr;
+  if (!st || st == cudaStreamLegacy || st == cudaStreamPerThread)
+    return invalid("graph capture needs a created stream");
+  KATO_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  const int rc = search(ix, queries, nq, k, p, ranking, survivors, max_batch, ws, ws_bytes,
+                        out_ids, out_dists, budget, st, nullptr);
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(st, &g);  // always ends the capture
+  if (rc || e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return rc ? rc : cuda_status(e, "cudaStreamEndCapture");
+  }
+  cudaGraphExec_t ex = nullptr;
+  const cudaError_t ei = cudaGraphInstantiate(&ex, g, 0);
+  if (ei != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return cuda_status(ei, "cudaGraphInstantiate");
+  }
+  *out = new SearchGraph{g, ex, g_launches};
+  return KATO_OK;
+}
+
+int graph_launch(void *h, cudaStream_t st) {
+  if (!h) return invalid("null graph");
+  KATO_CUDA(cudaGraphLaunch(static_cast<SearchGraph *>(h)->exec, st));
+  return KATO_OK;
+}
+
+uint32_t graph_launches(const void *h) {
+  return h ? static_cast<const SearchGraph *>(h)->launches : 0;
+}
+
+void graph_destroy(void *h) {
+  auto *g = static_cast<SearchGraph *>(h);
+  if (!g) return;
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  delete g;
+}
+
 void *timer_create(uint32_t max_passes) {
   auto *t = new PhaseTimer();
   t->max_passes = max_passes;

@@ -67,7 +67,7 @@ def _load():
     F = C.c_float
     lib.katoann_index_search_budget.argtypes = [P, P, U32, U32, U32, I32, U32, I32, P, F, P, P, P, P]
     lib.katoann_index_search_device_budget.argtypes = [P, P, U32, U32, U32, I32, U32, I32, P, F, P,
-                                                       P, P, P, P, P]
+                                                       P, P, P, P, P, I32]
     lib.katoann_probe_train.argtypes = [P, P, U32, P, U32, U32, U32, U32, I32, U32, I32, U32, U32,
                                         U32, F, F, U64, C.POINTER(P)]
     lib.katoann_probe_fit.argtypes = [P, P, U32, P, U32, U32, U32, U32, F, F, U64, C.POINTER(P)]
@@ -317,15 +317,16 @@ class Index:
                       ranking: str = "prefix", survivors: int = 32, selection: str = "threshold",
                       stream: int | None = None, timer: "PhaseTimer | None" = None,
                       budget: "ProbeModel | None" = None, threshold: float = 0.95,
-                      nprobe_per_query=None, nprobe_out=None) -> None:
+                      nprobe_per_query=None, nprobe_out=None, graph: bool = False) -> None:
         """CUDA tensors in (nq x dim float32) and out (nq x k uint32/int32,
         float32) on `stream` (a cudaStream_t as int, e.g. torch's
         ``Stream.cuda_stream``; 0 is the legacy default stream; None = the
         index's own stream). Asynchronous. nprobe_per_query / nprobe_out are
-        CUDA int32 tensors of nq values."""
+        CUDA int32 tensors of nq values. graph=True replays a CUDA graph of the
+        call, captured the first time these tensors and parameters are seen."""
         nq = int(queries.shape[0])
         tm = C.c_void_p(timer.handle) if timer else None
-        if budget is None and nprobe_per_query is None and nprobe_out is None:
+        if budget is None and nprobe_per_query is None and nprobe_out is None and not graph:
             _check(_lib.katoann_index_search_device(
                 self._h, C.c_void_p(queries.data_ptr()), nq, k, nprobe, _RANKING[ranking],
                 survivors, _SELECTION[selection], C.c_void_p(ids.data_ptr()),
@@ -336,7 +337,8 @@ class Index:
             _SELECTION[selection], budget._h if budget is not None else None, float(threshold),
             C.c_void_p(nprobe_per_query.data_ptr()) if nprobe_per_query is not None else None,
             C.c_void_p(nprobe_out.data_ptr()) if nprobe_out is not None else None,
-            C.c_void_p(ids.data_ptr()), C.c_void_p(dists.data_ptr()), _stream_arg(stream), tm))
+            C.c_void_p(ids.data_ptr()), C.c_void_p(dists.data_ptr()), _stream_arg(stream), tm,
+            int(graph)))
 
     def search_stats(self) -> dict:
         """Diagnostics of the last search (see katoann_gpu_workspace_stats)."""

@@ -256,3 +256,37 @@ def test_training_gradients_match_torch():
         g, want = grads[k].cpu(), p.grad
         tol = 1e-4 * float(want.abs().max()) + 1e-7
         assert float((g - want).abs().max()) <= tol, k
+
+
+@pytest.mark.gpu
+def test_graph_replay_equals_plain_search(tmp_path):
+    """search_device(graph=True): captured once per call signature, replayed
+    with whatever the query buffer holds; results equal the plain search."""
+    torch = pytest.importorskip("torch")
+    import katoann
+    prefix, queries, idx = _index(tmp_path)
+    train = _train_queries(SPEC, 1500)
+    model = katoann.ProbeModel.fit(katoann.ProbeModel.features(idx, train, 48),
+                                   np.random.default_rng(2).integers(0, len(LADDER), 1500)
+                                   .astype(np.uint8), ladder=LADDER, depth=48, epochs=2, seed=4)
+    nq = 128
+    q = torch.empty((nq, queries.shape[1]), dtype=torch.float32, device="cuda")
+    ids = torch.empty((nq, 10), dtype=torch.int32, device="cuda")
+    dists = torch.empty((nq, 10), dtype=torch.float32, device="cuda")
+    used = torch.empty(nq, dtype=torch.int32, device="cuda")
+    st = torch.cuda.Stream()
+    for kw in (dict(nprobe=24, ranking="prefix", survivors=32),
+               dict(nprobe=24, ranking="full"),
+               dict(nprobe=48, ranking="prefix", survivors=32, budget=model, threshold=0.8)):
+        for rep in range(3):  # capture, then two replays on new contents
+            block = queries[(rep * 37) % 150:][:nq]
+            q.copy_(torch.from_numpy(block))
+            torch.cuda.synchronize()
+            extra = dict(nprobe_out=used) if "budget" in kw else {}
+            idx.search_device(q, ids, dists, k=10, stream=st.cuda_stream, graph=True, **kw, **extra)
+            st.synchronize()
+            want = idx.search(block, k=10, return_nprobe="budget" in kw, **kw)
+            assert np.array_equal(ids.cpu().numpy().view(np.uint32), want[0]), (kw, rep)
+            assert np.array_equal(dists.cpu().numpy(), want[1]), (kw, rep)
+            if "budget" in kw:
+                assert np.array_equal(used.cpu().numpy().view(np.uint32), want[2])
