@@ -220,6 +220,7 @@ int katoann_gpu_search_timed(const katoann_gpu_index *index, const float *d_quer
  * total; epilogue waiting for query tiles, accumulators, total; TMA waiting
  * for free stages, total; query staging waiting for free query tiles, total;
  * [30] cycles the ranking pass's MMA thread spent issuing MMAs and commits;
+ * [31] cycles of the longest ranking CTA (the slowest SM's share);
  * [32..38] the same for the tensor-core coarse product: TMA waiting for free
  * stages, total; MMA waiting for accumulators, for stages, total; first
  * epilogue warp waiting for accumulators, total. */

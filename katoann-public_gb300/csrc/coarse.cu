@@ -232,14 +232,19 @@ __device__ void select_passes(const uint32_t *__restrict__ keys, uint32_t n, uin
   for (uint32_t i = tid; i < p; i += kSelThreads) outp[i] = static_cast<uint32_t>(sel[i] & 0xFFFFFFFFu);
 }
 
+// Rows are written `stride` apart. With `only`, rows whose only[q] is at
+// most only_above are skipped (a second, deeper selection for the queries
+// that need it).
 __global__ void __launch_bounds__(kSelThreads) select_topp_kernel(
-    const float *__restrict__ dists, uint32_t n, uint32_t p, uint32_t *__restrict__ probed,
-    unsigned long long *__restrict__ tie_count) {
+    const float *__restrict__ dists, uint32_t n, uint32_t p, uint32_t stride,
+    uint32_t *__restrict__ probed, unsigned long long *__restrict__ tie_count,
+    const uint32_t *__restrict__ only, uint32_t only_above) {
   extern __shared__ unsigned long long sel[];  // up to kSortMax (key << 32 | id)
   __shared__ uint32_t hist[256], scal[4];
   const uint32_t q = blockIdx.x;
+  if (only && only[q] <= only_above) return;
   select_passes(reinterpret_cast<const uint32_t *>(dists) + static_cast<size_t>(q) * n, n, p,
-                probed + static_cast<size_t>(q) * p, tie_count, sel, hist, scal);
+                probed + static_cast<size_t>(q) * stride, tie_count, sel, hist, scal);
 }
 
 // In-shared-memory bitonic sort of n 64-bit keys, ascending.
@@ -276,8 +281,9 @@ constexpr uint32_t kHistBins = 4096;
 constexpr uint32_t kCand = 2048;
 
 __global__ void __launch_bounds__(kSelThreads) select_topp_hist_kernel(
-    const float *__restrict__ dists, uint32_t n, uint32_t p, uint32_t *__restrict__ probed,
-    unsigned long long *__restrict__ tie_count) {
+    const float *__restrict__ dists, uint32_t n, uint32_t p, uint32_t stride,
+    uint32_t *__restrict__ probed, unsigned long long *__restrict__ tie_count,
+    const uint32_t *__restrict__ only, uint32_t only_above) {
   extern __shared__ unsigned long long dyn[];
   unsigned long long *cand = dyn;          // kCand
   unsigned long long *sel = dyn + kCand;   // np2(p)
@@ -285,8 +291,9 @@ __global__ void __launch_bounds__(kSelThreads) select_topp_hist_kernel(
   __shared__ uint32_t scal[8];
   __shared__ uint32_t wsum[kSelThreads / 32];
   const uint32_t q = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (only && only[q] <= only_above) return;
   const uint32_t *keys = reinterpret_cast<const uint32_t *>(dists) + static_cast<size_t>(q) * n;
-  uint32_t *outp = probed + static_cast<size_t>(q) * p;
+  uint32_t *outp = probed + static_cast<size_t>(q) * stride;
   for (uint32_t i = tid; i < kHistBins; i += kSelThreads) hist[i] = 0;
   if (tid < 8) scal[tid] = 0;
   __syncthreads();
@@ -387,10 +394,11 @@ int sq16_tiles(const uint8_t *qhi, const uint8_t *qlo, const uint8_t *xhi, const
   return KATO_OK;
 }
 
-int select_topp(const float *dists, uint32_t nq, uint32_t n, uint32_t p, uint32_t *probed,
-                unsigned long long *tie_count, cudaStream_t st) {
+int select_topp_ex(const float *dists, uint32_t nq, uint32_t n, uint32_t p, uint32_t stride,
+                   uint32_t *probed, unsigned long long *tie_count, const uint32_t *only,
+                   uint32_t only_above, cudaStream_t st) {
   if (nq == 0) return KATO_OK;
-  if (p == 0 || p > n) return invalid("need 1 <= nprobe <= nlist");
+  if (p == 0 || p > n || stride < p) return invalid("need 1 <= nprobe <= nlist");
   uint32_t np2 = 1;
   while (np2 < p) np2 <<= 1;
   static bool attr_set = false;
@@ -405,13 +413,20 @@ int select_topp(const float *dists, uint32_t nq, uint32_t n, uint32_t p, uint32_
   if (p <= kSortMax) {
     // candidates and the sorted selection (the bitonic sort pads to a power of two)
     const size_t smem = (kCand + std::max<uint32_t>(np2, 2)) * sizeof(unsigned long long);
-    select_topp_hist_kernel<<<nq, kSelThreads, smem, st>>>(dists, n, p, probed, tie_count);
+    select_topp_hist_kernel<<<nq, kSelThreads, smem, st>>>(dists, n, p, stride, probed, tie_count,
+                                                            only, only_above);
     KATO_LAUNCHED("select_topp_hist_kernel");
     return KATO_OK;
   }
-  select_topp_kernel<<<nq, kSelThreads, 0, st>>>(dists, n, p, probed, tie_count);
+  select_topp_kernel<<<nq, kSelThreads, 0, st>>>(dists, n, p, stride, probed, tie_count, only,
+                                                  only_above);
   KATO_LAUNCHED("select_topp_kernel");
   return KATO_OK;
+}
+
+int select_topp(const float *dists, uint32_t nq, uint32_t n, uint32_t p, uint32_t *probed,
+                unsigned long long *tie_count, cudaStream_t st) {
+  return select_topp_ex(dists, nq, n, p, p, probed, tie_count, nullptr, 0, st);
 }
 
 int dist_values(const int64_t *l2, uint32_t n, double step_sq, float *out, cudaStream_t st) {

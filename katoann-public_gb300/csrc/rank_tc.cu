@@ -517,6 +517,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   if (tid == 0) {
     if (*err) atomicAdd(A.timeouts, 1u);
     A.rec_n[blockIdx.x] = min(*rcount, A.rec_cap);
+    // the longest CTA (cycles): against the average it shows the schedule's imbalance
+    if (A.prof) atomicMax(A.prof + 15, static_cast<unsigned long long>(clock64() - tstart));
   }
   if (warp == kMmaWarp) tc::tmem_dealloc(tmem, S.tcols);
 }

@@ -631,8 +631,9 @@ int coarse_tc(const __half *ch, const __half *cl, const int64_t *cterm, uint32_t
 size_t rotate_scratch_bytes(uint32_t nrows, uint32_t d);
 int rotate_rows_kmajor(const float *in, uint32_t nrows, uint32_t d, const float *rot, void *scratch,
                        float *out, cudaStream_t st);
-int select_topp(const float *dists, uint32_t nq, uint32_t n, uint32_t p, uint32_t *probed,
-                unsigned long long *tie_count, cudaStream_t st);
+int select_topp_ex(const float *dists, uint32_t nq, uint32_t n, uint32_t p, uint32_t stride,
+                   uint32_t *probed, unsigned long long *tie_count, const uint32_t *only,
+                   uint32_t only_above, cudaStream_t st);
 
 struct PhaseTimer {
   std::vector<cudaEvent_t> ev;  // (KATO_PHASES + 1) per pass
@@ -748,11 +749,12 @@ int make_plan(const katoann_gpu_index *ix, uint32_t B, uint32_t k, uint32_t p, i
   return KATO_OK;
 }
 
-// Rotation, quantization, coarse product and top-p selection of nq queries
+// Rotation, quantization, coarse product and top-p1 selection of nq queries
 // (phases 0-2): leaves the query planes, the coarse distances (cd) and each
-// query's p nearest lists in order (probed) in the workspace.
+// query's p1 nearest lists in order (probed, rows pl.p apart) in the
+// workspace.
 int coarse_pass(const katoann_gpu_index *ix, const Plan &pl, const float *queries, uint32_t nq,
-                unsigned char *ws, cudaStream_t st, PhaseTimer *tm) {
+                unsigned char *ws, uint32_t p1, cudaStream_t st, PhaseTimer *tm) {
   int rc;
   const uint32_t L = ix->nlist, p = pl.p, dc = ix->dc;
   float *fq = reinterpret_cast<float *>(ws + pl.off_fq);
@@ -796,7 +798,7 @@ int coarse_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
     return rc;
   }
   mark(tm, 2, st);
-  if ((rc = select_topp(cd, nq, L, p, probed, stats + 0, st))) return rc;
+  if ((rc = select_topp_ex(cd, nq, L, p1, p, probed, stats + 0, nullptr, 0, st))) return rc;
   mark(tm, 3, st);
   return KATO_OK;
 }
@@ -823,7 +825,11 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
   uint32_t *nsurv = reinterpret_cast<uint32_t *>(ws + pl.off_nsurv);
   unsigned long long *stats = reinterpret_cast<unsigned long long *>(ws + pl.off_stats);
 
-  if ((rc = coarse_pass(ix, pl, queries, nq, ws, st, tm))) return rc;
+  // with a model, the selection first goes as deep as its features and then,
+  // for the queries whose budget is deeper, to the cap
+  const bool model = bud.model && !bud.nprobe_in;
+  const uint32_t p1 = model ? std::min(p, bud.model->depth) : p;
+  if ((rc = coarse_pass(ix, pl, queries, nq, ws, p1, st, tm))) return rc;
   // 2'. per-query budgets: given, or from the model over the coarse distances
   uint32_t *qprobes = nullptr;
   if (bud.active()) {
@@ -836,6 +842,10 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
       if ((rc = probe_features(cd, L, probed, p, bud.model->d_rank, nq, z, st))) return rc;
       if ((rc = probe_budget(*bud.model, z, nq, bud.cap, nullptr, qprobes, st))) return rc;
       g_launches += 2;
+      if (p1 < p) {
+        if ((rc = select_topp_ex(cd, nq, L, p, p, probed, nullptr, qprobes, p1, st))) return rc;
+        ++g_launches;
+      }
     }
     if (bud.nprobe_out)
       KATO_CUDA(cudaMemcpyAsync(bud.nprobe_out, qprobes, static_cast<size_t>(nq) * 4,
@@ -1047,7 +1057,8 @@ int probe_features_search(const katoann_gpu_index *ix, const float *queries, uin
   g_launches = 0;
   for (uint32_t q0 = 0; q0 < nq; q0 += max_batch) {
     const uint32_t b = std::min(max_batch, nq - q0);
-    if ((rc = coarse_pass(ix, pl, queries + static_cast<size_t>(q0) * ix->dim, b, w, st, nullptr)))
+    if ((rc = coarse_pass(ix, pl, queries + static_cast<size_t>(q0) * ix->dim, b, w, depth, st,
+                          nullptr)))
       return rc;
     if ((rc = probe_features(reinterpret_cast<float *>(w + pl.off_cd), ix->nlist,
                              reinterpret_cast<uint32_t *>(w + pl.off_probed), depth, rank, b,

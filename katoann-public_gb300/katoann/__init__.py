@@ -347,7 +347,7 @@ class Index:
         return dict(coarse_boundary_ties=int(s[0]), survivor_boundary_ties=int(s[1]),
                     ranking_timeouts=int(s[3]), ranking_tiles=int(s[4]),
                     ranking_candidates=int(s[5]), ranking_rescans=int(s[6]),
-                    ranking_max_candidates=int(s[7]),
+                    ranking_max_candidates=int(s[7]), ranking_cta_max_cycles=int(s[31]),
                     ranking_role_cycles=dict(zip(
                         ("conv_wait_raw", "conv_wait_a", "conv_total", "mma_wait_b", "mma_wait_acc",
                          "mma_wait_a", "mma_total", "epi_wait_b", "epi_wait_acc", "epi_total",

@@ -168,6 +168,14 @@ def test_trained_model_search_equals_oracle_at_its_budgets(tmp_path):
     _, _, u2 = idx.search(queries, nprobe=48, budget=again, threshold=0.9, return_nprobe=True)
     _, _, u1 = idx.search(queries, nprobe=48, budget=model, threshold=0.9, return_nprobe=True)
     assert np.array_equal(u1, u2)
+    # features shallower than the cap: the queries whose budget exceeds the
+    # feature depth take a second, deeper selection
+    shallow = katoann.ProbeModel.fit(katoann.ProbeModel.features(idx, train, 16), labels,
+                                     ladder=LADDER, depth=16, epochs=20, batch=256, seed=5)
+    ids, dists, used = idx.search(queries, k=10, nprobe=48, survivors=32, budget=shallow,
+                                  threshold=0.95, return_nprobe=True)
+    assert (used > 16).any() and (used <= 16).any()
+    _check_against_oracle(ref, queries, ids, dists, used, k=10, ranking="prefix", survivors=32)
 
 
 @pytest.mark.gpu
