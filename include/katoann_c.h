@@ -118,6 +118,28 @@ int katoann_probe_features(void *index, const float *queries, uint32_t nq, uint3
 int katoann_probe_predict(const void *model, const float *z, uint32_t n, float threshold,
                           uint32_t cap, float *probs, uint32_t *nprobe);
 
+/* ------------------------------------------- continuous-batching server
+ * katoann::Server (include/katoann/server.h); supersedes the serial loop of
+ * the reference's `katoann load` (tools/katoann.cpp:304-321). hbm_budget 0:
+ * room for max_in_flight full batches; model NULL: fixed nprobe. */
+int katoann_server_new(void *index, uint32_t max_batch, uint32_t max_in_flight,
+                       uint64_t hbm_budget, uint32_t max_k, uint32_t nprobe, int ranking,
+                       uint32_t survivors, const void *model, float threshold,
+                       double max_wait_ms, void **server);
+void katoann_server_free(void *server);
+/* Queues one query (dim floats) with its k; *id receives the request id. */
+int katoann_server_submit(void *server, const float *query, uint32_t k, uint64_t *id);
+/* Blocks until request `id` is done: ids and dists (k each), its nprobe and
+ * its latency from submit to completion. */
+int katoann_server_wait(void *server, uint64_t id, uint32_t *ids, float *dists,
+                        uint32_t *nprobe, double *latency_ms);
+/* The same without blocking: *done = 0 when the request is still running. */
+int katoann_server_poll(void *server, uint64_t id, uint32_t *ids, float *dists,
+                        uint32_t *nprobe, double *latency_ms, int *done);
+int katoann_server_drain(void *server);
+/* stats[5] = {requests, batches, peak_in_flight, peak_hbm_bytes, mean_batch x 1000} */
+int katoann_server_stats(void *server, uint64_t *stats);
+
 /* info[8] = {dim, nlist, size, prefix_dims, rotated, normalized, batched_coarse, engine=2} */
 int katoann_index_info(void *index, uint32_t *info);
 size_t katoann_index_memory_bytes(void *index);

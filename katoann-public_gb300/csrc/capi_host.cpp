@@ -6,6 +6,7 @@
 #include "dist_value.h"
 #include "katoann/index.h"
 #include "katoann/probe.h"
+#include "katoann/server.h"
 #include "katoann_c.h"
 
 namespace {
@@ -200,6 +201,72 @@ int katoann_index_stats(void *index, uint64_t *stats, uint32_t n) {
 }
 
 const void *katoann_index_device_view(void *index) { return I(index)->device_view(); }
+
+int katoann_server_new(void *index, uint32_t max_batch, uint32_t max_in_flight,
+                       uint64_t hbm_budget, uint32_t max_k, uint32_t nprobe, int ranking,
+                       uint32_t survivors, const void *model, float threshold,
+                       double max_wait_ms, void **server) {
+  return guarded([&] {
+    katoann::ServerOptions o;
+    o.max_batch = max_batch;
+    o.max_in_flight = max_in_flight;
+    o.hbm_budget = hbm_budget;
+    o.max_k = max_k;
+    o.nprobe = nprobe;
+    o.ranking = ranking_of(ranking);
+    o.survivors = survivors;
+    o.budget = M(model);
+    o.budget_threshold = threshold;
+    o.max_wait_ms = max_wait_ms;
+    *server = new katoann::Server(*I(index), o);
+  });
+}
+
+void katoann_server_free(void *server) { delete static_cast<katoann::Server *>(server); }
+
+namespace {
+katoann::Server *SV(void *p) { return static_cast<katoann::Server *>(p); }
+void put_result(const katoann::ServerResult &r, uint32_t *ids, float *dists, uint32_t *nprobe,
+                double *latency_ms) {
+  if (ids) std::copy(r.ids.begin(), r.ids.end(), ids);
+  if (dists) std::copy(r.dists.begin(), r.dists.end(), dists);
+  if (nprobe) *nprobe = r.nprobe;
+  if (latency_ms) *latency_ms = r.latency_ms;
+}
+}  // namespace
+
+int katoann_server_submit(void *server, const float *query, uint32_t k, uint64_t *id) {
+  return guarded([&] { *id = SV(server)->submit(query, k); });
+}
+
+int katoann_server_wait(void *server, uint64_t id, uint32_t *ids, float *dists,
+                        uint32_t *nprobe, double *latency_ms) {
+  return guarded([&] { put_result(SV(server)->wait(id), ids, dists, nprobe, latency_ms); });
+}
+
+int katoann_server_poll(void *server, uint64_t id, uint32_t *ids, float *dists,
+                        uint32_t *nprobe, double *latency_ms, int *done) {
+  return guarded([&] {
+    katoann::ServerResult r;
+    *done = SV(server)->poll(id, &r) ? 1 : 0;
+    if (*done) put_result(r, ids, dists, nprobe, latency_ms);
+  });
+}
+
+int katoann_server_drain(void *server) {
+  return guarded([&] { SV(server)->drain(); });
+}
+
+int katoann_server_stats(void *server, uint64_t *stats) {
+  return guarded([&] {
+    const katoann::ServerStats s = SV(server)->stats();
+    stats[0] = s.requests;
+    stats[1] = s.batches;
+    stats[2] = s.peak_in_flight;
+    stats[3] = s.peak_hbm_bytes;
+    stats[4] = static_cast<uint64_t>(s.mean_batch * 1000.0);
+  });
+}
 
 int katoann_index_search_budget(void *index, const float *queries, uint32_t nq, uint32_t k,
                                 uint32_t nprobe, int ranking, uint32_t survivors, int selection,

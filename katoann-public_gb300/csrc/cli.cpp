@@ -11,12 +11,16 @@
 //                  [--repeat 3] [--threads T] [--query-ids FILE] [--out PREFIX]
 //                  [--code-cache]
 //   katoann load   --index PREFIX --queries Q.fbin --rate QPS [--requests 10000]
-//                  [--nprobe 64] [--max-batch 4096] [--seed 42] and the search flags
+//                  [--nprobe 64] [--max-batch 4096] [--seed 42] [--k-mix 10,100]
+//                  [--in-flight 3] [--hbm-budget-gb G] [--max-wait-ms 0]
+//                  [--budget MODEL.kprb --threshold 0.95] and the search flags
 //
-// `load` is the serving loop: requests arrive as a Poisson process; whenever
-// the GPU is idle it takes every request that has arrived (up to --max-batch)
-// and answers them as one batch; latency runs from arrival to the end of that
-// batch (tools/katoann.cpp:263-337). Errors print to stderr and exit 1, as the
+// `load` serves requests that arrive as a Poisson process (tools/katoann.cpp:
+// 263-337), here through the continuous-batching katoann::Server: arrivals are
+// batched per k while earlier batches are still on the device (up to
+// --in-flight batches within --hbm-budget-gb), optionally with the learned
+// per-query nprobe of a ProbeModel file; latency runs from a request's
+// arrival to its completion. Errors print to stderr and exit 1, as the
 // reference's main does.
 #include <omp.h>
 
@@ -36,6 +40,8 @@
 #include <vector>
 
 #include "katoann/index.h"
+#include "katoann/probe.h"
+#include "katoann/server.h"
 
 namespace {
 
@@ -284,66 +290,89 @@ int cmd_load(const Args &a) {
   const std::vector<float> queries = load_queries(a, idx, nq);
   const uint32_t d = idx.dim();
   const std::vector<uint32_t> pool = query_ids(a, nq);
-  katoann::SearchParams p = search_params(a);
-  p.nprobe = a.u32("nprobe", 64);
+  const katoann::SearchParams sp = search_params(a);
+  // per-request k: one value, or a list drawn uniformly per request
+  const std::vector<uint32_t> kmix = u32_list(a.get("k-mix", std::to_string(sp.k)));
+  if (kmix.empty()) throw std::invalid_argument("empty --k-mix");
+  katoann::ProbeModel model;
+  katoann::ServerOptions so;
+  so.max_batch = std::max(1u, std::min(4096u, a.u32("max-batch", 4096)));
+  so.max_in_flight = a.u32("in-flight", 3);
+  so.hbm_budget = static_cast<size_t>(a.num("hbm-budget-gb", 0) * 1e9);
+  so.max_k = *std::max_element(kmix.begin(), kmix.end());
+  so.nprobe = a.u32("nprobe", 64);
+  so.ranking = sp.ranking;
+  so.survivors = sp.survivors;
+  so.max_wait_ms = a.num("max-wait-ms", 0);
+  if (!a.get("budget").empty()) {  // learned per-query nprobe, capped at --nprobe
+    model = katoann::ProbeModel::load(a.get("budget"));
+    so.budget = &model;
+    so.budget_threshold = static_cast<float>(a.num("threshold", 0.95));
+  }
   const double rate = a.num("rate", 1000);
-  const uint32_t n = a.u32("requests", 10000), max_batch = std::max(1u, a.u32("max-batch", 4096));
+  const uint32_t n = a.u32("requests", 10000);
   // Poisson arrivals, queries taken round-robin from the pool
   std::mt19937_64 rng(a.u32("seed", 42));
   std::exponential_distribution<double> gap(rate);
   std::vector<double> arrival(n);
-  std::vector<uint32_t> which(n);
+  std::vector<uint32_t> which(n), kof(n);
   double t = 0;
   for (uint32_t i = 0; i < n; ++i) {
     t += gap(rng);
     arrival[i] = t;
     which[i] = pool[i % pool.size()];
+    kof[i] = kmix[rng() % kmix.size()];
   }
-  std::vector<float> batch_q(static_cast<size_t>(max_batch) * d);
-  std::vector<uint32_t> ids(static_cast<size_t>(max_batch) * p.k);
-  std::vector<float> dists(static_cast<size_t>(max_batch) * p.k);
-  std::vector<double> latency(n);
-  std::vector<uint32_t> sizes;
-  const uint32_t warm = std::min<uint32_t>(max_batch, static_cast<uint32_t>(pool.size()));
-  for (uint32_t w = 0; w < warm; ++w)
-    std::memcpy(batch_q.data() + static_cast<size_t>(w) * d,
-                queries.data() + static_cast<size_t>(pool[w]) * d, d * sizeof(float));
-  idx.search(batch_q.data(), warm, p, ids.data(), dists.data());  // warm-up
+  katoann::Server server(idx, so);
+  {  // warm-up: one full batch of each k
+    std::vector<uint64_t> ids;
+    for (uint32_t k : kmix)
+      for (uint32_t w = 0; w < std::min<uint32_t>(so.max_batch, static_cast<uint32_t>(pool.size())); ++w)
+        ids.push_back(server.submit(queries.data() + static_cast<size_t>(pool[w]) * d, k));
+    for (uint64_t id : ids) server.wait(id);
+  }
+  const katoann::ServerStats before = server.stats();
+  // the client: submits each request at its arrival time, then collects;
+  // latency runs from the scheduled arrival to completion
+  std::vector<uint64_t> rid(n);
+  std::vector<double> lag(n);
   const auto start = Clock::now();
-  uint32_t next = 0;
-  while (next < n) {
-    double now = seconds_since(start);
-    if (arrival[next] > now) {
-      std::this_thread::sleep_for(std::chrono::duration<double>(arrival[next] - now));
-      now = seconds_since(start);
+  std::thread client([&] {
+    for (uint32_t i = 0; i < n; ++i) {
+      const double now = seconds_since(start);
+      if (arrival[i] > now)
+        std::this_thread::sleep_for(std::chrono::duration<double>(arrival[i] - now));
+      lag[i] = std::max(0.0, seconds_since(start) - arrival[i]);
+      rid[i] = server.submit(queries.data() + static_cast<size_t>(which[i]) * d, kof[i]);
     }
-    uint32_t end = next;
-    while (end < n && end - next < max_batch && arrival[end] <= now) ++end;
-    const uint32_t b = end - next;
-    for (uint32_t i = 0; i < b; ++i)
-      std::memcpy(batch_q.data() + static_cast<size_t>(i) * d,
-                  queries.data() + static_cast<size_t>(which[next + i]) * d, d * sizeof(float));
-    idx.search(batch_q.data(), b, p, ids.data(), dists.data());
-    const double done = seconds_since(start);
-    for (uint32_t i = 0; i < b; ++i) latency[next + i] = done - arrival[next + i];
-    sizes.push_back(b);
-    next = end;
+  });
+  client.join();
+  std::vector<double> latency(n);
+  uint64_t probes = 0;
+  for (uint32_t i = 0; i < n; ++i) {
+    const katoann::ServerResult r = server.wait(rid[i]);
+    latency[i] = lag[i] + r.latency_ms / 1e3;
+    probes += r.nprobe;
   }
   const double span = seconds_since(start);
+  const katoann::ServerStats st = server.stats();
   std::vector<double> sorted = latency;
   std::sort(sorted.begin(), sorted.end());
   auto pct = [&](double f) {
     const size_t r = static_cast<size_t>(std::ceil(f * sorted.size()));
     return sorted[std::min(sorted.size() - 1, r ? r - 1 : 0)];
   };
-  double mean_batch = 0;
-  for (const uint32_t s : sizes) mean_batch += s;
-  mean_batch /= static_cast<double>(sizes.size());
+  const uint64_t batches = st.batches - before.batches;
   std::printf("{\"rate\": %.1f, \"requests\": %u, \"nprobe\": %u, \"engine\": \"gpu\", "
               "\"achieved_qps\": %.1f, \"p50_ms\": %.2f, \"p95_ms\": %.2f, \"p99_ms\": %.2f, "
-              "\"max_ms\": %.2f, \"batches\": %zu, \"mean_batch\": %.1f}\n",
-              rate, n, p.nprobe, n / span, pct(0.50) * 1e3, pct(0.95) * 1e3, pct(0.99) * 1e3,
-              sorted.back() * 1e3, sizes.size(), mean_batch);
+              "\"max_ms\": %.2f, \"batches\": %llu, \"mean_batch\": %.1f, \"in_flight\": %u, "
+              "\"peak_in_flight\": %u, \"peak_hbm_gb\": %.3f, \"learned\": %s, "
+              "\"mean_nprobe\": %.2f}\n",
+              rate, n, so.nprobe, n / span, pct(0.50) * 1e3, pct(0.95) * 1e3, pct(0.99) * 1e3,
+              sorted.back() * 1e3, static_cast<unsigned long long>(batches),
+              batches ? static_cast<double>(n) / batches : 0.0, so.max_in_flight,
+              st.peak_in_flight, st.peak_hbm_bytes / 1e9, so.budget ? "true" : "false",
+              static_cast<double>(probes) / n);
   return 0;
 }
 
@@ -358,8 +387,9 @@ void usage() {
                "                      [--repeat 3] [--threads T] [--query-ids FILE] [--out PREFIX]\n"
                "                      [--code-cache]\n"
                "       katoann load   --index PREFIX --queries Q.fbin --rate QPS [--requests 10000]\n"
-               "                      [--nprobe 64] [--max-batch 4096] [--seed 42] and the search\n"
-               "                      flags\n");
+               "                      [--nprobe 64] [--max-batch 4096] [--seed 42] [--k-mix 10,100]\n"
+               "                      [--in-flight 3] [--hbm-budget-gb G] [--max-wait-ms 0]\n"
+               "                      [--budget MODEL.kprb --threshold 0.95] and the search flags\n");
 }
 
 }  // namespace

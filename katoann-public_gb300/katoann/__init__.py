@@ -79,6 +79,13 @@ def _load():
     lib.katoann_probe_weights.argtypes = [P, P, P, P, P, P, P, P, P]
     lib.katoann_probe_features.argtypes = [P, P, U32, U32, P]
     lib.katoann_probe_predict.argtypes = [P, P, U32, F, U32, P, P]
+    lib.katoann_server_new.argtypes = [P, U32, U32, U64, U32, U32, I32, U32, P, F, D, C.POINTER(P)]
+    lib.katoann_server_free.argtypes = [P]
+    lib.katoann_server_submit.argtypes = [P, P, U32, C.POINTER(U64)]
+    lib.katoann_server_wait.argtypes = [P, U64, P, P, P, P]
+    lib.katoann_server_poll.argtypes = [P, U64, P, P, P, P, P]
+    lib.katoann_server_drain.argtypes = [P]
+    lib.katoann_server_stats.argtypes = [P, P]
     return lib
 
 
@@ -566,3 +573,64 @@ class ProbeModel:
         _check(_lib.katoann_probe_predict(self._h, _ptr(z), n, threshold, cap, _ptr(probs),
                                           _ptr(nprobe)))
         return probs, nprobe
+
+
+class Server:
+    """Continuous-batching search server (include/katoann/server.h): requests
+    with their own k are batched on arrival, several batches run on the
+    device at once within an HBM budget, and every result equals the search
+    of that query alone. ``submit`` returns an id; ``wait`` returns
+    (ids, dists, nprobe, latency_ms)."""
+
+    def __init__(self, index: Index, max_batch: int = 4096, max_in_flight: int = 3,
+                 hbm_budget: int = 0, max_k: int = 128, nprobe: int = 64,
+                 ranking: str = "prefix", survivors: int = 32,
+                 budget: "ProbeModel | None" = None, threshold: float = 0.95,
+                 max_wait_ms: float = 0.0):
+        self._index = index  # the server reads the index's device arrays
+        self._budget = budget
+        self.dim = index.dim
+        self.normalized = index.normalized
+        self._k = {}
+        h = C.c_void_p()
+        _check(_lib.katoann_server_new(index._h, max_batch, max_in_flight, hbm_budget, max_k,
+                                       nprobe, _RANKING[ranking], survivors,
+                                       budget._h if budget is not None else None, threshold,
+                                       max_wait_ms, C.byref(h)))
+        self._h = h.value
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            _lib.katoann_server_free(h)
+            self._h = None
+
+    def submit(self, query, k: int = 10) -> int:
+        q = np.ascontiguousarray(query, dtype=np.float32).reshape(1, -1)
+        if q.shape[1] != self.dim:
+            raise ValueError("query must have dim floats")
+        if self.normalized:
+            q = normalize_rows(q)
+        rid = C.c_uint64()
+        _check(_lib.katoann_server_submit(self._h, _ptr(q), k, C.byref(rid)))
+        self._k[rid.value] = k
+        return rid.value
+
+    def wait(self, rid: int):
+        k = self._k.pop(rid)
+        ids = np.zeros(k, np.uint32)
+        dists = np.zeros(k, np.float32)
+        npb = np.zeros(1, np.uint32)
+        lat = np.zeros(1, np.float64)
+        _check(_lib.katoann_server_wait(self._h, rid, _ptr(ids), _ptr(dists), _ptr(npb),
+                                        _ptr(lat)))
+        return ids, dists, int(npb[0]), float(lat[0])
+
+    def drain(self) -> None:
+        _check(_lib.katoann_server_drain(self._h))
+
+    def stats(self) -> dict:
+        s = np.zeros(5, np.uint64)
+        _check(_lib.katoann_server_stats(self._h, _ptr(s)))
+        return dict(requests=int(s[0]), batches=int(s[1]), peak_in_flight=int(s[2]),
+                    peak_hbm_bytes=int(s[3]), mean_batch=float(s[4]) / 1000.0)

@@ -116,3 +116,24 @@ def test_load_serves_poisson_requests(tmp_path):
     assert x["requests"] == 3000 and x["engine"] == "gpu" and x["nprobe"] == 8
     assert 0 < x["p50_ms"] <= x["p95_ms"] <= x["p99_ms"] <= x["max_ms"]
     assert x["batches"] >= 3000 / 256 and 1 <= x["mean_batch"] <= 256
+
+
+@pytest.mark.gpu
+def test_load_serves_mixed_k_with_a_learned_budget(tmp_path):
+    import katoann
+    spec = dict(seed=33, n=6000, dim=64, ncomp=8, nlist=48, nq=300, rotation="random")
+    prefix = str(tmp_path / "x")
+    queries, _ = synth.materialize(spec, prefix)
+    write_fbin(tmp_path / "q.fbin", queries)
+    idx = katoann.Index()
+    idx.load(prefix)
+    train = synth.to_f32(synth.mixture_ints(33, 30, 1500, 64, 8))
+    model = katoann.ProbeModel.train(idx, train, ladder=(2, 4, 8, 16, 32), depth=32,
+                                     label_nprobe=48, survivors=32, epochs=5, batch=256)
+    model.save(str(tmp_path / "m.kprb"))
+    p = run("load", "--index", prefix, "--queries", str(tmp_path / "q.fbin"), "--rate", "20000",
+            "--requests", "2000", "--nprobe", "32", "--k-mix", "10,100", "--in-flight", "2",
+            "--budget", str(tmp_path / "m.kprb"), "--threshold", "0.9")
+    x = json_lines(p.stdout)[-1]
+    assert x["requests"] == 2000 and x["learned"] is True and x["in_flight"] == 2
+    assert 0 < x["p50_ms"] <= x["p99_ms"] and 1 <= x["mean_nprobe"] <= 32

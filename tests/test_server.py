@@ -1,0 +1,102 @@
+"""The continuous-batching server (katoann.Server, csrc/server.cpp): requests
+with their own k, submitted from several threads while earlier batches are on
+the device, come back exactly as a search of that query alone gives them,
+with a fixed or a learned nprobe and under an HBM budget that forces small
+batches."""
+import threading
+
+import numpy as np
+import pytest
+
+import synth
+
+SPEC = dict(seed=61, n=20000, dim=64, ncomp=24, nlist=96, nq=400, rotation="random")
+
+
+def test_server_before_load_is_a_logic_error():
+    import katoann
+    with pytest.raises(RuntimeError, match="logic error: server before load"):
+        katoann.Server(katoann.Index())
+
+
+def _index(tmp_path):
+    import katoann
+    prefix = str(tmp_path / "x")
+    queries, _ = synth.materialize(SPEC, prefix)
+    idx = katoann.Index()
+    idx.load(prefix)
+    return queries, idx
+
+
+def _serve(server, queries, ks, threads=3, seed=0):
+    """Submits queries[i] with ks[i] from several threads with random pauses;
+    returns every result by request index."""
+    ids = [None] * len(queries)
+    rng = np.random.default_rng(seed)
+    pauses = rng.exponential(2e-5, len(queries))
+
+    def client(part):
+        import time
+        for i in part:
+            time.sleep(pauses[i])
+            ids[i] = server.submit(queries[i], int(ks[i]))
+
+    parts = np.array_split(np.arange(len(queries)), threads)
+    ts = [threading.Thread(target=client, args=(p,)) for p in parts]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    return [server.wait(r) for r in ids]
+
+
+def _check_alone(idx, queries, ks, results, **kw):
+    for k in np.unique(ks):
+        sel = np.nonzero(ks == k)[0]
+        out = idx.search(queries[sel], k=int(k), return_nprobe=True, **kw)
+        for j, i in enumerate(sel):
+            ids, dists, npb, _ = results[i]
+            assert np.array_equal(ids, out[0][j]) and np.array_equal(dists, out[1][j]), (i, k)
+            assert npb == out[2][j]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("learned", [False, True])
+def test_results_in_the_mix_equal_alone(tmp_path, learned):
+    import katoann
+    queries, idx = _index(tmp_path)
+    model = None
+    if learned:
+        train = synth.to_f32(synth.mixture_ints(SPEC["seed"], 30, 2000, SPEC["dim"], SPEC["ncomp"]))
+        model = katoann.ProbeModel.train(idx, train, ladder=(2, 4, 8, 16, 32), depth=32,
+                                         label_nprobe=96, survivors=32, epochs=10, batch=256)
+    ks = np.random.default_rng(3).choice([10, 100], len(queries))
+    server = katoann.Server(idx, max_batch=64, max_in_flight=3, max_k=100, nprobe=32,
+                            survivors=32, budget=model, threshold=0.9)
+    res = _serve(server, queries, ks)
+    stats = server.stats()
+    assert stats["requests"] == len(queries) and stats["batches"] >= len(queries) / 64
+    assert stats["peak_in_flight"] >= 1
+    assert all(r[3] > 0 for r in res)
+    _check_alone(idx, queries, ks, res, nprobe=32, survivors=32, budget=model, threshold=0.9)
+
+
+@pytest.mark.gpu
+def test_hbm_budget_cuts_batches(tmp_path):
+    import katoann
+    queries, idx = _index(tmp_path)
+    # room for about ten queries' worth of workspace at k = 10
+    big = katoann.Server(idx, max_batch=4096, max_in_flight=1, max_k=10, nprobe=16)
+    res_big = _serve(big, queries, np.full(len(queries), 10), threads=1)
+    peak = big.stats()["peak_hbm_bytes"]
+    del big
+    budget = max(1, peak // 40)
+    small = katoann.Server(idx, max_batch=4096, max_in_flight=2, max_k=10, nprobe=16,
+                           hbm_budget=budget)
+    res = _serve(small, queries, np.full(len(queries), 10), threads=2)
+    st = small.stats()
+    assert st["peak_hbm_bytes"] <= budget
+    assert st["batches"] > 1
+    for a, b in zip(res, res_big):
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    _check_alone(idx, queries, np.full(len(queries), 10), res, nprobe=16)
