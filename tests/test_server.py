@@ -85,18 +85,19 @@ def test_results_in_the_mix_equal_alone(tmp_path, learned):
 def test_hbm_budget_cuts_batches(tmp_path):
     import katoann
     queries, idx = _index(tmp_path)
-    # room for about ten queries' worth of workspace at k = 10
-    big = katoann.Server(idx, max_batch=4096, max_in_flight=1, max_k=10, nprobe=16)
-    res_big = _serve(big, queries, np.full(len(queries), 10), threads=1)
-    peak = big.stats()["peak_hbm_bytes"]
-    del big
-    budget = max(1, peak // 40)
+    ks = np.full(len(queries), 10)
+    # the device memory of a 16-query batch, from a server capped at 16
+    probe = katoann.Server(idx, max_batch=16, max_in_flight=1, max_k=10, nprobe=16)
+    res16 = _serve(probe, queries, ks, threads=1)
+    budget = probe.stats()["peak_hbm_bytes"]
+    del probe
+    # a server allowed 4096-query batches, but with only that much memory
     small = katoann.Server(idx, max_batch=4096, max_in_flight=2, max_k=10, nprobe=16,
                            hbm_budget=budget)
-    res = _serve(small, queries, np.full(len(queries), 10), threads=2)
+    res = _serve(small, queries, ks, threads=2)
     st = small.stats()
     assert st["peak_hbm_bytes"] <= budget
-    assert st["batches"] > 1
-    for a, b in zip(res, res_big):
+    assert st["batches"] >= len(queries) // 16 and st["mean_batch"] <= 16
+    for a, b in zip(res, res16):
         assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
-    _check_alone(idx, queries, np.full(len(queries), 10), res, nprobe=16)
+    _check_alone(idx, queries, ks, res, nprobe=16)
