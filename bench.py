@@ -67,6 +67,9 @@ def parse_args():
                     help="lists of the search that gives the training labels' exact top-k")
     ap.add_argument("--label-survivors", type=int, default=256,
                     help="survivors of that search (prefix ranking, exact refinement)")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--serve-seconds", type=float, default=1.5,
+                    help="arrivals per serving run (seconds of the Poisson stream)")
     return ap.parse_args()
 
 
@@ -491,6 +494,17 @@ def main():
     e2e_qps = world * B * e2e_steps / e2e_s
     e2e_recall = recall(ih.numpy().view(np.uint32), gt, k)
 
+    # ---- serving: Poisson arrivals through the continuous-batching server
+    serve = None
+    if rank == 0 and world == 1 and not args.no_serving:
+        fixed_cfg = {"nprobe": fixed99["nprobe"], "survivors": fixed99["survivors"]}
+        l99 = best(0.99, "learned")
+        learned_cfg = (dict(nprobe=l99["cap"], survivors=l99["survivors"],
+                            model=models[l99["survivors"]], threshold=l99["threshold"])
+                       if l99 else None)
+        serve = serving(katoann, idx, queries, (1000, 5000, 20000, 50000), args.serve_seconds,
+                        fixed_cfg, learned_cfg)
+
     # ---- roofline of the dominant phase
     peaks = measured_peaks()
     per_launch = {ph: v / max(passes, 1) for ph, v in phases.items()}
@@ -559,6 +573,7 @@ def main():
             "recall_0.999": {"fixed": summary(best(0.999, "fixed")),
                              "learned": summary(best(0.999, "learned"))}},
         "probe_model": learned_info,
+        "serving": serve,
         "sweep": sweep,
         "phases_ms_per_step": {k2: round(v, 4) for k2, v in per_launch.items()},
         "roofline": roofline,
@@ -582,6 +597,64 @@ def main():
         print(json.dumps(out))
     if dist:
         dist.destroy_process_group()
+
+
+def serving(katoann, idx, queries, rates, seconds, fixed, learned, seed=0):
+    """Poisson arrivals at each rate, k drawn from {10, 100} per request, served
+    by katoann.Server (continuous batching, 3 batches in flight); latency from
+    the scheduled arrival to completion. `fixed` / `learned` are the search
+    settings (learned: model, threshold, cap)."""
+    import threading
+    out = []
+    q = queries.cpu().numpy()
+    for name, cfg in (("fixed", fixed), ("learned", learned)):
+        if cfg is None:
+            continue
+        server = katoann.Server(idx, max_batch=4096, max_in_flight=3, max_k=100,
+                                nprobe=cfg["nprobe"], survivors=cfg["survivors"],
+                                budget=cfg.get("model"), threshold=cfg.get("threshold", 0.95))
+        for _ in range(2):  # warm-up: a full batch of each k
+            for r in [server.submit(q[i], k) for k in (10, 100) for i in range(len(q))]:
+                server.wait(r)
+        for rate in rates:
+            rng = np.random.default_rng(seed + int(rate))
+            n = max(2000, int(rate * seconds))
+            arrival = np.cumsum(rng.exponential(1.0 / rate, n))
+            ks = rng.choice([10, 100], n)
+            which = rng.integers(0, len(q), n)
+            rid, lag = [None] * n, np.zeros(n)
+            t0 = time.perf_counter()
+
+            def client():
+                for i in range(n):
+                    now = time.perf_counter() - t0
+                    if arrival[i] > now:
+                        time.sleep(arrival[i] - now)
+                    lag[i] = max(0.0, time.perf_counter() - t0 - arrival[i])
+                    rid[i] = server.submit(q[which[i]], int(ks[i]))
+
+            before = server.stats()
+            th = threading.Thread(target=client)
+            th.start()
+            th.join()
+            lat = np.zeros(n)
+            probes = 0
+            for i in range(n):
+                _, _, npb, ms = server.wait(rid[i])
+                lat[i] = lag[i] * 1e3 + ms
+                probes += npb
+            span = time.perf_counter() - t0
+            st = server.stats()
+            out.append({"nprobe_path": name, "rate": rate, "requests": n,
+                        "achieved_qps": round(n / span, 1),
+                        "p50_ms": round(float(np.percentile(lat, 50)), 3),
+                        "p99_ms": round(float(np.percentile(lat, 99)), 3),
+                        "batches": st["batches"] - before["batches"],
+                        "mean_batch": round(n / max(1, st["batches"] - before["batches"]), 1),
+                        "peak_in_flight": st["peak_in_flight"],
+                        "mean_nprobe": round(probes / n, 2)})
+        del server
+    return out
 
 
 def _time_oracle(o, qs, k, p, S, budget_s):
