@@ -502,7 +502,7 @@ def main():
         learned_cfg = (dict(nprobe=l99["cap"], survivors=l99["survivors"],
                             model=models[l99["survivors"]], threshold=l99["threshold"])
                        if l99 else None)
-        serve = serving(katoann, idx, queries, (1000, 5000, 20000, 50000), args.serve_seconds,
+        serve = serving(katoann, idx, queries, (1000, 5000, 20000, 100000, 400000), args.serve_seconds,
                         fixed_cfg, learned_cfg)
 
     # ---- roofline of the dominant phase
@@ -601,10 +601,10 @@ def main():
 
 def serving(katoann, idx, queries, rates, seconds, fixed, learned, seed=0):
     """Poisson arrivals at each rate, k drawn from {10, 100} per request, served
-    by katoann.Server (continuous batching, 3 batches in flight); latency from
-    the scheduled arrival to completion. `fixed` / `learned` are the search
-    settings (learned: model, threshold, cap)."""
-    import threading
+    by katoann.Server (continuous batching, 3 batches in flight) from the
+    library's native client; latency from the scheduled arrival to
+    completion. `fixed` / `learned` are the search settings (learned: model,
+    threshold, cap)."""
     out = []
     q = queries.cpu().numpy()
     for name, cfg in (("fixed", fixed), ("learned", learned)):
@@ -617,42 +617,11 @@ def serving(katoann, idx, queries, rates, seconds, fixed, learned, seed=0):
             for r in [server.submit(q[i], k) for k in (10, 100) for i in range(len(q))]:
                 server.wait(r)
         for rate in rates:
-            rng = np.random.default_rng(seed + int(rate))
             n = max(2000, int(rate * seconds))
-            arrival = np.cumsum(rng.exponential(1.0 / rate, n))
-            ks = rng.choice([10, 100], n)
-            which = rng.integers(0, len(q), n)
-            rid, lag = [None] * n, np.zeros(n)
-            t0 = time.perf_counter()
-
-            def client():
-                for i in range(n):
-                    now = time.perf_counter() - t0
-                    if arrival[i] > now:
-                        time.sleep(arrival[i] - now)
-                    lag[i] = max(0.0, time.perf_counter() - t0 - arrival[i])
-                    rid[i] = server.submit(q[which[i]], int(ks[i]))
-
-            before = server.stats()
-            th = threading.Thread(target=client)
-            th.start()
-            th.join()
-            lat = np.zeros(n)
-            probes = 0
-            for i in range(n):
-                _, _, npb, ms = server.wait(rid[i])
-                lat[i] = lag[i] * 1e3 + ms
-                probes += npb
-            span = time.perf_counter() - t0
-            st = server.stats()
+            r = server.load(q, rate, n, kmix=(10, 100), seed=seed + int(rate))
             out.append({"nprobe_path": name, "rate": rate, "requests": n,
-                        "achieved_qps": round(n / span, 1),
-                        "p50_ms": round(float(np.percentile(lat, 50)), 3),
-                        "p99_ms": round(float(np.percentile(lat, 99)), 3),
-                        "batches": st["batches"] - before["batches"],
-                        "mean_batch": round(n / max(1, st["batches"] - before["batches"]), 1),
-                        "peak_in_flight": st["peak_in_flight"],
-                        "mean_nprobe": round(probes / n, 2)})
+                        **{key: (round(v, 3) if isinstance(v, float) else v)
+                           for key, v in r.items()}})
         del server
     return out
 

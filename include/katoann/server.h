@@ -49,6 +49,27 @@ struct ServerStats {
   double mean_batch = 0;
 };
 
+struct LoadReport {
+  uint32_t requests = 0;
+  double achieved_qps = 0, p50_ms = 0, p95_ms = 0, p99_ms = 0, max_ms = 0;
+  uint64_t batches = 0;
+  double mean_batch = 0, mean_nprobe = 0;
+  uint32_t peak_in_flight = 0;
+  size_t peak_hbm_bytes = 0;
+};
+
+class Server;
+
+// A Poisson stream of n requests at `rate` per second through `server`: each
+// takes a query from `pool` (indices into queries, nq x dim; round-robin) and
+// a k drawn uniformly from kmix, and is submitted at its arrival time by a
+// native client thread. Latency runs from the scheduled arrival to
+// completion (the reference's `katoann load` measure, tools/katoann.cpp:
+// 317-327). Returns after every request is done.
+LoadReport run_load(Server &server, const float *queries, uint32_t dim,
+                    const std::vector<uint32_t> &pool, double rate, uint32_t n,
+                    const std::vector<uint32_t> &kmix, uint64_t seed);
+
 class Server {
  public:
   Server(const Index &index, const ServerOptions &opt = {});

@@ -257,6 +257,22 @@ int katoann_server_drain(void *server) {
   return guarded([&] { SV(server)->drain(); });
 }
 
+int katoann_server_load(void *server, const float *queries, uint32_t nq, uint32_t dim, double rate,
+                        uint32_t n, const uint32_t *kmix, uint32_t nk, uint64_t seed,
+                        double *report) {
+  return guarded([&] {
+    std::vector<uint32_t> pool(nq);
+    for (uint32_t i = 0; i < nq; ++i) pool[i] = i;
+    const katoann::LoadReport r = katoann::run_load(*SV(server), queries, dim, pool, rate, n,
+                                                    std::vector<uint32_t>(kmix, kmix + nk), seed);
+    const double v[10] = {r.achieved_qps, r.p50_ms,      r.p95_ms,
+                          r.p99_ms,       r.max_ms,      static_cast<double>(r.batches),
+                          r.mean_batch,   r.mean_nprobe, static_cast<double>(r.peak_in_flight),
+                          static_cast<double>(r.peak_hbm_bytes)};
+    std::copy(v, v + 10, report);
+  });
+}
+
 int katoann_server_stats(void *server, uint64_t *stats) {
   return guarded([&] {
     const katoann::ServerStats s = SV(server)->stats();

@@ -311,18 +311,6 @@ int cmd_load(const Args &a) {
   }
   const double rate = a.num("rate", 1000);
   const uint32_t n = a.u32("requests", 10000);
-  // Poisson arrivals, queries taken round-robin from the pool
-  std::mt19937_64 rng(a.u32("seed", 42));
-  std::exponential_distribution<double> gap(rate);
-  std::vector<double> arrival(n);
-  std::vector<uint32_t> which(n), kof(n);
-  double t = 0;
-  for (uint32_t i = 0; i < n; ++i) {
-    t += gap(rng);
-    arrival[i] = t;
-    which[i] = pool[i % pool.size()];
-    kof[i] = kmix[rng() % kmix.size()];
-  }
   katoann::Server server(idx, so);
   {  // warm-up: one full batch of each k
     std::vector<uint64_t> ids;
@@ -331,48 +319,18 @@ int cmd_load(const Args &a) {
         ids.push_back(server.submit(queries.data() + static_cast<size_t>(pool[w]) * d, k));
     for (uint64_t id : ids) server.wait(id);
   }
-  const katoann::ServerStats before = server.stats();
-  // the client: submits each request at its arrival time, then collects;
-  // latency runs from the scheduled arrival to completion
-  std::vector<uint64_t> rid(n);
-  std::vector<double> lag(n);
-  const auto start = Clock::now();
-  std::thread client([&] {
-    for (uint32_t i = 0; i < n; ++i) {
-      const double now = seconds_since(start);
-      if (arrival[i] > now)
-        std::this_thread::sleep_for(std::chrono::duration<double>(arrival[i] - now));
-      lag[i] = std::max(0.0, seconds_since(start) - arrival[i]);
-      rid[i] = server.submit(queries.data() + static_cast<size_t>(which[i]) * d, kof[i]);
-    }
-  });
-  client.join();
-  std::vector<double> latency(n);
-  uint64_t probes = 0;
-  for (uint32_t i = 0; i < n; ++i) {
-    const katoann::ServerResult r = server.wait(rid[i]);
-    latency[i] = lag[i] + r.latency_ms / 1e3;
-    probes += r.nprobe;
-  }
-  const double span = seconds_since(start);
-  const katoann::ServerStats st = server.stats();
-  std::vector<double> sorted = latency;
-  std::sort(sorted.begin(), sorted.end());
-  auto pct = [&](double f) {
-    const size_t r = static_cast<size_t>(std::ceil(f * sorted.size()));
-    return sorted[std::min(sorted.size() - 1, r ? r - 1 : 0)];
-  };
-  const uint64_t batches = st.batches - before.batches;
+  // Poisson arrivals, queries round-robin from the pool, k uniform over the mix
+  const katoann::LoadReport r =
+      katoann::run_load(server, queries.data(), d, pool, rate, n, kmix, a.u32("seed", 42));
   std::printf("{\"rate\": %.1f, \"requests\": %u, \"nprobe\": %u, \"engine\": \"gpu\", "
               "\"achieved_qps\": %.1f, \"p50_ms\": %.2f, \"p95_ms\": %.2f, \"p99_ms\": %.2f, "
               "\"max_ms\": %.2f, \"batches\": %llu, \"mean_batch\": %.1f, \"in_flight\": %u, "
               "\"peak_in_flight\": %u, \"peak_hbm_gb\": %.3f, \"learned\": %s, "
               "\"mean_nprobe\": %.2f}\n",
-              rate, n, so.nprobe, n / span, pct(0.50) * 1e3, pct(0.95) * 1e3, pct(0.99) * 1e3,
-              sorted.back() * 1e3, static_cast<unsigned long long>(batches),
-              batches ? static_cast<double>(n) / batches : 0.0, so.max_in_flight,
-              st.peak_in_flight, st.peak_hbm_bytes / 1e9, so.budget ? "true" : "false",
-              static_cast<double>(probes) / n);
+              rate, n, so.nprobe, r.achieved_qps, r.p50_ms, r.p95_ms, r.p99_ms, r.max_ms,
+              static_cast<unsigned long long>(r.batches), r.mean_batch, so.max_in_flight,
+              r.peak_in_flight, r.peak_hbm_bytes / 1e9, so.budget ? "true" : "false",
+              r.mean_nprobe);
   return 0;
 }
 

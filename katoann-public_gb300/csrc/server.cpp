@@ -14,6 +14,8 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cmath>
+#include <random>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
@@ -427,6 +429,64 @@ void Server::drain() {
   Impl &m = *m_;
   std::unique_lock<std::mutex> lk(m.mu);
   m.cv_done.wait(lk, [&] { return m.pending == 0 && m.in_flight == 0; });
+}
+
+LoadReport run_load(Server &server, const float *queries, uint32_t dim,
+                    const std::vector<uint32_t> &pool, double rate, uint32_t n,
+                    const std::vector<uint32_t> &kmix, uint64_t seed) {
+  if (pool.empty() || kmix.empty() || n == 0 || !(rate > 0))
+    throw std::invalid_argument("load: need queries, a k, requests and a positive rate");
+  std::mt19937_64 rng(seed);
+  std::exponential_distribution<double> gap(rate);
+  std::vector<double> arrival(n), lag(n);
+  std::vector<uint32_t> which(n), kof(n);
+  double t = 0;
+  for (uint32_t i = 0; i < n; ++i) {
+    t += gap(rng);
+    arrival[i] = t;
+    which[i] = pool[i % pool.size()];
+    kof[i] = kmix[rng() % kmix.size()];
+  }
+  const ServerStats before = server.stats();
+  std::vector<uint64_t> rid(n);
+  const auto start = Clock::now();
+  auto since = [&] { return std::chrono::duration<double>(Clock::now() - start).count(); };
+  std::thread client([&] {
+    for (uint32_t i = 0; i < n; ++i) {
+      const double now = since();
+      if (arrival[i] > now) std::this_thread::sleep_for(std::chrono::duration<double>(arrival[i] - now));
+      lag[i] = std::max(0.0, since() - arrival[i]);
+      rid[i] = server.submit(queries + static_cast<size_t>(which[i]) * dim, kof[i]);
+    }
+  });
+  client.join();
+  std::vector<double> lat(n);
+  double probes = 0;
+  for (uint32_t i = 0; i < n; ++i) {
+    const ServerResult r = server.wait(rid[i]);
+    lat[i] = lag[i] * 1e3 + r.latency_ms;
+    probes += r.nprobe;
+  }
+  const double span = since();
+  const ServerStats st = server.stats();
+  std::sort(lat.begin(), lat.end());
+  auto pct = [&](double f) {
+    const size_t r = static_cast<size_t>(std::ceil(f * lat.size()));
+    return lat[std::min(lat.size() - 1, r ? r - 1 : 0)];
+  };
+  LoadReport rep;
+  rep.requests = n;
+  rep.achieved_qps = n / span;
+  rep.p50_ms = pct(0.50);
+  rep.p95_ms = pct(0.95);
+  rep.p99_ms = pct(0.99);
+  rep.max_ms = lat.back();
+  rep.batches = st.batches - before.batches;
+  rep.mean_batch = rep.batches ? double(n) / double(rep.batches) : 0;
+  rep.mean_nprobe = probes / n;
+  rep.peak_in_flight = st.peak_in_flight;
+  rep.peak_hbm_bytes = st.peak_hbm_bytes;
+  return rep;
 }
 
 ServerStats Server::stats() const {

@@ -86,6 +86,7 @@ def _load():
     lib.katoann_server_poll.argtypes = [P, U64, P, P, P, P, P]
     lib.katoann_server_drain.argtypes = [P]
     lib.katoann_server_stats.argtypes = [P, P]
+    lib.katoann_server_load.argtypes = [P, P, U32, U32, D, U32, P, U32, U64, P]
     return lib
 
 
@@ -628,6 +629,26 @@ class Server:
 
     def drain(self) -> None:
         _check(_lib.katoann_server_drain(self._h))
+
+    def load(self, queries, rate: float, requests: int, kmix=(10,), seed: int = 42) -> dict:
+        """A Poisson stream of `requests` arrivals at `rate` per second from a
+        native client (queries round-robin, k uniform over kmix); latency
+        from the scheduled arrival to completion."""
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        if q.ndim != 2 or q.shape[1] != self.dim:
+            raise ValueError("queries must be (n, dim) float32")
+        if self.normalized:
+            q = normalize_rows(q)
+        ks = np.ascontiguousarray(kmix, dtype=np.uint32)
+        r = np.zeros(10, np.float64)
+        _check(_lib.katoann_server_load(self._h, _ptr(q), q.shape[0], q.shape[1], float(rate),
+                                        requests, _ptr(ks), ks.size, seed, _ptr(r)))
+        keys = ("achieved_qps", "p50_ms", "p95_ms", "p99_ms", "max_ms", "batches", "mean_batch",
+                "mean_nprobe", "peak_in_flight", "peak_hbm_bytes")
+        out = dict(zip(keys, map(float, r)))
+        for key in ("batches", "peak_in_flight", "peak_hbm_bytes"):
+            out[key] = int(out[key])
+        return out
 
     def stats(self) -> dict:
         s = np.zeros(5, np.uint64)
