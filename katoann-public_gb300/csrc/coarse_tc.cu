@@ -40,7 +40,7 @@ constexpr uint32_t kBTile = kQN * kBK * 2;  // 8 KiB
 constexpr uint32_t kStage = 2 * kATile + 2 * kBTile;
 constexpr uint32_t kAccCols = 4 * kQN;      // HH, HL, LH, LL
 constexpr uint32_t kTmemCols = 2 * kAccCols;
-constexpr int kEpiWarps = 8;
+constexpr int kEpiWarps = 16;  // four per TMEM lane quarter, 16 query columns each
 constexpr int kThreads = (2 + kEpiWarps) * 32;  // TMA warp, MMA warp, epilogue
 constexpr uint32_t kSmem = kStages * kStage + 2048;  // + alignment slack and barriers
 
@@ -209,34 +209,36 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     __syncwarp();
   } else {
-    // ---- epilogue: thread = centroid row (its TMEM lane), warpgroup = query half
-    const uint32_t q4 = warp & 3, half = (warp - 2) >> 2;
+    // ---- epilogue: thread = centroid row (its TMEM lane); the four warps of
+    // a lane quarter take 16 query columns each
+    const uint32_t q4 = warp & 3, part = (warp - 2) >> 2;
     const uint32_t row = q4 * 32 + lane;
     uint32_t ab = 0, abph = 0;
     for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-      const uint32_t c = (t % nct) * kCM + row, qb = (t / nct) * kQN + half * 32;
+      const uint32_t c = (t % nct) * kCM + row, qb = (t / nct) * kQN + part * 16;
       const int64_t ct = c < A.n ? A.cterm[c] : 0;
+      // lane j < 16 holds query qb + j's term; the pairs take it by shuffle
+      const int64_t qt_lane = (lane < 16 && qb + lane < A.m) ? A.qterm[qb + lane] : 0;
       if (!__all_sync(0xffffffffu, cwait(acc_full + ab, abph, err, pw[0]))) break;
       tc::fence_after();
-      const uint32_t taddr = tmem + ((q4 * 32u) << 16) + ab * kAccCols + half * 32;
-      // the group loop stays rolled (code size); the 16 columns of a group unroll
-#pragma unroll 1
-      for (uint32_t g = 0; g < 32; g += 16) {
+      const uint32_t taddr = tmem + ((q4 * 32u) << 16) + ab * kAccCols + part * 16;
+      {
         uint32_t hh[16], hl[16], lh[16], ll[16];
-        tc::tmem_ld16(taddr + 0 * kQN + g, hh);
-        tc::tmem_ld16(taddr + 1 * kQN + g, hl);
-        tc::tmem_ld16(taddr + 2 * kQN + g, lh);
-        tc::tmem_ld16(taddr + 3 * kQN + g, ll);
+        tc::tmem_ld16(taddr + 0 * kQN, hh);
+        tc::tmem_ld16(taddr + 1 * kQN, hl);
+        tc::tmem_ld16(taddr + 2 * kQN, lh);
+        tc::tmem_ld16(taddr + 3 * kQN, ll);
         tc::tmem_wait_ld();
 #pragma unroll
         for (uint32_t j = 0; j < 16; ++j) {
-          const uint32_t q = qb + g + j;
+          const uint32_t q = qb + j;
+          const int64_t qt = __shfl_sync(0xffffffffu, qt_lane, j);
           if (q >= A.m || c >= A.n) continue;
           const int64_t p = 65536ll * __float2int_rn(__uint_as_float(hh[j])) +
                             256ll * (__float2int_rn(__uint_as_float(hl[j])) +
                                      __float2int_rn(__uint_as_float(lh[j]))) +
                             __float2int_rn(__uint_as_float(ll[j]));
-          A.out[static_cast<size_t>(q) * A.n + c] = dist_value(A.qterm[q] + ct - 2 * p, A.scale);
+          A.out[static_cast<size_t>(q) * A.n + c] = dist_value(qt + ct - 2 * p, A.scale);
         }
       }
       tc::fence_before();
