@@ -523,18 +523,6 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   if (warp == kMmaWarp) tc::tmem_dealloc(tmem, S.tcols);
 }
 
-// Radix selection step shared by the seed and overflow kernels: the digit at
-// `shift` of the rank-th smallest value given its histogram; one thread.
-__device__ __forceinline__ void pick_digit(const uint32_t *hist, uint32_t rank, uint32_t *sel) {
-  uint32_t acc = 0, b = 0;
-  for (; b < 255; ++b) {
-    if (rank < acc + hist[b]) break;
-    acc += hist[b];
-  }
-  sel[0] = b;
-  sel[1] = acc;
-}
-
 // The squared L2 over the first h high bytes of a row and a query whose bytes
 // are in shared memory as words; dp4a over 16 bytes per step.
 __device__ __forceinline__ uint32_t row_dot(const uint8_t *row, const uint32_t *qw, uint32_t h) {
@@ -639,7 +627,7 @@ __global__ void __launch_bounds__(256) rank_seed_kernel(
     uint32_t want, int32_t *__restrict__ bound) {
   __shared__ int32_t l2s[kSeedCap];
   __shared__ uint32_t qw[2048 / 4];
-  __shared__ uint32_t hist[256], sel[2];
+  __shared__ uint32_t hist[256], sel[2], wsum[8];
   const uint32_t q = blockIdx.x, tid = threadIdx.x;
   for (uint32_t i = tid; i < h / 4; i += blockDim.x)
     qw[i] = reinterpret_cast<const uint32_t *>(qhi + static_cast<size_t>(q) * dc)[i];
@@ -670,8 +658,7 @@ __global__ void __launch_bounds__(256) rank_seed_kernel(
       if ((v & hm) == prefix) atomicAdd(&hist[(v >> shift) & 0xFFu], 1u);
     }
     __syncthreads();
-    if (tid == 0) pick_digit(hist, rank, sel);
-    __syncthreads();
+    block_pick_digit(hist, rank, sel, wsum);
     rank -= sel[1];
     prefix |= sel[0] << shift;
     __syncthreads();
@@ -705,6 +692,7 @@ constexpr int kRescanRounds = 2;
 template <typename KeyAt>
 __device__ unsigned long long block_select64(uint32_t n, uint32_t rank, KeyAt key, uint32_t *hist,
                                              uint32_t *sel) {
+  __shared__ uint32_t wsum[8];
   unsigned long long prefix = 0;
   for (int shift = 56; shift >= 0; shift -= 8) {
     for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x) hist[i] = 0;
@@ -715,8 +703,7 @@ __device__ unsigned long long block_select64(uint32_t n, uint32_t rank, KeyAt ke
       if ((k & hm) == prefix) atomicAdd(&hist[(k >> shift) & 0xFFu], 1u);
     }
     __syncthreads();
-    if (threadIdx.x == 0) pick_digit(hist, rank, sel);
-    __syncthreads();
+    block_pick_digit(hist, rank, sel, wsum);
     rank -= sel[1];
     prefix |= static_cast<unsigned long long>(sel[0]) << shift;
     __syncthreads();

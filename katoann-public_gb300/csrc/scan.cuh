@@ -58,4 +58,34 @@ __device__ uint2 block_scan2(uint32_t n, Val val, Out out) {
   return carry;
 }
 
+// Radix-selection step by a whole CTA (blockDim.x >= 256, whole warps): the
+// bin of a 256-bin histogram that holds the rank-th smallest value (rank <
+// the histogram's total), into sel[0], and the count below that bin, into
+// sel[1]. Thread t owns bin t; warp scans and the 8 warp totals (wsum) give
+// each bin's exclusive prefix, and the one bin whose range holds the rank
+// writes. Contains barriers: every thread of the CTA calls it.
+__device__ __forceinline__ void block_pick_digit(const uint32_t *hist, uint32_t rank, uint32_t *sel,
+                                                 uint32_t *wsum) {
+  const uint32_t t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const uint32_t h = t < 256 ? hist[t] : 0u;
+  uint32_t incl = h;
+#pragma unroll
+  for (uint32_t o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (t < 256 && lane == 31) wsum[w] = incl;
+  __syncthreads();
+  if (t < 256) {
+    uint32_t base = 0;
+    for (uint32_t i = 0; i < w; ++i) base += wsum[i];
+    const uint32_t excl = base + incl - h;
+    if (rank >= excl && rank < excl + h) {
+      sel[0] = t;
+      sel[1] = excl;
+    }
+  }
+  __syncthreads();
+}
+
 }  // namespace kato

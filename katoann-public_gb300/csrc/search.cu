@@ -325,7 +325,7 @@ __global__ void __launch_bounds__(kThreads) rank_kernel(RankArgs A) {
 // first of the key, then of the id among the entries tied at the boundary key.
 template <class KeyF, class IdF>
 __device__ uint32_t block_select(uint32_t n, uint32_t p, KeyF K, IdF I, unsigned long long *sel,
-                                 uint32_t *pos, uint32_t *hist, uint32_t *scratch,
+                                 uint32_t *pos, uint32_t *hist, uint32_t *scratch, uint32_t *wsum,
                                  bool *boundary_tie) {
   const uint32_t tid = threadIdx.x, nt = blockDim.x;
   // count non-empty
@@ -355,16 +355,7 @@ __device__ uint32_t block_select(uint32_t n, uint32_t p, KeyF K, IdF I, unsigned
         if (k != kEmpty && (k & hm) == prefix) atomicAdd(&hist[(k >> shift) & 0xFFu], 1u);
       }
       __syncthreads();
-      if (tid == 0) {
-        uint32_t acc = 0, b = 0;
-        for (; b < 256; ++b) {
-          if (rank < acc + hist[b]) break;
-          acc += hist[b];
-        }
-        scratch[1] = b;
-        scratch[2] = acc;
-      }
-      __syncthreads();
+      block_pick_digit(hist, rank, scratch + 1, wsum);
       rank -= scratch[2];
       prefix |= scratch[1] << shift;
       __syncthreads();
@@ -393,16 +384,7 @@ __device__ uint32_t block_select(uint32_t n, uint32_t p, KeyF K, IdF I, unsigned
           if ((id & hm) == ip) atomicAdd(&hist[(id >> shift) & 0xFFu], 1u);
         }
         __syncthreads();
-        if (tid == 0) {
-          uint32_t acc = 0, b = 0;
-          for (; b < 256; ++b) {
-            if (ir < acc + hist[b]) break;
-            acc += hist[b];
-          }
-          scratch[1] = b;
-          scratch[2] = acc;
-        }
-        __syncthreads();
+        block_pick_digit(hist, ir, scratch + 1, wsum);
         ir -= scratch[2];
         ip |= scratch[1] << shift;
         __syncthreads();
@@ -477,7 +459,7 @@ __global__ void __launch_bounds__(kThreads) merge_kernel(
     uint32_t *__restrict__ out_ids, float *__restrict__ out_dists,
     unsigned long long *__restrict__ tie_count) {
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ uint32_t hist[256], scratch[8];
+  __shared__ uint32_t hist[256], scratch[8], wsum[8];
   __shared__ bool tie;
   unsigned long long *sel = reinterpret_cast<unsigned long long *>(smem);
   uint32_t np2 = 1;
@@ -493,7 +475,7 @@ __global__ void __launch_bounds__(kThreads) merge_kernel(
                                : per_query;
   auto K = [&](uint32_t i) { return e[i].x; };
   auto I = [&](uint32_t i) { return ids[e[i].y]; };
-  const uint32_t got = block_select(n, S, K, I, sel, pos, hist, scratch, &tie);
+  const uint32_t got = block_select(n, S, K, I, sel, pos, hist, scratch, wsum, &tie);
   if (threadIdx.x == 0 && tie && tie_count) atomicAdd(tie_count, 1ull);
   block_sort_pairs(sel, pos, got);
   if (final_topk) {
@@ -530,46 +512,142 @@ __global__ void __launch_bounds__(kThreads) refine_kernel(
     uint32_t *__restrict__ out_ids, float *__restrict__ out_dists) {
   extern __shared__ __align__(16) unsigned char smem[];
   const uint32_t q = blockIdx.x, ns = nsurv[q];
-  uint32_t *sq = reinterpret_cast<uint32_t *>(smem);  // [2][dc/4]
-  float *ex = reinterpret_cast<float *>(sq + dc / 2);  // [S]
+  const uint32_t n16 = dc / 16;                        // 16-byte words of a plane row
+  uint4 *sq = reinterpret_cast<uint4 *>(smem);         // [2][n16]
+  float *ex = reinterpret_cast<float *>(sq + 2 * n16);  // [S]
   uint32_t *eid = reinterpret_cast<uint32_t *>(ex + S);  // [S]
   float *hd = reinterpret_cast<float *>(eid + S);      // [k]
   uint32_t *hid = reinterpret_cast<uint32_t *>(hd + k);  // [k]
-  const uint32_t nw = dc / 4;
-  for (uint32_t i = threadIdx.x; i < nw; i += blockDim.x) {
-    sq[i] = reinterpret_cast<const uint32_t *>(qhi + static_cast<size_t>(q) * dc)[i];
-    sq[nw + i] = reinterpret_cast<const uint32_t *>(qlo + static_cast<size_t>(q) * dc)[i];
+  for (uint32_t i = threadIdx.x; i < n16; i += blockDim.x) {
+    sq[i] = reinterpret_cast<const uint4 *>(qhi + static_cast<size_t>(q) * dc)[i];
+    sq[n16 + i] = reinterpret_cast<const uint4 *>(qlo + static_cast<size_t>(q) * dc)[i];
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t nwarps = blockDim.x / 32;
   const int64_t qn = qnorm[q];
-  for (uint32_t s = warp; s < ns; s += blockDim.x / 32) {
-    const uint2 v = surv[static_cast<size_t>(q) * S + s];
-    const uint32_t row = v.y, id = ids[row];
-    const uint32_t *xh = reinterpret_cast<const uint32_t *>(xhi + static_cast<size_t>(row) * dc);
-    const uint32_t *xl = reinterpret_cast<const uint32_t *>(xlo + static_cast<size_t>(row) * dc);
-    uint32_t hh = 0, mx = 0, ll = 0;
-    for (uint32_t u = lane; u < nw; u += 32) {
-      const uint32_t ah = sq[u], al = sq[nw + u], bh = xh[u], bl = xl[u];
-      hh = dp4(ah, bh, hh);
-      mx = dp4(ah, bl, mx);
-      mx = dp4(al, bh, mx);
-      ll = dp4(al, bl, ll);
+  // two survivors per warp step, every row load issued before the products
+  for (uint32_t s0 = warp; s0 < ns; s0 += 2 * nwarps) {
+    const uint32_t s1 = s0 + nwarps;
+    const bool two = s1 < ns;
+    const uint32_t r0 = surv[static_cast<size_t>(q) * S + s0].y;
+    const uint32_t r1 = two ? surv[static_cast<size_t>(q) * S + s1].y : r0;
+    uint32_t id0 = 0, id1 = 0;
+    int64_t xn0 = 0, xn1 = 0;
+    if (lane == 0) {
+      id0 = ids[r0];
+      xn0 = xnorm[r0];
+      id1 = ids[r1];
+      xn1 = xnorm[r1];
+    }
+    const uint4 *h0 = reinterpret_cast<const uint4 *>(xhi + static_cast<size_t>(r0) * dc);
+    const uint4 *l0 = reinterpret_cast<const uint4 *>(xlo + static_cast<size_t>(r0) * dc);
+    const uint4 *h1 = reinterpret_cast<const uint4 *>(xhi + static_cast<size_t>(r1) * dc);
+    const uint4 *l1 = reinterpret_cast<const uint4 *>(xlo + static_cast<size_t>(r1) * dc);
+    uint32_t hh0 = 0, mx0 = 0, ll0 = 0, hh1 = 0, mx1 = 0, ll1 = 0;
+#pragma unroll 2
+    for (uint32_t u = lane; u < n16; u += 32) {
+      const uint4 bh0 = h0[u], bl0 = l0[u];
+      uint4 bh1 = make_uint4(0, 0, 0, 0), bl1 = bh1;
+      if (two) {
+        bh1 = h1[u];
+        bl1 = l1[u];
+      }
+      const uint4 ah = sq[u], al = sq[n16 + u];
+      const uint32_t a_h[4] = {ah.x, ah.y, ah.z, ah.w}, a_l[4] = {al.x, al.y, al.z, al.w};
+      const uint32_t b_h0[4] = {bh0.x, bh0.y, bh0.z, bh0.w}, b_l0[4] = {bl0.x, bl0.y, bl0.z, bl0.w};
+      const uint32_t b_h1[4] = {bh1.x, bh1.y, bh1.z, bh1.w}, b_l1[4] = {bl1.x, bl1.y, bl1.z, bl1.w};
+#pragma unroll
+      for (int w = 0; w < 4; ++w) {
+        hh0 = dp4(a_h[w], b_h0[w], hh0);
+        mx0 = dp4(a_h[w], b_l0[w], mx0);
+        mx0 = dp4(a_l[w], b_h0[w], mx0);
+        ll0 = dp4(a_l[w], b_l0[w], ll0);
+        hh1 = dp4(a_h[w], b_h1[w], hh1);
+        mx1 = dp4(a_h[w], b_l1[w], mx1);
+        mx1 = dp4(a_l[w], b_h1[w], mx1);
+        ll1 = dp4(a_l[w], b_l1[w], ll1);
+      }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      hh += __shfl_xor_sync(0xffffffffu, hh, o);
-      mx += __shfl_xor_sync(0xffffffffu, mx, o);
-      ll += __shfl_xor_sync(0xffffffffu, ll, o);
+      hh0 += __shfl_xor_sync(0xffffffffu, hh0, o);
+      mx0 += __shfl_xor_sync(0xffffffffu, mx0, o);
+      ll0 += __shfl_xor_sync(0xffffffffu, ll0, o);
+      hh1 += __shfl_xor_sync(0xffffffffu, hh1, o);
+      mx1 += __shfl_xor_sync(0xffffffffu, mx1, o);
+      ll1 += __shfl_xor_sync(0xffffffffu, ll1, o);
     }
     if (lane == 0) {
-      const int64_t dot = static_cast<int64_t>((static_cast<uint64_t>(hh) << 16) +
-                                               (static_cast<uint64_t>(mx) << 8) + ll);
-      ex[s] = dist_value(qn + xnorm[row] - 2 * dot, scale);
-      eid[s] = id;
+      const int64_t dot0 = static_cast<int64_t>((static_cast<uint64_t>(hh0) << 16) +
+                                                (static_cast<uint64_t>(mx0) << 8) + ll0);
+      ex[s0] = dist_value(qn + xn0 - 2 * dot0, scale);
+      eid[s0] = id0;
+      if (two) {
+        const int64_t dot1 = static_cast<int64_t>((static_cast<uint64_t>(hh1) << 16) +
+                                                  (static_cast<uint64_t>(mx1) << 8) + ll1);
+        ex[s1] = dist_value(qn + xn1 - 2 * dot1, scale);
+        eid[s1] = id1;
+      }
     }
   }
   __syncthreads();
+  // The reference's heap (:1113-1124), survivors in the given order: the
+  // first k enter; a later one replaces the largest (distance, id) when its
+  // distance is strictly smaller; then ascending by (distance, id).
+  if (k <= 32) {
+    // one warp: lane i holds heap slot i
+    if (warp != 0) return;
+    float d = 3.402823466e+38f;
+    uint32_t id = 0xFFFFFFFFu, n = 0;
+    for (uint32_t s = 0; s < ns; ++s) {
+      const float dd = ex[s];
+      const uint32_t ii = eid[s];
+      if (ii >= npts) continue;  // ids without a row are skipped (:1091-1094)
+      if (n < k) {
+        if (lane == static_cast<int>(n)) {
+          d = dd;
+          id = ii;
+        }
+        ++n;
+        continue;
+      }
+      // the largest (distance, id) of the k slots
+      float md = lane < static_cast<int>(k) ? d : -1.0f;
+      uint32_t mid = lane < static_cast<int>(k) ? id : 0u;
+      int ml = lane;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float od = __shfl_xor_sync(0xffffffffu, md, o);
+        const uint32_t oid = __shfl_xor_sync(0xffffffffu, mid, o);
+        const int ol = __shfl_xor_sync(0xffffffffu, ml, o);
+        if (od > md || (od == md && oid > mid)) {
+          md = od;
+          mid = oid;
+          ml = ol;
+        }
+      }
+      if (dd < md && lane == ml) {
+        d = dd;
+        id = ii;
+      }
+    }
+    // rank of each slot among the n filled ones (ids are distinct)
+    uint32_t r = 0;
+    for (uint32_t j = 0; j < n; ++j) {
+      const float od = __shfl_sync(0xffffffffu, d, j);
+      const uint32_t oid = __shfl_sync(0xffffffffu, id, j);
+      r += (od < d || (od == d && oid < id)) ? 1u : 0u;
+    }
+    if (lane < static_cast<int>(n)) {
+      out_ids[static_cast<size_t>(q) * k + r] = id;
+      out_dists[static_cast<size_t>(q) * k + r] = d;
+    } else if (lane < static_cast<int>(k)) {
+      out_ids[static_cast<size_t>(q) * k + lane] = 0xFFFFFFFFu;
+      out_dists[static_cast<size_t>(q) * k + lane] = 3.402823466e+38f;
+    }
+    return;
+  }
   if (threadIdx.x == 0) {
     uint32_t n = 0;
     for (uint32_t s = 0; s < ns; ++s) {
