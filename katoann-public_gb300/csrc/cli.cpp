@@ -14,6 +14,8 @@
 //                  [--nprobe 64] [--max-batch 4096] [--seed 42] [--k-mix 10,100]
 //                  [--in-flight 3] [--hbm-budget-gb G] [--max-wait-ms 0]
 //                  [--budget MODEL.kprb --threshold 0.95] and the search flags
+//   katoann budget --index PREFIX --queries TRAIN.fbin --out MODEL.kprb [--ladder ...]
+//                  [--depth 256] [--label-nprobe N] [--epochs 24] and the search flags
 //
 // `load` serves requests that arrive as a Poisson process (tools/katoann.cpp:
 // 263-337), here through the continuous-batching katoann::Server: arrivals are
@@ -282,6 +284,46 @@ int cmd_search(const Args &a) {
   return 0;
 }
 
+// The learned probe budget for `load --budget`: labels the training queries by
+// searching the index and trains the model on the GPU (katoann::ProbeModel).
+int cmd_budget(const Args &a) {
+  set_threads(a);
+  katoann::Index idx;
+  idx.load(a.need("index"), load_options(a));
+  uint32_t nq = 0;
+  const std::vector<float> queries = load_queries(a, idx, nq);
+  const katoann::SearchParams sp = search_params(a);
+  katoann::ProbeTrainOptions o;
+  if (!a.get("ladder").empty()) o.ladder = u32_list(a.get("ladder"));
+  o.depth = a.u32("depth", std::min(256u, idx.nlist()));
+  o.k = sp.k;
+  o.label_nprobe = a.u32("label-nprobe", 0);
+  if (a.get("label-ranking", "full") == "prefix") o.label_ranking = katoann::Ranking::kPrefix;
+  else if (a.get("label-ranking", "full") == "high") o.label_ranking = katoann::Ranking::kHighBytes;
+  o.label_survivors = a.u32("label-survivors", 0);
+  o.ranking = sp.ranking;
+  o.survivors = sp.survivors;
+  o.epochs = a.u32("epochs", 24);
+  o.batch = a.u32("train-batch", 1024);
+  o.seed = std::stoull(a.get("seed", "0"));
+  std::vector<uint32_t> ladder;
+  for (uint32_t v : o.ladder)
+    if (v <= idx.nlist()) ladder.push_back(v);
+  o.ladder = ladder;
+  const auto t0 = Clock::now();
+  const katoann::ProbeModel m = katoann::ProbeModel::train(idx, queries.data(), nq, o);
+  m.save(a.need("out"));
+  std::vector<uint64_t> hist(m.classes(), 0);
+  for (uint8_t l : m.labels()) ++hist[l];
+  std::printf("{\"queries\": %u, \"classes\": %u, \"depth\": %u, \"train_s\": %.2f, "
+              "\"loss_first\": %.4f, \"loss_last\": %.4f, \"label_histogram\": [",
+              nq, m.classes(), m.depth(), seconds_since(t0), m.loss().front(), m.loss().back());
+  for (size_t i = 0; i < hist.size(); ++i)
+    std::printf("%s%llu", i ? ", " : "", static_cast<unsigned long long>(hist[i]));
+  std::printf("]}\n");
+  return 0;
+}
+
 int cmd_load(const Args &a) {
   set_threads(a);
   katoann::Index idx;
@@ -347,7 +389,11 @@ void usage() {
                "       katoann load   --index PREFIX --queries Q.fbin --rate QPS [--requests 10000]\n"
                "                      [--nprobe 64] [--max-batch 4096] [--seed 42] [--k-mix 10,100]\n"
                "                      [--in-flight 3] [--hbm-budget-gb G] [--max-wait-ms 0]\n"
-               "                      [--budget MODEL.kprb --threshold 0.95] and the search flags\n");
+               "                      [--budget MODEL.kprb --threshold 0.95] and the search flags\n"
+               "       katoann budget --index PREFIX --queries TRAIN.fbin --out MODEL.kprb\n"
+               "                      [--ladder 8,16,...] [--depth 256] [--label-nprobe N]\n"
+               "                      [--label-ranking full|prefix] [--label-survivors S]\n"
+               "                      [--epochs 24] [--train-batch 1024] and the search flags\n");
 }
 
 }  // namespace
@@ -363,6 +409,7 @@ int main(int argc, char **argv) {
     if (cmd == "build") return cmd_build(a);
     if (cmd == "search") return cmd_search(a);
     if (cmd == "load") return cmd_load(a);
+    if (cmd == "budget") return cmd_budget(a);
     usage();
     return 2;
   } catch (const std::exception &e) {

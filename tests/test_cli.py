@@ -127,10 +127,14 @@ def test_load_serves_mixed_k_with_a_learned_budget(tmp_path):
     write_fbin(tmp_path / "q.fbin", queries)
     idx = katoann.Index()
     idx.load(prefix)
-    train = synth.to_f32(synth.mixture_ints(33, 30, 1500, 64, 8))
-    model = katoann.ProbeModel.train(idx, train, ladder=(2, 4, 8, 16, 32), depth=32,
-                                     label_nprobe=48, survivors=32, epochs=5, batch=256)
-    model.save(str(tmp_path / "m.kprb"))
+    write_fbin(tmp_path / "train.fbin", synth.to_f32(synth.mixture_ints(33, 30, 1500, 64, 8)))
+    b = run("budget", "--index", prefix, "--queries", str(tmp_path / "train.fbin"), "--out",
+            str(tmp_path / "m.kprb"), "--ladder", "2,4,8,16,32", "--depth", "32",
+            "--label-nprobe", "48", "--survivors", "32", "--epochs", "5", "--train-batch", "256")
+    info = json_lines(b.stdout)[-1]
+    assert info["queries"] == 1500 and info["classes"] == 5 and sum(info["label_histogram"]) == 1500
+    model = katoann.ProbeModel.load(str(tmp_path / "m.kprb"))
+    assert list(model.ladder) == [2, 4, 8, 16, 32] and model.depth == 32
     p = run("load", "--index", prefix, "--queries", str(tmp_path / "q.fbin"), "--rate", "20000",
             "--requests", "2000", "--nprobe", "32", "--k-mix", "10,100", "--in-flight", "2",
             "--budget", str(tmp_path / "m.kprb"), "--threshold", "0.9")
