@@ -154,6 +154,16 @@ class Index {
   std::vector<uint32_t> list_sizes() const;
   size_t memory_bytes() const;
 
+  // The autotuner (no counterpart in the reference): times a search of these
+  // queries (host; the first max_batch of them) with `p` under every
+  // candidate setting of the ranking pass's knobs and keeps the fastest for
+  // the process (katoann_gpu_autotune). Results never depend on the knobs.
+  struct Tuning {
+    uint32_t seed_rows, schedule, width;
+    double us_per_search;
+  };
+  Tuning autotune(const float *queries, uint32_t nq, const SearchParams &p);
+
   // Diagnostics of the last search: coarse boundary ties, survivor boundary
   // ties, queries (see katoann_gpu_workspace_stats).
   std::vector<uint64_t> last_search_stats() const;

@@ -84,6 +84,12 @@ int katoann_index_search_device_budget(void *index, const float *d_queries, uint
                                        uint32_t *d_nprobe_out, uint32_t *d_ids, float *d_dists,
                                        void *stream, void *timer, int graph);
 
+/* Index::autotune: out[4] = {seed rows, split weight, item width,
+ * microseconds per search}; model NULL: fixed nprobe. */
+int katoann_index_autotune(void *index, const float *queries, uint32_t nq, uint32_t k,
+                           uint32_t nprobe, int ranking, uint32_t survivors, const void *model,
+                           float threshold, uint32_t *out);
+
 /* ------------------------------------------------ learned probe budget
  * katoann::ProbeModel (include/katoann/probe.h). train: labels nq queries by
  * searching the index and trains on the device; options as in

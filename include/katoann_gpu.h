@@ -197,6 +197,16 @@ int katoann_gpu_set_candidate_cap(uint32_t cap);
  * a looser one less work up front. Results do not depend on it. */
 int katoann_gpu_set_seed_rows(uint32_t rows);
 
+/* Knobs of the tensor-core ranking pass (process-wide; results never depend
+ * on them): the largest work-item width (0 = by the prefix width, else 16,
+ * 32 or 64 queries) and the cost weight of the split of tiles over the
+ * persistent CTAs (0 = equal tile counts; 1 to 8 = a tile of an item of MMA
+ * width w costs 64 + beta w, and the CTAs take equal cost). */
+int katoann_gpu_set_rank_width(uint32_t width);
+int katoann_gpu_set_rank_schedule(uint32_t beta);
+/* The current knobs: h_out[3] = {seed rows (0 = default), split weight, item width}. */
+void katoann_gpu_rank_knobs(uint32_t *h_out);
+
 /* katoann_gpu_search that also records phase events into `timer` (may be
  * NULL, then identical to katoann_gpu_search). */
 int katoann_gpu_search_timed(const katoann_gpu_index *index, const float *d_queries, uint32_t nq,
@@ -352,6 +362,17 @@ int katoann_gpu_probe_train(const float *d_z, const uint8_t *d_label, uint32_t n
 int katoann_gpu_probe_grads(const katoann_gpu_probe_model *model, const float *d_z,
                             const uint8_t *d_label, uint32_t n, float *h_loss, float *d_gw1,
                             float *d_gb1, float *d_gw2, float *d_gb2, float *d_gw3, float *d_gb3);
+
+/* The autotuner: times one search of these queries (the workspace sized for
+ * it) under every candidate setting - seed rows {512, 1024, 2048}, split
+ * weight {0, 1, 2, 4}, item width {default, 32} - and keeps the fastest
+ * (settings that need a larger workspace are skipped). h_out[4] = {seed
+ * rows, split weight, item width, microseconds per search}. Synchronous. */
+int katoann_gpu_autotune(const katoann_gpu_index *index, const float *d_queries, uint32_t nq,
+                         uint32_t k, uint32_t nprobe, int ranking, uint32_t survivors,
+                         uint32_t max_batch, const uint32_t *d_nprobe_in,
+                         const katoann_gpu_probe_model *model, void *d_ws, size_t ws_bytes,
+                         katoann_stream_t stream, uint32_t *h_out);
 
 #ifdef __cplusplus
 }

@@ -9,6 +9,7 @@
 
 #include "kcommon.cuh"
 #include "probe.cuh"
+#include "rank_tc.cuh"
 
 namespace kato {
 
@@ -43,6 +44,9 @@ int search(const katoann_gpu_index *ix, const float *queries, uint32_t nq, uint3
 int probe_features_search(const katoann_gpu_index *ix, const float *queries, uint32_t nq,
                           const uint32_t *rank, uint32_t depth, uint32_t max_batch, void *ws,
                           size_t ws_bytes, float *z, cudaStream_t st);
+int autotune(const katoann_gpu_index *ix, const float *queries, uint32_t nq, uint32_t k, uint32_t p,
+             int ranking, uint32_t survivors, uint32_t max_batch, const Budget &budget, void *ws,
+             size_t ws_bytes, cudaStream_t st, uint32_t *out);
 int search_capture(const katoann_gpu_index *ix, const float *queries, uint32_t nq, uint32_t k,
                    uint32_t p, int ranking, uint32_t survivors, uint32_t max_batch, void *ws,
                    size_t ws_bytes, uint32_t *out_ids, float *out_dists, const Budget &budget,
@@ -199,6 +203,42 @@ int katoann_gpu_search_budget(const katoann_gpu_index *ix, const float *d_querie
   b.nprobe_out = d_nprobe_out;
   return kato::search(ix, d_queries, nq, k, nprobe, ranking, survivors, max_batch, d_ws, ws_bytes,
                       d_ids, d_dists, b, as_stream(stream), timer);
+}
+
+int katoann_gpu_set_rank_width(uint32_t width) {
+  if (width != 0 && width != 16 && width != 32 && width != 64)
+    return kato::invalid("rank width must be 0, 16, 32 or 64");
+  kato::g_tc_width = width;
+  return KATO_OK;
+}
+
+void katoann_gpu_rank_knobs(uint32_t *h_out) {
+  h_out[0] = kato::g_seed_rows.load();
+  h_out[1] = kato::g_tc_beta.load();
+  h_out[2] = kato::g_tc_width.load();
+}
+
+int katoann_gpu_set_rank_schedule(uint32_t beta) {
+  if (beta > 8) return kato::invalid("rank schedule weight must be at most 8");
+  kato::g_tc_beta = beta;
+  return KATO_OK;
+}
+
+int katoann_gpu_autotune(const katoann_gpu_index *ix, const float *d_queries, uint32_t nq,
+                         uint32_t k, uint32_t nprobe, int ranking, uint32_t survivors,
+                         uint32_t max_batch, const uint32_t *d_nprobe_in,
+                         const katoann_gpu_probe_model *model, void *d_ws, size_t ws_bytes,
+                         katoann_stream_t stream, uint32_t *h_out) {
+  if (!ix || !h_out) return kato::invalid("null index or output");
+  if (ix->nlist == 0) {
+    kato::set_error("autotune before load");
+    return KATO_ELOGIC;
+  }
+  kato::Budget b;
+  b.nprobe_in = d_nprobe_in;
+  b.model = d_nprobe_in ? nullptr : model;
+  return kato::autotune(ix, d_queries, nq, k, nprobe, ranking, survivors, max_batch, b, d_ws,
+                        ws_bytes, as_stream(stream), h_out);
 }
 
 int katoann_gpu_search_capture(const katoann_gpu_index *ix, const float *d_queries, uint32_t nq,

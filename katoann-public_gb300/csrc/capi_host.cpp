@@ -315,6 +315,21 @@ int katoann_index_search_device_budget(void *index, const float *d_queries, uint
   });
 }
 
+int katoann_index_autotune(void *index, const float *queries, uint32_t nq, uint32_t k,
+                           uint32_t nprobe, int ranking, uint32_t survivors, const void *model,
+                           float threshold, uint32_t *out) {
+  return guarded([&] {
+    katoann::SearchParams p = params(k, nprobe, ranking, survivors, 0);
+    p.budget = M(model);
+    p.budget_threshold = threshold;
+    const katoann::Index::Tuning t = I(index)->autotune(queries, nq, p);
+    out[0] = t.seed_rows;
+    out[1] = t.schedule;
+    out[2] = t.width;
+    out[3] = static_cast<uint32_t>(t.us_per_search);
+  });
+}
+
 int katoann_probe_train(void *index, const float *queries, uint32_t nq, const uint32_t *ladder,
                         uint32_t nladder, uint32_t depth, uint32_t k, uint32_t label_nprobe,
                         int label_ranking, uint32_t label_survivors, int ranking,

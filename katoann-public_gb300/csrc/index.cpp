@@ -700,6 +700,37 @@ void Index::search_device(const float *d_queries, uint32_t nq, const SearchParam
   s.last_stream = st;
 }
 
+Index::Tuning Index::autotune(const float *queries, uint32_t nq, const SearchParams &p) {
+  if (nq == 0) throw std::invalid_argument("autotune needs queries");
+  validate(s_.get(), s_ ? s_->nlist : 0, s_ ? s_->head : 0, p);
+  State &s = *s_;
+  const BudgetPlan bp = budget_plan(p, s.nlist);
+  std::lock_guard<std::mutex> lock(s.mu);
+  const uint32_t b = std::min(nq, s.max_batch);
+  const int rk = ranking_code(p.ranking);
+  // room for every candidate item width
+  uint32_t knobs[3];
+  katoann_gpu_rank_knobs(knobs);
+  size_t need = 0;
+  for (uint32_t w : {0u, 32u}) {
+    gpu_check(katoann_gpu_set_rank_width(w));
+    need = std::max(need, katoann_gpu_search_workspace(&s.view, b, p.k, bp.depth, rk, p.survivors));
+  }
+  gpu_check(katoann_gpu_set_rank_width(knobs[2]));
+  if (need == 0) gpu_check(KATO_EINVAL);
+  cuda_check(cudaStreamSynchronize(s.stream), "autotune");
+  s.drop_graphs();
+  s.ws.ensure(need);
+  s.dq.ensure(static_cast<size_t>(b) * s.dim * 4);
+  cuda_check(cudaMemcpy(s.dq.p, queries, static_cast<size_t>(b) * s.dim * 4, cudaMemcpyHostToDevice),
+             "copy queries");
+  uint32_t out[4] = {0, 0, 0, 0};
+  gpu_check(katoann_gpu_autotune(&s.view, s.dq.as<float>(), b, p.k, p.nprobe, rk, p.survivors, b,
+                                 nullptr, bp.use_model ? &bp.model : nullptr, s.ws.p, s.ws.n,
+                                 reinterpret_cast<katoann_stream_t>(s.stream), out));
+  return Tuning{out[0], out[1], out[2], static_cast<double>(out[3])};
+}
+
 std::vector<uint64_t> Index::last_search_stats() const {
   std::vector<uint64_t> out(39, 0);
   if (!s_ || !s_->ws.p) return out;

@@ -191,8 +191,28 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const uint32_t acol = kTcAStages * N;  // TMEM columns of the A stages follow the accumulators
   const uint32_t nitems = *A.nitems;
   const uint32_t T = nitems ? A.tile_off[nitems] : 0;
-  const uint32_t t0 = static_cast<uint32_t>(static_cast<uint64_t>(T) * blockIdx.x / gridDim.x);
-  const uint32_t t1 = static_cast<uint32_t>(static_cast<uint64_t>(T) * (blockIdx.x + 1) / gridDim.x);
+  uint32_t t0, t1;
+  if (A.cost_off && nitems) {
+    // an equal share of the cost; cost unit c lies in tile tile_at(c)
+    const uint32_t C = A.cost_off[nitems];
+    auto tile_at = [&](uint32_t c) -> uint32_t {
+      if (c >= C) return T;
+      uint32_t lo = 0, hi = nitems;  // cost_off[lo] <= c < cost_off[hi]
+      while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) / 2;
+        if (A.cost_off[mid] <= c) lo = mid;
+        else hi = mid;
+      }
+      const uint32_t tiles = A.tile_off[lo + 1] - A.tile_off[lo];
+      const uint32_t per = (A.cost_off[lo + 1] - A.cost_off[lo]) / tiles;
+      return A.tile_off[lo] + (c - A.cost_off[lo]) / per;
+    };
+    t0 = tile_at(static_cast<uint32_t>(static_cast<uint64_t>(C) * blockIdx.x / gridDim.x));
+    t1 = tile_at(static_cast<uint32_t>(static_cast<uint64_t>(C) * (blockIdx.x + 1) / gridDim.x));
+  } else {
+    t0 = static_cast<uint32_t>(static_cast<uint64_t>(T) * blockIdx.x / gridDim.x);
+    t1 = static_cast<uint32_t>(static_cast<uint64_t>(T) * (blockIdx.x + 1) / gridDim.x);
+  }
   const uint32_t nkc = (h + S.inner - 1) / S.inner;
   const __half2 bias = __floats2half2_rn(1152.0f, 1152.0f);  // 1024 + 128
   // per-role cycle profile (first thread of each role): waits, then total
@@ -843,9 +863,15 @@ __global__ void __launch_bounds__(256) rescan_exact_kernel(
 // -------------------------------------------------- work items and offsets
 // Per list: items = ceil(queries / N) (none for an empty list), tiles per
 // item = ceil(rows / 128); counts[c] = items, counts[L + 1 + c] = items x tiles.
+// MMA width of an item of ne queries (host and device, as mma_width<N>).
+__host__ __device__ __forceinline__ uint32_t item_width(uint32_t ne, uint32_t N) {
+  return ne <= 16 ? 16u : (ne <= 32 && N > 32 ? 32u : N);
+}
+
 __global__ void tc_count_kernel(const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ list_off,
-                                uint32_t L, uint32_t N, uint32_t B, uint32_t *__restrict__ counts,
-                                uint32_t *__restrict__ qcount, uint32_t *__restrict__ qfill) {
+                                uint32_t L, uint32_t N, uint32_t B, uint32_t beta,
+                                uint32_t *__restrict__ counts, uint32_t *__restrict__ qcount,
+                                uint32_t *__restrict__ qfill) {
   const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c < B) {
     qcount[c] = 0;
@@ -854,31 +880,48 @@ __global__ void tc_count_kernel(const uint32_t *__restrict__ cnt, const uint32_t
   if (c >= L) return;
   const uint32_t n = list_off[c + 1] - list_off[c];
   const uint32_t items = n ? (cnt[c] + N - 1) / N : 0;
+  const uint32_t tiles = (n + kTcRows - 1) / kTcRows;
   counts[c] = items;
-  counts[L + 1 + c] = items * ((n + kTcRows - 1) / kTcRows);
+  counts[L + 1 + c] = items * tiles;
+  if (beta) {  // full items first, then the remainder
+    const uint32_t full = n ? cnt[c] / N : 0, rem = n ? cnt[c] % N : 0;
+    counts[2 * (L + 1) + c] =
+        tiles * (full * (64 + beta * N) + (rem ? 64 + beta * item_width(rem, N) : 0));
+  }
 }
 
 // Exclusive scans of the two count arrays by one CTA of 1024 threads (in
 // place); the totals go to *nitems and tile_off[*nitems].
 __global__ void __launch_bounds__(1024) tc_scan_kernel(uint32_t *__restrict__ counts, uint32_t L,
                                                        uint32_t *__restrict__ nitems,
-                                                       uint32_t *__restrict__ tile_off) {
-  uint32_t *ca = counts, *cb = counts + L + 1;
+                                                       uint32_t *__restrict__ tile_off,
+                                                       uint32_t *__restrict__ cost_off) {
+  uint32_t *ca = counts, *cb = counts + L + 1, *cc = counts + 2 * (L + 1);
   const uint2 tot = block_scan2(
       L, [&](uint32_t i) { return make_uint2(ca[i], cb[i]); },
       [&](uint32_t i, uint32_t a, uint32_t b) {
         ca[i] = a;
         cb[i] = b;
       });
+  uint32_t cost = 0;
+  if (cost_off) {
+    __syncthreads();
+    cost = block_scan2(
+               L, [&](uint32_t i) { return make_uint2(cc[i], 0u); },
+               [&](uint32_t i, uint32_t a, uint32_t) { cc[i] = a; })
+               .x;
+  }
   if (threadIdx.x == 0) {
     *nitems = tot.x;
     tile_off[tot.x] = tot.y;
+    if (cost_off) cost_off[tot.x] = cost;
   }
 }
 
 __global__ void tc_expand_kernel(const uint32_t *__restrict__ list_off, const uint32_t *__restrict__ counts,
-                                 uint32_t L, uint32_t N, const uint32_t *__restrict__ nitems,
-                                 TcItem *__restrict__ items, uint32_t *__restrict__ tile_off) {
+                                 uint32_t L, uint32_t N, uint32_t beta,
+                                 const uint32_t *__restrict__ nitems, TcItem *__restrict__ items,
+                                 uint32_t *__restrict__ tile_off, uint32_t *__restrict__ cost_off) {
   const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= L) return;
   const uint32_t i0 = counts[c], i1 = c + 1 < L ? counts[c + 1] : *nitems;
@@ -887,6 +930,8 @@ __global__ void tc_expand_kernel(const uint32_t *__restrict__ list_off, const ui
   for (uint32_t j = 0; j < i1 - i0; ++j) {
     items[i0 + j] = TcItem{c, j * N, list_off[c], list_off[c + 1] - list_off[c]};
     tile_off[i0 + j] = tb + j * tiles;
+    // every item before the last of its list is full (width N)
+    if (cost_off) cost_off[i0 + j] = counts[2 * (L + 1) + c] + j * tiles * (64 + beta * N);
   }
 }
 
@@ -921,10 +966,14 @@ uint32_t rank_tc_ctas() {
   return static_cast<uint32_t>(std::max(sms, 1));
 }
 
+std::atomic<uint32_t> g_tc_width{0}, g_tc_beta{0};
+
 bool rank_tc_plan(uint32_t h, uint32_t dc, TcShape *s) {
   if (h == 0 || h % 64 || h > 1024 || h > dc || dc % 64) return false;
   TcShape t{};
   t.N = h <= 256 ? 64 : (h <= 512 ? 32 : 16);
+  const uint32_t cap = g_tc_width.load();
+  if (cap >= 16 && cap < t.N) t.N = cap;
   t.inner = dc >= 128 ? 128 : 64;
   // accumulators (two slots of N columns), then the two A stages (inner / 2 columns each)
   t.tcols = 32;
@@ -1003,12 +1052,15 @@ int rank_seed(const uint8_t *xhi, const int64_t *xnorm, const uint8_t *qhi, cons
 }
 
 int rank_tc_prepare(const uint32_t *cnt, const uint32_t *list_off, uint32_t L, uint32_t N,
-                    uint32_t B, uint32_t *scratch, TcItem *items, uint32_t *tile_off,
-                    uint32_t *nitems, uint32_t *qcount, uint32_t *qfill, cudaStream_t st) {
-  tc_count_kernel<<<div_up(std::max(std::max(L, B), 1u), 256), 256, 0, st>>>(cnt, list_off, L, N, B,
-                                                                           scratch, qcount, qfill);
-  tc_scan_kernel<<<1, 1024, 0, st>>>(scratch, L, nitems, tile_off);
-  tc_expand_kernel<<<div_up(L, 256), 256, 0, st>>>(list_off, scratch, L, N, nitems, items, tile_off);
+                    uint32_t B, uint32_t beta, uint32_t *scratch, TcItem *items,
+                    uint32_t *tile_off, uint32_t *cost_off, uint32_t *nitems, uint32_t *qcount,
+                    uint32_t *qfill, cudaStream_t st) {
+  uint32_t *co = beta ? cost_off : nullptr;
+  tc_count_kernel<<<div_up(std::max(std::max(L, B), 1u), 256), 256, 0, st>>>(
+      cnt, list_off, L, N, B, beta, scratch, qcount, qfill);
+  tc_scan_kernel<<<1, 1024, 0, st>>>(scratch, L, nitems, tile_off, co);
+  tc_expand_kernel<<<div_up(L, 256), 256, 0, st>>>(list_off, scratch, L, N, beta, nitems, items,
+                                                   tile_off, co);
   KATO_LAUNCHED("ranking work preparation");
   return KATO_OK;
 }

@@ -2,6 +2,8 @@
 // search orchestration (search.cu).
 #pragma once
 
+#include <atomic>
+
 #include <cstdint>
 
 #include "kcommon.cuh"
@@ -21,6 +23,7 @@ struct RankTcArgs {
   const uint32_t *off;       // nlist + 1
   const TcItem *items;
   const uint32_t *tile_off;  // per item: first global tile; [nitems] = total tiles
+  const uint32_t *cost_off;  // per item: first cost unit; [nitems] = total (null: split by tiles)
   const uint32_t *nitems;
   const int32_t *bound;      // per query: rows with a larger l2 cannot be selected
   uint32_t *qcount;          // per query: candidates found (bit 31: some were dropped)
@@ -89,11 +92,17 @@ int rank_seed(const uint8_t *xhi, const int64_t *xnorm, const uint8_t *qhi, cons
               uint32_t B, uint32_t p,
               uint32_t dc, uint32_t h, uint32_t S, uint32_t rows, int32_t *bound, cudaStream_t st);
 // Work items of the pass (per list: groups of N queries) and their tile
-// offsets; also zeroes the B candidate counts and buffer fills. scratch:
-// 2 x (L + 1) words.
+// offsets; also zeroes the B candidate counts and buffer fills. With
+// beta > 0, also per-item cost offsets: a tile of an item of MMA width w
+// costs 64 + beta * w, and the CTAs split the cost instead of the tiles.
+// scratch: 3 x (L + 1) words.
 int rank_tc_prepare(const uint32_t *cnt, const uint32_t *list_off, uint32_t L, uint32_t N,
-                    uint32_t B, uint32_t *scratch, TcItem *items, uint32_t *tile_off,
-                    uint32_t *nitems, uint32_t *qcount, uint32_t *qfill, cudaStream_t st);
+                    uint32_t B, uint32_t beta, uint32_t *scratch, TcItem *items,
+                    uint32_t *tile_off, uint32_t *cost_off, uint32_t *nitems, uint32_t *qcount,
+                    uint32_t *qfill, cudaStream_t st);
+// Process-wide knobs of the pass (0 = default): the largest item width and
+// the cost weight of the CTA split.
+extern std::atomic<uint32_t> g_tc_width, g_tc_beta;
 // Candidate records of the pass into per-query buffers of cap entries
 // (distance bits, row); qfill counts the entries each query was offered.
 int rank_tc_bucket(const uint4 *rec, const uint32_t *rec_n, uint32_t rec_cap, uint32_t ctas,

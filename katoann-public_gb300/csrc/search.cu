@@ -730,12 +730,12 @@ struct Plan {
   bool tc;                          // tensor-core ranking pass
   bool coarse_tc;                   // tensor-core coarse product
   TcShape tcs;
-  uint32_t tcitems, cap, seed_rows, ctas, rec_cap;
+  uint32_t tcitems, cap, seed_rows, ctas, rec_cap, beta;
   size_t off_fq, off_qhi, off_qlo, off_qn, off_qhn, off_qh0, off_cd, off_probed, off_cnt, off_off,
       off_woff, off_cur, off_work, off_ent, off_slots, off_surv, off_nsurv, off_stats,
       off_tcscratch, off_tcitems, off_tileoff, off_nitems, off_qcount, off_qfill, off_bound,
       off_rec, off_recn, off_rlist, off_rkey, off_rcount, off_qh16, off_ql16, off_qterm, off_rot,
-      off_qprobes, off_z, total;
+      off_qprobes, off_z, off_costoff, total;
 };
 
 static size_t align256(size_t x) { return (x + 255) / 256 * 256; }
@@ -776,6 +776,11 @@ int make_plan(const katoann_gpu_index *ix, uint32_t B, uint32_t k, uint32_t p, i
     pl.ctas = rank_tc_ctas();
     pl.rec_cap = static_cast<uint32_t>(
         std::max<size_t>(8192, static_cast<size_t>(B) * pl.S * 32 / pl.ctas));
+    // the cost split, unless its 32-bit cost units could overflow
+    pl.beta = g_tc_beta.load();
+    const uint64_t worst = static_cast<uint64_t>(pl.tcitems) * ((ix->max_list + 127) / 128) *
+                           (64 + static_cast<uint64_t>(pl.beta) * pl.tcs.N);
+    if (worst >= (1ull << 31)) pl.beta = 0;
   } else {
     pl.ctas = 1;
     pl.rec_cap = 0;
@@ -802,7 +807,8 @@ int make_plan(const katoann_gpu_index *ix, uint32_t B, uint32_t k, uint32_t p, i
   pl.off_work = take(wmax * sizeof(Work));
   pl.off_ent = take(bp * 4);
   pl.off_slots = take((pl.tc ? static_cast<size_t>(B) * pl.cap : bp * pl.SC) * sizeof(uint2));
-  pl.off_tcscratch = take(2 * (static_cast<size_t>(L) + 1) * 4);
+  pl.off_tcscratch = take(3 * (static_cast<size_t>(L) + 1) * 4);
+  pl.off_costoff = take(pl.tc ? (static_cast<size_t>(pl.tcitems) + 1) * 4 : 16);
   pl.off_tcitems = take(pl.tc ? (static_cast<size_t>(pl.tcitems) + 1) * sizeof(TcItem) : 16);
   pl.off_tileoff = take(pl.tc ? (static_cast<size_t>(pl.tcitems) + 1) * 4 : 16);
   pl.off_nitems = take(16);
@@ -967,9 +973,10 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
                         pl.dims, pl.S, pl.seed_rows, bound, st)))
       return rc;
     mark(tm, 6, st);
-    if ((rc = rank_tc_prepare(cnt, ix->d_list_off, L, pl.tcs.N, nq,
+    uint32_t *cost_off = reinterpret_cast<uint32_t *>(ws + pl.off_costoff);
+    if ((rc = rank_tc_prepare(cnt, ix->d_list_off, L, pl.tcs.N, nq, pl.beta,
                               reinterpret_cast<uint32_t *>(ws + pl.off_tcscratch), items, tile_off,
-                              nitems, qcount, qfill, st)))
+                              cost_off, nitems, qcount, qfill, st)))
       return rc;
     RankTcArgs T{};
     T.qhi = qhi;
@@ -978,6 +985,7 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
     T.off = off;
     T.items = items;
     T.tile_off = tile_off;
+    T.cost_off = pl.beta ? cost_off : nullptr;
     T.nitems = nitems;
     T.bound = bound;
     T.qcount = qcount;
@@ -1147,6 +1155,76 @@ int probe_features_search(const katoann_gpu_index *ix, const float *queries, uin
 }
 
 uint32_t last_launches() { return g_launches; }
+
+// --------------------------------------------------------------- autotune
+// Times one search of these queries under every candidate setting of the
+// ranking pass's knobs - seed rows, CTA split weight, item width - and keeps
+// the fastest. The knobs change the work and its schedule, never a result.
+int autotune(const katoann_gpu_index *ix, const float *queries, uint32_t nq, uint32_t k, uint32_t p,
+             int ranking, uint32_t survivors, uint32_t max_batch, const Budget &budget, void *ws,
+             size_t ws_bytes, cudaStream_t st, uint32_t *out) {
+  if (nq == 0) return invalid("autotune needs queries");
+  // the batch the search runs, once: the buffers of the results
+  uint32_t *ids = nullptr;
+  float *dists = nullptr;
+  KATO_CUDA(cudaMalloc(&ids, static_cast<size_t>(nq) * k * 4));
+  const cudaError_t e2 = cudaMalloc(&dists, static_cast<size_t>(nq) * k * 4);
+  if (e2 != cudaSuccess) {
+    cudaFree(ids);
+    return cuda_status(e2, "autotune buffers");
+  }
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  const uint32_t seed0 = g_seed_rows.load(), beta0 = g_tc_beta.load(), width0 = g_tc_width.load();
+  float best = 1e30f;
+  uint32_t bs = seed0, bb = beta0, bw = width0;
+  int rc = KATO_OK;
+  for (uint32_t seed : {512u, 1024u, 2048u})
+    for (uint32_t beta : {0u, 1u, 2u, 4u})
+      for (uint32_t width : {0u, 32u}) {
+        g_seed_rows = seed;
+        g_tc_beta = beta;
+        g_tc_width = width;
+        int r = search(ix, queries, nq, k, p, ranking, survivors, max_batch, ws, ws_bytes, ids,
+                       dists, budget, st, nullptr);
+        if (r == KATO_ENOMEM) continue;  // this setting needs a larger workspace
+        if (r) {
+          rc = r;
+          break;
+        }
+        cudaEventRecord(a, st);
+        for (int rep = 0; rep < 3 && !r; ++rep)
+          r = search(ix, queries, nq, k, p, ranking, survivors, max_batch, ws, ws_bytes, ids, dists,
+                     budget, st, nullptr);
+        cudaEventRecord(b, st);
+        if (r || cudaEventSynchronize(b) != cudaSuccess) {
+          rc = r ? r : cuda_status(cudaGetLastError(), "autotune");
+          break;
+        }
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        if (ms < best) {
+          best = ms;
+          bs = seed;
+          bb = beta;
+          bw = width;
+        }
+      }
+  g_seed_rows = rc ? seed0 : bs;
+  g_tc_beta = rc ? beta0 : bb;
+  g_tc_width = rc ? width0 : bw;
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(ids);
+  cudaFree(dists);
+  if (rc) return rc;
+  out[0] = bs;
+  out[1] = bb;
+  out[2] = bw;
+  out[3] = static_cast<uint32_t>(best / 3 * 1000.0f);
+  return KATO_OK;
+}
 
 // ------------------------------------------------------------ CUDA graphs
 struct SearchGraph {

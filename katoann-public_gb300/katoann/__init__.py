@@ -87,6 +87,7 @@ def _load():
     lib.katoann_server_drain.argtypes = [P]
     lib.katoann_server_stats.argtypes = [P, P]
     lib.katoann_server_load.argtypes = [P, P, U32, U32, D, U32, P, U32, U64, P]
+    lib.katoann_index_autotune.argtypes = [P, P, U32, U32, U32, I32, U32, P, F, P]
     return lib
 
 
@@ -347,6 +348,25 @@ class Index:
             C.c_void_p(nprobe_out.data_ptr()) if nprobe_out is not None else None,
             C.c_void_p(ids.data_ptr()), C.c_void_p(dists.data_ptr()), _stream_arg(stream), tm,
             int(graph)))
+
+    def autotune(self, queries, k: int = 10, nprobe: int = 64, ranking: str = "prefix",
+                 survivors: int = 32, budget: "ProbeModel | None" = None,
+                 threshold: float = 0.95) -> dict:
+        """Times a search of these queries under every candidate setting of the
+        ranking pass's knobs (seed rows, CTA split weight, item width) and
+        keeps the fastest for the process; results never depend on them."""
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        if q.ndim != 2 or q.shape[1] != self.dim:
+            raise ValueError("queries must be (n, dim) float32")
+        if self.normalized:
+            q = normalize_rows(q)
+        out = np.zeros(4, np.uint32)
+        _check(_lib.katoann_index_autotune(self._h, _ptr(q), q.shape[0], k, nprobe,
+                                           _RANKING[ranking], survivors,
+                                           budget._h if budget is not None else None,
+                                           float(threshold), _ptr(out)))
+        return dict(seed_rows=int(out[0]), schedule=int(out[1]), width=int(out[2]),
+                    us_per_search=int(out[3]))
 
     def search_stats(self) -> dict:
         """Diagnostics of the last search (see katoann_gpu_workspace_stats)."""

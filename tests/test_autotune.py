@@ -1,0 +1,77 @@
+"""The ranking pass's knobs (seed rows, CTA split weight, item width) and the
+autotuner that picks them: every setting gives the oracle's results bit for
+bit; the autotuner returns one of its candidates and leaves results alone."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle
+import synth
+
+SPEC = dict(seed=71, n=30000, dim=128, ncomp=12, nlist=64, nq=256, rotation="random")
+
+
+def test_knob_setters_check_their_ranges():
+    from _gpu import gpu
+    lib = gpu()
+    assert lib.katoann_gpu_set_rank_width(24) == -1
+    assert lib.katoann_gpu_set_rank_schedule(9) == -1
+    knobs = (C.c_uint32 * 3)()
+    lib.katoann_gpu_rank_knobs(knobs)
+    assert lib.katoann_gpu_set_rank_width(32) == 0 and lib.katoann_gpu_set_rank_schedule(3) == 0
+    mine = (C.c_uint32 * 3)()
+    lib.katoann_gpu_rank_knobs(mine)
+    assert list(mine)[1:] == [3, 32]
+    assert lib.katoann_gpu_set_rank_width(knobs[2]) == 0
+    assert lib.katoann_gpu_set_rank_schedule(knobs[1]) == 0
+
+
+@pytest.mark.gpu
+def test_every_knob_setting_matches_the_oracle(tmp_path):
+    import katoann
+    from _gpu import gpu
+    lib = gpu()
+    prefix = str(tmp_path / "x")
+    queries, _ = synth.materialize(SPEC, prefix)
+    idx = katoann.Index()
+    idx.load(prefix)
+    ref = oracle.OracleIndex(prefix)
+    want = ref.search(queries, k=10, nprobe=12, survivors=32)
+    try:
+        for beta in (0, 1, 4, 8):
+            for width in (0, 16, 32):
+                for seed in (0, 64, 2048):
+                    assert lib.katoann_gpu_set_rank_schedule(beta) == 0
+                    assert lib.katoann_gpu_set_rank_width(width) == 0
+                    assert lib.katoann_gpu_set_seed_rows(seed) == 0
+                    got = idx.search(queries, k=10, nprobe=12, survivors=32)
+                    assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1]), \
+                        (beta, width, seed)
+    finally:
+        lib.katoann_gpu_set_rank_schedule(0)
+        lib.katoann_gpu_set_rank_width(0)
+        lib.katoann_gpu_set_seed_rows(0)
+
+
+@pytest.mark.gpu
+def test_autotune_keeps_results(tmp_path):
+    import katoann
+    from _gpu import gpu
+    lib = gpu()
+    prefix = str(tmp_path / "x")
+    queries, _ = synth.materialize(SPEC, prefix)
+    idx = katoann.Index()
+    idx.load(prefix)
+    ref = oracle.OracleIndex(prefix)
+    try:
+        t = idx.autotune(queries, k=10, nprobe=12, survivors=32)
+        assert t["seed_rows"] in (512, 1024, 2048) and t["schedule"] in (0, 1, 2, 4)
+        assert t["width"] in (0, 32) and t["us_per_search"] > 0
+        got = idx.search(queries, k=10, nprobe=12, survivors=32)
+        want = ref.search(queries, k=10, nprobe=12, survivors=32)
+        assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
+    finally:
+        lib.katoann_gpu_set_rank_schedule(0)
+        lib.katoann_gpu_set_rank_width(0)
+        lib.katoann_gpu_set_seed_rows(0)
