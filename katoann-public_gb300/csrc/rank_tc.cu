@@ -639,16 +639,38 @@ __device__ __forceinline__ void for_rows_split(const uint8_t *__restrict__ x, ui
 // bound = L + (L >> 22) + 1: the distance value is monotone in l2 and two l2
 // that far apart never round to the same float, so every row whose distance
 // can tie the S-th best is still inside. Fewer than S rows: no bound.
+// The queries grouped by their nearest list: a counting sort by one CTA, so
+// that seed CTAs reading the same list's rows run together and share them
+// through L2. order[i] = the query the i-th seed CTA takes.
+constexpr uint32_t kOrderLists = 16384;  // lists the counting sort holds in shared memory
+
+__global__ void __launch_bounds__(1024) seed_order_kernel(const uint32_t *__restrict__ probed,
+                                                          uint32_t p, uint32_t B, uint32_t L,
+                                                          uint32_t *__restrict__ order) {
+  extern __shared__ uint32_t lh[];  // L counters, then offsets
+  for (uint32_t i = threadIdx.x; i < L; i += blockDim.x) lh[i] = 0;
+  __syncthreads();
+  for (uint32_t q = threadIdx.x; q < B; q += blockDim.x)
+    atomicAdd(&lh[probed[static_cast<size_t>(q) * p]], 1u);
+  __syncthreads();
+  block_scan2(
+      L, [&](uint32_t i) { return make_uint2(lh[i], 0u); },
+      [&](uint32_t i, uint32_t a, uint32_t) { lh[i] = a; });
+  __syncthreads();
+  for (uint32_t q = threadIdx.x; q < B; q += blockDim.x)
+    order[atomicAdd(&lh[probed[static_cast<size_t>(q) * p]], 1u)] = q;
+}
+
 __global__ void __launch_bounds__(256) rank_seed_kernel(
     const uint8_t *__restrict__ xhi, const int64_t *__restrict__ xnorm,
     const uint8_t *__restrict__ qhi, const int64_t *__restrict__ qnorm,
     const uint32_t *__restrict__ probed, const uint32_t *__restrict__ qprobes,
-    const uint32_t *__restrict__ list_off, uint32_t p, uint32_t dc, uint32_t h, uint32_t S,
-    uint32_t want, int32_t *__restrict__ bound) {
+    const uint32_t *__restrict__ list_off, const uint32_t *__restrict__ order, uint32_t p,
+    uint32_t dc, uint32_t h, uint32_t S, uint32_t want, int32_t *__restrict__ bound) {
   __shared__ int32_t l2s[kSeedCap];
   __shared__ uint32_t qw[2048 / 4];
   __shared__ uint32_t hist[256], sel[2], wsum[8];
-  const uint32_t q = blockIdx.x, tid = threadIdx.x;
+  const uint32_t q = order ? order[blockIdx.x] : blockIdx.x, tid = threadIdx.x;
   for (uint32_t i = tid; i < h / 4; i += blockDim.x)
     qw[i] = reinterpret_cast<const uint32_t *>(qhi + static_cast<size_t>(q) * dc)[i];
   __syncthreads();
@@ -1041,12 +1063,24 @@ int rank_tc_bucket(const uint4 *rec, const uint32_t *rec_n, uint32_t rec_cap, ui
 
 int rank_seed(const uint8_t *xhi, const int64_t *xnorm, const uint8_t *qhi, const int64_t *qnorm,
               const uint32_t *probed, const uint32_t *qprobes, const uint32_t *list_off,
-              uint32_t B, uint32_t p,
-              uint32_t dc, uint32_t h, uint32_t S, uint32_t rows, int32_t *bound, cudaStream_t st) {
+              uint32_t L, uint32_t B, uint32_t p, uint32_t dc, uint32_t h, uint32_t S,
+              uint32_t rows, uint32_t *order, int32_t *bound, cudaStream_t st) {
   if (h > 2048 || h % 16) return invalid("seed bounds need h <= 2048, a multiple of 16");
   if (B == 0) return KATO_OK;
-  rank_seed_kernel<<<B, 256, 0, st>>>(xhi, xnorm, qhi, qnorm, probed, qprobes, list_off, p, dc, h, S,
-                                      std::min(std::max(rows, S), kSeedCap), bound);
+  const uint32_t *ord = nullptr;
+  if (order && L <= kOrderLists) {
+    static bool attr = false;
+    if (!attr) {
+      KATO_CUDA(cudaFuncSetAttribute(seed_order_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(kOrderLists * 4)));
+      attr = true;
+    }
+    seed_order_kernel<<<1, 1024, L * 4, st>>>(probed, p, B, L, order);
+    KATO_LAUNCHED("seed_order_kernel");
+    ord = order;
+  }
+  rank_seed_kernel<<<B, 256, 0, st>>>(xhi, xnorm, qhi, qnorm, probed, qprobes, list_off, ord, p, dc,
+                                      h, S, std::min(std::max(rows, S), kSeedCap), bound);
   KATO_LAUNCHED("rank_seed_kernel");
   return KATO_OK;
 }

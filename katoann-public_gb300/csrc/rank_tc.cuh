@@ -89,8 +89,8 @@ int rank_tc(const RankTcArgs &A, const uint8_t *xhi, uint32_t npts, const TcShap
 // `rows` rows (at most 4096) of its probed lists in probe order.
 int rank_seed(const uint8_t *xhi, const int64_t *xnorm, const uint8_t *qhi, const int64_t *qnorm,
               const uint32_t *probed, const uint32_t *qprobes, const uint32_t *list_off,
-              uint32_t B, uint32_t p,
-              uint32_t dc, uint32_t h, uint32_t S, uint32_t rows, int32_t *bound, cudaStream_t st);
+              uint32_t L, uint32_t B, uint32_t p, uint32_t dc, uint32_t h, uint32_t S,
+              uint32_t rows, uint32_t *order, int32_t *bound, cudaStream_t st);
 // Work items of the pass (per list: groups of N queries) and their tile
 // offsets; also zeroes the B candidate counts and buffer fills. With
 // beta > 0, also per-item cost offsets: a tile of an item of MMA width w

@@ -735,7 +735,7 @@ struct Plan {
       off_woff, off_cur, off_work, off_ent, off_slots, off_surv, off_nsurv, off_stats,
       off_tcscratch, off_tcitems, off_tileoff, off_nitems, off_qcount, off_qfill, off_bound,
       off_rec, off_recn, off_rlist, off_rkey, off_rcount, off_qh16, off_ql16, off_qterm, off_rot,
-      off_qprobes, off_z, off_costoff, total;
+      off_qprobes, off_z, off_costoff, off_seedorder, total;
 };
 
 static size_t align256(size_t x) { return (x + 255) / 256 * 256; }
@@ -826,6 +826,7 @@ int make_plan(const katoann_gpu_index *ix, uint32_t B, uint32_t k, uint32_t p, i
   pl.off_rkey = take(static_cast<size_t>(B) * 8);
   pl.off_rcount = take(kRescanCounters * 4);
   pl.off_qprobes = take(static_cast<size_t>(B) * 4);
+  pl.off_seedorder = take(static_cast<size_t>(B) * 4);
   pl.off_z = take(static_cast<size_t>(B) * KATO_PROBE_FEATURES * 4);
   pl.off_surv = take(static_cast<size_t>(B) * pl.S * sizeof(uint2));
   pl.off_nsurv = take(static_cast<size_t>(B) * 4);
@@ -969,9 +970,11 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
     const int64_t *xnorm = prefix_mode ? ix->d_headnorm : ix->d_hinorm;
     const int64_t *qnorm = prefix_mode ? qh0 : qhn;
     const DistScale scale = make_dist_scale(ix->step_sq);
-    if ((rc = rank_seed(ix->d_hi, xnorm, qhi, qnorm, probed, qprobes, ix->d_list_off, nq, p, dc,
-                        pl.dims, pl.S, pl.seed_rows, bound, st)))
+    if ((rc = rank_seed(ix->d_hi, xnorm, qhi, qnorm, probed, qprobes, ix->d_list_off, L, nq, p, dc,
+                        pl.dims, pl.S, pl.seed_rows,
+                        reinterpret_cast<uint32_t *>(ws + pl.off_seedorder), bound, st)))
       return rc;
+    g_launches += L <= 16384 ? 1 : 0;  // the seed order
     mark(tm, 6, st);
     uint32_t *cost_off = reinterpret_cast<uint32_t *>(ws + pl.off_costoff);
     if ((rc = rank_tc_prepare(cnt, ix->d_list_off, L, pl.tcs.N, nq, pl.beta,
