@@ -574,14 +574,25 @@ __device__ __forceinline__ uint32_t row_dot(const uint8_t *row, const uint32_t *
 // (G steps, all loads of the batch in flight together) and hands row
 // base + l of the batch to one lane, so f(i, dot) runs on all 32 lanes at
 // once. All threads of the CTA take part.
-template <uint32_t G, typename F>
+//
+// pre(i) - a per-row value the callback needs (e.g. the row's norm) - is
+// loaded at the start of the batch by the lane that later calls
+// f(i, dot, pre(i)), so that it arrives with the rows instead of after them.
+struct NoPre {
+  __device__ int64_t operator()(uint32_t) const { return 0; }
+};
+
+template <uint32_t G, typename F, typename Pre>
 __device__ __forceinline__ void rows_split(const uint8_t *__restrict__ x, uint32_t dc, uint32_t h,
-                                           const uint32_t *qw, uint32_t r0, uint32_t n, F f) {
+                                           const uint32_t *qw, uint32_t r0, uint32_t n, Pre pre,
+                                           F f) {
   constexpr uint32_t RPW = 32 / G;  // rows per step
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const uint32_t sub = lane / G, gl = lane % G, cpl = (h / 16) / G;
   for (uint32_t base = warp * 32; base < n; base += nw * 32) {
     uint32_t mine = 0;
+    const uint32_t my_row = base + gl * RPW + sub;
+    const int64_t pv = my_row < n ? pre(my_row) : 0;
     if (G <= 16 && cpl == 1) {
       // every load of the batch first, then the sums
       uint4 v[G <= 16 ? G : 1];
@@ -618,19 +629,19 @@ __device__ __forceinline__ void rows_split(const uint8_t *__restrict__ x, uint32
         if (gl == it) mine = dot;
       }
     }
-    const uint32_t i = base + gl * RPW + sub;
-    if (i < n) f(i, mine);
+    if (my_row < n) f(my_row, mine, pv);
   }
 }
 
-template <typename F>
+template <typename F, typename Pre = NoPre>
 __device__ __forceinline__ void for_rows_split(const uint8_t *__restrict__ x, uint32_t dc, uint32_t h,
-                                               const uint32_t *qw, uint32_t r0, uint32_t n, F f) {
+                                               const uint32_t *qw, uint32_t r0, uint32_t n, F f,
+                                               Pre pre = Pre{}) {
   const uint32_t g = min(32u, h / 16);
-  if (g == 16) rows_split<16>(x, dc, h, qw, r0, n, f);
-  else if (g == 32) rows_split<32>(x, dc, h, qw, r0, n, f);
-  else if (g == 8) rows_split<8>(x, dc, h, qw, r0, n, f);
-  else rows_split<4>(x, dc, h, qw, r0, n, f);
+  if (g == 16) rows_split<16>(x, dc, h, qw, r0, n, pre, f);
+  else if (g == 32) rows_split<32>(x, dc, h, qw, r0, n, pre, f);
+  else if (g == 8) rows_split<8>(x, dc, h, qw, r0, n, pre, f);
+  else rows_split<4>(x, dc, h, qw, r0, n, pre, f);
 }
 
 // ------------------------------------------------------------- seed bounds
@@ -661,7 +672,7 @@ __global__ void __launch_bounds__(1024) seed_order_kernel(const uint32_t *__rest
     order[atomicAdd(&lh[probed[static_cast<size_t>(q) * p]], 1u)] = q;
 }
 
-__global__ void __launch_bounds__(256) rank_seed_kernel(
+__global__ void __launch_bounds__(256, 3) rank_seed_kernel(
     const uint8_t *__restrict__ xhi, const int64_t *__restrict__ xnorm,
     const uint8_t *__restrict__ qhi, const int64_t *__restrict__ qnorm,
     const uint32_t *__restrict__ probed, const uint32_t *__restrict__ qprobes,
@@ -680,9 +691,12 @@ __global__ void __launch_bounds__(256) rank_seed_kernel(
   for (uint32_t r = 0; r < pq && count < want; ++r) {
     const uint32_t c = probed[static_cast<size_t>(q) * p + r];
     const uint32_t r0 = list_off[c], n = min(list_off[c + 1] - r0, kSeedCap - count);
-    for_rows_split(xhi, dc, h, qw, r0, n, [&](uint32_t i, uint32_t dot) {
-      l2s[count + i] = static_cast<int32_t>(qn + xnorm[r0 + i] - 2 * static_cast<int64_t>(dot));
-    });
+    for_rows_split(
+        xhi, dc, h, qw, r0, n,
+        [&](uint32_t i, uint32_t dot, int64_t xn) {
+          l2s[count + i] = static_cast<int32_t>(qn + xn - 2 * static_cast<int64_t>(dot));
+        },
+        [&](uint32_t i) { return xnorm[r0 + i]; });
     count += n;
   }
   __syncthreads();
@@ -824,9 +838,11 @@ __global__ void __launch_bounds__(256) rescan_rows_kernel(
     const unsigned long long K = kbound[q];
     uint2 *buf = qbuf + static_cast<size_t>(q) * cap;
     const uint32_t r0 = list_off[c];
-    for_rows_split(key.xhi, key.dc, key.h, qw, r0, list_off[c + 1] - r0, [&](uint32_t i, uint32_t dot) {
+    for_rows_split(
+        key.xhi, key.dc, key.h, qw, r0, list_off[c + 1] - r0,
+        [&](uint32_t i, uint32_t dot, int64_t xn) {
       const uint32_t row = r0 + i;
-      const int64_t l2 = qn + key.xnorm[row] - 2 * static_cast<int64_t>(dot);
+      const int64_t l2 = qn + xn - 2 * static_cast<int64_t>(dot);
       const unsigned long long k =
           (static_cast<unsigned long long>(__float_as_uint(dist_value(l2, key.scale))) << 32) |
           key.ids[row];
@@ -834,7 +850,8 @@ __global__ void __launch_bounds__(256) rescan_rows_kernel(
         const uint32_t at = atomicAdd(qcount + q, 1u);
         if (at < cap) buf[at] = make_uint2(static_cast<uint32_t>(k >> 32), row);
       }
-    });
+    },
+        [&](uint32_t i) { return key.xnorm[r0 + i]; });
   }
 }
 
