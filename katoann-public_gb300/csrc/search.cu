@@ -518,10 +518,13 @@ __global__ void __launch_bounds__(kThreads) refine_kernel(
   uint32_t *eid = reinterpret_cast<uint32_t *>(ex + S);  // [S]
   float *hd = reinterpret_cast<float *>(eid + S);      // [k]
   uint32_t *hid = reinterpret_cast<uint32_t *>(hd + k);  // [k]
+  uint32_t *srow = hid + k;                             // [S] the survivors' rows
   for (uint32_t i = threadIdx.x; i < n16; i += blockDim.x) {
     sq[i] = reinterpret_cast<const uint4 *>(qhi + static_cast<size_t>(q) * dc)[i];
     sq[n16 + i] = reinterpret_cast<const uint4 *>(qlo + static_cast<size_t>(q) * dc)[i];
   }
+  for (uint32_t i = threadIdx.x; i < ns; i += blockDim.x)
+    srow[i] = surv[static_cast<size_t>(q) * S + i].y;
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t nwarps = blockDim.x / 32;
@@ -530,8 +533,8 @@ __global__ void __launch_bounds__(kThreads) refine_kernel(
   for (uint32_t s0 = warp; s0 < ns; s0 += 2 * nwarps) {
     const uint32_t s1 = s0 + nwarps;
     const bool two = s1 < ns;
-    const uint32_t r0 = surv[static_cast<size_t>(q) * S + s0].y;
-    const uint32_t r1 = two ? surv[static_cast<size_t>(q) * S + s1].y : r0;
+    const uint32_t r0 = srow[s0];
+    const uint32_t r1 = two ? srow[s1] : r0;
     uint32_t id0 = 0, id1 = 0;
     int64_t xn0 = 0, xn1 = 0;
     if (lane == 0) {
@@ -596,55 +599,52 @@ __global__ void __launch_bounds__(kThreads) refine_kernel(
   // first k enter; a later one replaces the largest (distance, id) when its
   // distance is strictly smaller; then ascending by (distance, id).
   if (k <= 32) {
-    // one warp: lane i holds heap slot i
+    // one warp holds the heap sorted descending by (distance, id) across its
+    // lanes - lane 0 is the largest, the one the reference evicts - so an
+    // insertion is one ballot and one shift; unused lanes sort below all
     if (warp != 0) return;
-    float d = 3.402823466e+38f;
-    uint32_t id = 0xFFFFFFFFu, n = 0;
+    const uint32_t u = static_cast<uint32_t>(lane);
+    float d = -1.0f;
+    uint32_t id = 0u, n = 0;
     for (uint32_t s = 0; s < ns; ++s) {
       const float dd = ex[s];
       const uint32_t ii = eid[s];
       if (ii >= npts) continue;  // ids without a row are skipped (:1091-1094)
+      const bool gt = d > dd || (d == dd && id > ii);  // this slot sorts above the new one
       if (n < k) {
-        if (lane == static_cast<int>(n)) {
+        // enters after the g larger ones; the rest move up one lane
+        const uint32_t g = __popc(__ballot_sync(0xffffffffu, gt && u < n));
+        const float ud = __shfl_up_sync(0xffffffffu, d, 1);
+        const uint32_t uid = __shfl_up_sync(0xffffffffu, id, 1);
+        if (u == g) {
           d = dd;
           id = ii;
+        } else if (u > g && u <= n) {
+          d = ud;
+          id = uid;
         }
         ++n;
         continue;
       }
-      // the largest (distance, id) of the k slots
-      float md = lane < static_cast<int>(k) ? d : -1.0f;
-      uint32_t mid = lane < static_cast<int>(k) ? id : 0u;
-      int ml = lane;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const float od = __shfl_xor_sync(0xffffffffu, md, o);
-        const uint32_t oid = __shfl_xor_sync(0xffffffffu, mid, o);
-        const int ol = __shfl_xor_sync(0xffffffffu, ml, o);
-        if (od > md || (od == md && oid > mid)) {
-          md = od;
-          mid = oid;
-          ml = ol;
-        }
-      }
-      if (dd < md && lane == ml) {
+      if (!(dd < __shfl_sync(0xffffffffu, d, 0))) continue;  // strictly below the largest
+      // the largest leaves; the g larger ones below it move down one lane
+      const uint32_t g = __popc(__ballot_sync(0xffffffffu, gt && u >= 1 && u < k));
+      const float nd = __shfl_down_sync(0xffffffffu, d, 1);
+      const uint32_t nid = __shfl_down_sync(0xffffffffu, id, 1);
+      if (u < g) {
+        d = nd;
+        id = nid;
+      } else if (u == g) {
         d = dd;
         id = ii;
       }
     }
-    // rank of each slot among the n filled ones (ids are distinct)
-    uint32_t r = 0;
-    for (uint32_t j = 0; j < n; ++j) {
-      const float od = __shfl_sync(0xffffffffu, d, j);
-      const uint32_t oid = __shfl_sync(0xffffffffu, id, j);
-      r += (od < d || (od == d && oid < id)) ? 1u : 0u;
-    }
-    if (lane < static_cast<int>(n)) {
-      out_ids[static_cast<size_t>(q) * k + r] = id;
-      out_dists[static_cast<size_t>(q) * k + r] = d;
-    } else if (lane < static_cast<int>(k)) {
-      out_ids[static_cast<size_t>(q) * k + lane] = 0xFFFFFFFFu;
-      out_dists[static_cast<size_t>(q) * k + lane] = 3.402823466e+38f;
+    if (u < n) {  // ascending: lane u is the (n - 1 - u)-th
+      out_ids[static_cast<size_t>(q) * k + (n - 1 - u)] = id;
+      out_dists[static_cast<size_t>(q) * k + (n - 1 - u)] = d;
+    } else if (u < k) {
+      out_ids[static_cast<size_t>(q) * k + u] = 0xFFFFFFFFu;
+      out_dists[static_cast<size_t>(q) * k + u] = 3.402823466e+38f;
     }
     return;
   }
@@ -1071,7 +1071,7 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
     return KATO_OK;
   }
   // 6. exact refinement and top-k (:1081-1125)
-  const size_t rsmem = static_cast<size_t>(dc) * 2 + static_cast<size_t>(pl.S) * 8 +
+  const size_t rsmem = static_cast<size_t>(dc) * 2 + static_cast<size_t>(pl.S) * 12 +
                        static_cast<size_t>(pl.k) * 8;
   KATO_CUDA(cudaFuncSetAttribute(refine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(rsmem)));
