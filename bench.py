@@ -722,14 +722,16 @@ def run_reference(args, torch, vectors, order, cen, rot, sizes, queries, gt, set
         tot_q += m
     value = tot_q / tot_t
     r = recall(ids, gt[:m], k)
-    out = {"impl": "reference", "metric": "QPS at recall@10 >= 0.99 (fixed nprobe), 10M x 1024 IVF, "
-           "batch 4096, 1 GB300", "value": round(value, 1), "unit": "queries/s", "n_gpus": 1,
+    # the same metric as the GPU arm; the reference's own path has one nprobe
+    # for the batch (its setting that reaches recall 0.99 on this workload)
+    out = {"impl": "reference", "metric": "QPS at recall@10 >= 0.99, 10M x 1024 IVF, learned vs fixed "
+           "nprobe, batch 4096, 1 GB300", "value": round(value, 1), "unit": "queries/s", "n_gpus": 1,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(tot_t / args.steps * 1e3, 3),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
            "data": "synthetic (same seeded workload as the GPU arm)",
            "config": {"workload": f"{args.n // 1000000}M x {args.dim} IVF, nlist {args.nlist}, "
-                                  f"batch {args.batch}, k {k}", "nprobe": p, "survivors": S,
-                      "prefix_dims": args.head},
+                                  f"batch {args.batch}, k {k}", "nprobe_path": "fixed",
+                      "nprobe": p, "survivors": S, "prefix_dims": args.head},
            "recall_sample": round(r, 5),
            "cpu_baseline": {"value": round(value, 1), "unit": "queries/s", "cores": cores, "kind": "port",
                             "sample": f"{m} queries per step of the 4096-query batch",
