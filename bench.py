@@ -68,6 +68,9 @@ def parse_args():
     ap.add_argument("--label-survivors", type=int, default=256,
                     help="survivors of that search (prefix ranking, exact refinement)")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default knobs of the ranking pass (profiling runs)")
+    ap.add_argument("--probe-epochs", type=int, default=48, help="training epochs of the probe model")
     ap.add_argument("--serve-seconds", type=float, default=1.5,
                     help="arrivals per serving run (seconds of the Poisson stream)")
     return ap.parse_args()
@@ -376,7 +379,8 @@ def main():
             m = katoann.ProbeModel.train(idx, tq, ladder=ladder, depth=min(256, L), k=k,
                                          label_nprobe=lab_p, label_ranking="prefix",
                                          label_survivors=args.label_survivors, ranking="prefix",
-                                         survivors=s_l, epochs=24, batch=1024, seed=args.seed)
+                                         survivors=s_l, epochs=args.probe_epochs, batch=512,
+                                         seed=args.seed)
             models[s_l] = m
             hist = np.bincount(m.labels, minlength=len(ladder))
             learned_info["models"][s_l] = {"train_s": round(time.time() - t_l, 1),
@@ -423,9 +427,11 @@ def main():
 
     # ---- the autotuner picks the ranking pass's knobs for this setting
     # (seed rows, CTA split weight, item width; results never depend on them)
-    tuned = idx.autotune(queries.cpu().numpy(), k=k, nprobe=cfg["nprobe"], survivors=S,
-                         budget=cfg.get("model"), threshold=cfg.get("threshold", 0.95))
-    tuned["ms_before"] = chosen["ms"]
+    tuned = None
+    if not args.no_autotune:
+        tuned = idx.autotune(queries.cpu().numpy(), k=k, nprobe=cfg["nprobe"], survivors=S,
+                             budget=cfg.get("model"), threshold=cfg.get("threshold", 0.95))
+        tuned["ms_before"] = chosen["ms"]
 
     # ---- timed region: K steps on device-resident queries
     for _ in range(max(3, args.warmup)):
