@@ -35,7 +35,8 @@ for _p in (os.path.join(ROOT, "katoann-public_gb300"), os.path.join(ROOT, "oracl
 
 PUBLISHED_QPS_099 = 6294.0  # README.md:84 (BioASQ-1024-10M, 28-core Xeon, nlist 8192)
 LADDER = (8, 12, 16, 24, 32, 48, 64, 96, 128, 192, 256, 384, 512)  # learned nprobe choices
-THRESHOLDS = (0.3, 0.5, 0.7, 0.8, 0.9, 0.95, 0.98, 0.99, 0.995, 0.999)
+THRESHOLDS = (0.3, 0.5, 0.7, 0.8, 0.82, 0.84, 0.86, 0.88, 0.9, 0.92, 0.94, 0.96, 0.97, 0.98,
+              0.985, 0.99, 0.995, 0.999)
 
 
 def parse_args():
@@ -70,7 +71,7 @@ def parse_args():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default knobs of the ranking pass (profiling runs)")
-    ap.add_argument("--probe-epochs", type=int, default=48, help="training epochs of the probe model")
+    ap.add_argument("--probe-epochs", type=int, default=24, help="training epochs of the probe model")
     ap.add_argument("--serve-seconds", type=float, default=1.5,
                     help="arrivals per serving run (seconds of the Poisson stream)")
     return ap.parse_args()
@@ -352,8 +353,10 @@ def main():
     if args.nprobe:
         grid = [(args.nprobe, args.survivors)]
     else:
-        grid = [(p, s) for s in (32, 64) for p in (16, 24, 32, 48, 64, 96, 128, 192, 256) if p <= L]
-        grid += [(p, 128) for p in (128, 192, 256, 384, 512) if p <= L]  # towards recall 0.999
+        # the same granularity for the fixed path as for the learned thresholds
+        grid = [(p, s) for s in (32, 64)
+                for p in (16, 24, 32, 48, 64, 72, 80, 88, 96, 112, 128, 160, 192, 256) if p <= L]
+        grid += [(p, 128) for p in (128, 160, 192, 224, 256, 320, 384, 512) if p <= L]
     for p, s in grid:
         r, ms, _ = run(dict(nprobe=p, survivors=s))
         sweep.append({"path": "fixed", "nprobe": p, "survivors": s, "recall": round(r, 5),
@@ -379,7 +382,7 @@ def main():
             m = katoann.ProbeModel.train(idx, tq, ladder=ladder, depth=min(256, L), k=k,
                                          label_nprobe=lab_p, label_ranking="prefix",
                                          label_survivors=args.label_survivors, ranking="prefix",
-                                         survivors=s_l, epochs=args.probe_epochs, batch=512,
+                                         survivors=s_l, epochs=args.probe_epochs, batch=1024,
                                          seed=args.seed)
             models[s_l] = m
             hist = np.bincount(m.labels, minlength=len(ladder))
