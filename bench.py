@@ -72,6 +72,8 @@ def parse_args():
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default knobs of the ranking pass (profiling runs)")
     ap.add_argument("--probe-epochs", type=int, default=24, help="training epochs of the probe model")
+    ap.add_argument("--probe-depth", type=int, default=256,
+                    help="coarse ranks the probe model's features read")
     ap.add_argument("--serve-seconds", type=float, default=1.5,
                     help="arrivals per serving run (seconds of the Poisson stream)")
     return ap.parse_args()
@@ -373,13 +375,14 @@ def main():
         cap = min(LADDER[-1], L)
         ladder = tuple(v for v in LADDER if v <= L)
         lab_p = min(L, args.label_nprobe)
-        learned_info = {"train_queries": len(tq), "ladder": list(ladder), "depth": min(256, L),
+        depth = min(args.probe_depth, L)
+        learned_info = {"train_queries": len(tq), "ladder": list(ladder), "depth": depth,
                         "label_search": {"nprobe": lab_p, "ranking": "prefix",
                                          "survivors": args.label_survivors},
                         "models": {}}
         for s_l in (64, 128):
             t_l = time.time()
-            m = katoann.ProbeModel.train(idx, tq, ladder=ladder, depth=min(256, L), k=k,
+            m = katoann.ProbeModel.train(idx, tq, ladder=ladder, depth=depth, k=k,
                                          label_nprobe=lab_p, label_ranking="prefix",
                                          label_survivors=args.label_survivors, ranking="prefix",
                                          survivors=s_l, epochs=args.probe_epochs, batch=1024,
