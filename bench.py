@@ -72,7 +72,7 @@ def parse_args():
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default knobs of the ranking pass (profiling runs)")
     ap.add_argument("--probe-epochs", type=int, default=24, help="training epochs of the probe model")
-    ap.add_argument("--probe-depth", type=int, default=256,
+    ap.add_argument("--probe-depth", type=int, default=128,
                     help="coarse ranks the probe model's features read")
     ap.add_argument("--serve-seconds", type=float, default=1.5,
                     help="arrivals per serving run (seconds of the Poisson stream)")

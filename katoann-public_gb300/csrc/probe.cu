@@ -33,8 +33,9 @@ namespace {
 constexpr uint32_t kF = KATO_PROBE_FEATURES;  // 64
 constexpr uint32_t kH = KATO_PROBE_HIDDEN;    // 256
 constexpr uint32_t kCMax = KATO_PROBE_MAX_CLASSES;
-constexpr uint32_t kQB = 32;   // queries per MLP CTA
-constexpr uint32_t kAS = 36;   // shared-memory row stride of the activations (floats)
+constexpr uint32_t kQB = 16;   // queries per MLP CTA
+constexpr uint32_t kAS = 20;   // shared-memory row stride of the activations (floats; 16-byte
+                               // rows, conflict-free 128-bit stores)
 
 __device__ __forceinline__ float bf16_value(uint16_t b) {
   return __uint_as_float(static_cast<uint32_t>(b) << 16);
@@ -81,7 +82,7 @@ struct MlpArgs {
   float threshold;
 };
 
-// One dense ReLU layer over the CTA's 32 queries: thread j owns output unit j.
+// One dense ReLU layer over the CTA's 16 queries: thread j owns output unit j.
 // in: [K][kAS] (unit-major, query fastest), out: [kH][kAS]; w is K x kH bf16
 // (global memory through L2, or shared memory).
 template <uint32_t K>
@@ -148,26 +149,26 @@ __global__ void __launch_bounds__(kH) probe_mlp_kernel(const float *__restrict__
   dense_relu<kH>(h1, m.w2, m.b2, h2);
   __syncthreads();
   {
-    // logits: thread = (query t / 8, classes t % 8 + 8 u)
-    const uint32_t qi = t >> 3, part = t & 7;
-    float acc[kCMax / 8];
+    // logits: thread = (query t / 16, classes t % 16 + 16 u)
+    const uint32_t qi = t >> 4, part = t & 15;
+    float acc[kCMax / 16];
 #pragma unroll
-    for (uint32_t u = 0; u < kCMax / 8; ++u) {
-      const uint32_t c = part + 8 * u;
+    for (uint32_t u = 0; u < kCMax / 16; ++u) {
+      const uint32_t c = part + 16 * u;
       acc[u] = c < m.C ? m.b3[c] : 0.f;
     }
 #pragma unroll 4
     for (uint32_t k = 0; k < kH; ++k) {
       const float x = h2[k * kAS + qi];
 #pragma unroll
-      for (uint32_t u = 0; u < kCMax / 8; ++u) {
-        const uint32_t c = part + 8 * u;
+      for (uint32_t u = 0; u < kCMax / 16; ++u) {
+        const uint32_t c = part + 16 * u;
         if (c < m.C) acc[u] = fmaf(bf16_value(sw3[k * m.C + c]), x, acc[u]);
       }
     }
 #pragma unroll
-    for (uint32_t u = 0; u < kCMax / 8; ++u) {
-      const uint32_t c = part + 8 * u;
+    for (uint32_t u = 0; u < kCMax / 16; ++u) {
+      const uint32_t c = part + 16 * u;
       if (c < m.C) lg[qi * (kCMax + 1) + c] = acc[u];
     }
   }
