@@ -79,14 +79,51 @@ def parse_args():
     return ap.parse_args()
 
 
+# ----------------------------------------------------------------- ranks
+# N GPUs run N replicas: every rank holds the same index (same data seed) and
+# searches its own batches of queries. No collective touches the search; the
+# job's QPS is all ranks' queries over the slowest rank's time, and every
+# rank runs the setting rank 0 chose.
+
+def query_seed(seed: int, rank: int) -> int:
+    """The seed of a rank's evaluation queries: rank 0 keeps the single-GPU
+    queries, every other rank draws its own."""
+    return seed + 1_000_003 * rank
+
+
+def max_over_ranks(dist, x: float) -> float:
+    """The largest x over all ranks (the slowest rank's time); x itself
+    without a process group."""
+    if dist is None:
+        return float(x)
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def from_rank0(dist, i: int) -> int:
+    """Rank 0's integer on every rank (i itself without a process group)."""
+    if dist is None:
+        return int(i)
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([int(i)], dtype=torch.int64, device=dev)
+    dist.broadcast(t, src=0)
+    return int(t.item())
+
+
 # ----------------------------------------------------------------- data
-def make_data(torch, n, d, ncomp, seed, queries, train_queries=0):
+def make_data(torch, n, d, ncomp, seed, queries, train_queries=0, qseed=None, dev="cuda"):
     """Unit vectors: mixture centres and per-point noise share an anisotropic
     spectrum (eigenvalue_i ~ i^-1.2) in a random orthogonal basis; component
     weights follow Zipf(1.1), so the inverted lists come out skewed. Returns
     the base, the evaluation queries and (another stream of the same
-    distribution) the probe-budget training queries."""
-    dev = "cuda"
+    distribution) the probe-budget training queries. `seed` fixes the
+    distribution, the base and the training queries; `qseed` (default: seed)
+    the evaluation queries, so that replicas share an index and differ in
+    their queries."""
     g = torch.Generator(device=dev).manual_seed(seed)
     # random orthogonal basis (QR on the host: torch's linear-algebra library is
     # not needed on the device path)
@@ -110,7 +147,7 @@ def make_data(torch, n, d, ncomp, seed, queries, train_queries=0):
         return out
 
     base = sample(n, g)
-    gq = torch.Generator(device=dev).manual_seed(seed + 7919)
+    gq = torch.Generator(device=dev).manual_seed((seed if qseed is None else qseed) + 7919)
     q = sample(queries, gq)
     gt_ = torch.Generator(device=dev).manual_seed(seed + 104729)
     tq = sample(train_queries, gt_) if train_queries else None
@@ -284,20 +321,19 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference" and rank != 0:
+        return  # rank 0 alone times the CPU reference; it needs no process group
     torch.cuda.set_device(local)
     dist = None
-    if world > 1:
+    if world > 1 and args.impl == "ours":
         import torch.distributed as dist
-        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
-    if args.impl == "reference" and rank != 0:
-        if dist:
-            dist.destroy_process_group()
-        return
+        dist.init_process_group("nccl")
     torch.backends.cuda.matmul.allow_tf32 = True
     t0 = time.time()
     n, d, L, B, k = args.n, args.dim, args.nlist, args.batch, args.k
     ntrain = 0 if (args.no_learned or args.nprobe or args.impl == "reference") else args.train_queries
-    base, queries, train_q = make_data(torch, n, d, args.ncomp, args.seed + rank, B, ntrain)
+    base, queries, train_q = make_data(torch, n, d, args.ncomp, args.seed, B, ntrain,
+                                       qseed=query_seed(args.seed, rank))
     cen = kmeans(torch, base, L, args.kmeans_iters, min(args.train, n), args.seed)
     rot = pca_rotation(torch, base, min(100000, n), args.seed)
     a = assign(torch, base, cen)
@@ -422,6 +458,7 @@ def main():
 
     b99, b999 = best(0.99), best(0.999)
     chosen = b99 or max(sweep, key=lambda x: x["recall"])
+    chosen = sweep[from_rank0(dist, sweep.index(chosen))]  # the same grid on every rank
     if chosen["path"] == "learned":
         cfg = dict(nprobe=chosen["cap"], survivors=chosen["survivors"],
                    model=models[chosen["survivors"]], threshold=chosen["threshold"])
@@ -459,11 +496,7 @@ def main():
     if dist:
         dist.barrier()
     phases, passes = timer.read()
-    ms = elapsed_ms
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(dist, elapsed_ms)
     value = world * B * args.steps / (ms / 1e3)
     search(cfg, nprobe_out=np_d)
     torch.cuda.synchronize()
@@ -481,13 +514,15 @@ def main():
     for _ in range(max(3, args.warmup)):
         search_graph()
     torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
     g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     g0.record()
     for _ in range(args.steps):
         search_graph()
     g1.record()
     torch.cuda.synchronize()
-    graph_ms = g0.elapsed_time(g1) / args.steps
+    graph_ms = max_over_ranks(dist, g0.elapsed_time(g1) / args.steps)
     graph_recall = recall(ids_d.cpu().numpy().view(np.uint32), gt, k)
 
     # ---- end to end through the public host API (pinned host buffers)
@@ -508,7 +543,7 @@ def main():
     t2 = time.perf_counter()
     for _ in range(e2e_steps):
         host_search()
-    e2e_s = time.perf_counter() - t2
+    e2e_s = max_over_ranks(dist, time.perf_counter() - t2)
     e2e_qps = world * B * e2e_steps / e2e_s
     e2e_recall = recall(ih.numpy().view(np.uint32), gt, k)
 
