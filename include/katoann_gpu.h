@@ -71,6 +71,10 @@ typedef struct {
   const uint16_t *d_chi16;
   const uint16_t *d_clo16;
   const int64_t *d_cterm;
+  /* Optional (NULL: each search transposes d_rotation): d_rotation in the
+   * k-major layout the query rotation stages from; see
+   * katoann_gpu_rotation_kmajor. */
+  const float *d_rotation_t;
 } katoann_gpu_index;
 
 const char *katoann_gpu_last_error(void);
@@ -81,6 +85,15 @@ int katoann_gpu_version(void);
  * which give identical bits), nrows x d row-major in and out. */
 int katoann_gpu_rotate_rows(const float *d_in, uint32_t nrows, uint32_t d, const float *d_rot,
                             float *d_out, katoann_stream_t stream);
+
+/* d_rot (d x d, row j = basis j) in the k-major layout the search's query
+ * rotation reads: entry [k][j] = rot[j][k] for k < (d & ~15), j < (d & ~3),
+ * rows of round_up(d & ~3, 32) floats, zero beyond d & ~3. Made once per index
+ * (katoann_gpu_index.d_rotation_t) instead of once per search;
+ * katoann_gpu_rotation_kmajor_bytes(d) bytes at d_out. */
+size_t katoann_gpu_rotation_kmajor_bytes(uint32_t d);
+int katoann_gpu_rotation_kmajor(const float *d_rot, uint32_t d, float *d_out,
+                                katoann_stream_t stream);
 
 /* Global minimum and maximum of n floats, written to h_out[0..1] (host);
  * d_scratch is 8 bytes of device memory. Synchronous. Replaces the reduction

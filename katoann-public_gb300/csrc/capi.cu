@@ -26,6 +26,8 @@ int cuda_status(cudaError_t e, const char *what) {
 
 int rotate_rows(const float *in, uint32_t nrows, uint32_t d, const float *rot, float *out,
                 cudaStream_t st);
+size_t rotation_kmajor_bytes(uint32_t d);
+int rotation_kmajor(const float *rot, uint32_t d, float *out, cudaStream_t st);
 int minmax(const float *x, size_t n, uint32_t *d_keys, float *h_out, cudaStream_t st);
 int quantize_rows(const float *x, uint32_t nrows, uint32_t d, uint32_t dc, float lo,
                   double inv_step, uint32_t head, uint8_t *hi, uint8_t *lop, int64_t *norm,
@@ -83,6 +85,14 @@ int katoann_gpu_rotate_rows(const float *d_in, uint32_t nrows, uint32_t d, const
                             float *d_out, katoann_stream_t stream) {
   if (d == 0 || d > 4096) return kato::invalid("dimension must be 1 to 4096");
   return kato::rotate_rows(d_in, nrows, d, d_rot, d_out, as_stream(stream));
+}
+
+size_t katoann_gpu_rotation_kmajor_bytes(uint32_t d) { return kato::rotation_kmajor_bytes(d); }
+
+int katoann_gpu_rotation_kmajor(const float *d_rot, uint32_t d, float *d_out,
+                                katoann_stream_t stream) {
+  if (d == 0 || d > 4096) return kato::invalid("dimension must be 1 to 4096");
+  return kato::rotation_kmajor(d_rot, d, d_out, as_stream(stream));
 }
 
 int katoann_gpu_minmax(const float *d_x, size_t n, uint32_t *d_scratch, float *h_out,

@@ -81,6 +81,7 @@ struct Index::State {
   uint64_t source[4] = {0, 0, 0, 0};  // the index files the codes came from (code cache)
   uint32_t req_prefix = 0;            // the prefix_dims the load was asked for
   DevBuf rot, hi, lop, norm, hinorm, headnorm, ids, list_off, chi, clo, cnorm, chi16, clo16, cterm;
+  DevBuf rot_t;  // the rotation in the k-major layout the query rotation reads (made at load)
   katoann_gpu_index view{};
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
@@ -513,6 +514,12 @@ void Index::load_arrays(const IndexArrays &a, const LoadOptions &opt) {
 
 void Index::set_view(State &s) {
   const uint32_t d = s.dim, dc = s.dc, n = s.npts, L = s.nlist;
+  if (s.rotated && !s.rot_t.p && katoann_gpu_rotation_kmajor_bytes(d)) {
+    s.rot_t.alloc(katoann_gpu_rotation_kmajor_bytes(d));
+    gpu_check(katoann_gpu_rotation_kmajor(s.rot.as<float>(), d, s.rot_t.as<float>(),
+                                          reinterpret_cast<katoann_stream_t>(s.stream)));
+    cuda_check(cudaStreamSynchronize(s.stream), "load");
+  }
   katoann_gpu_index &v = s.view;
   v.dim = d;
   v.dc = dc;
@@ -538,6 +545,7 @@ void Index::set_view(State &s) {
   v.d_chi16 = s.chi16.as<uint16_t>();
   v.d_clo16 = s.clo16.as<uint16_t>();
   v.d_cterm = s.cterm.as<int64_t>();
+  v.d_rotation_t = s.rot_t.p ? s.rot_t.as<float>() : nullptr;
 }
 
 namespace {
@@ -757,7 +765,7 @@ size_t Index::memory_bytes() const {
   const State &s = *s_;
   return s.rot.n + s.hi.n + s.lop.n + s.norm.n + s.hinorm.n + s.headnorm.n + s.ids.n +
          s.list_off.n + s.chi.n + s.clo.n + s.cnorm.n + s.chi16.n + s.clo16.n + s.cterm.n +
-         s.sizes.size() * 4;
+         s.rot_t.n + s.sizes.size() * 4;
 }
 
 }  // namespace katoann

@@ -173,6 +173,44 @@ __global__ void __launch_bounds__(256) transpose_pad_kernel(const float *__restr
   }
 }
 
+// The same transpose with 16-byte accesses on both sides (d % 4 == 0, `in`
+// 16-byte aligned, ld % 32 == 0): 64 x 64 tiles, four float4 loads and four
+// float4 stores per thread.
+__global__ void __launch_bounds__(256) transpose_pad4_kernel(const float *__restrict__ in,
+                                                             uint32_t rows, uint32_t d, uint32_t kn,
+                                                             float *__restrict__ out, uint32_t ld) {
+  __shared__ float tile[64][65];
+  const uint32_t r0 = blockIdx.x * 64, k0 = blockIdx.y * 64;
+  const uint32_t t = threadIdx.x;
+#pragma unroll
+  for (uint32_t i = 0; i < 4; ++i) {
+    const uint32_t idx = t + 256 * i, rr = idx >> 4, k = k0 + (idx & 15) * 4;
+    float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (r0 + rr < rows && k < kn)
+      v = *reinterpret_cast<const float4 *>(in + static_cast<size_t>(r0 + rr) * d + k);
+    float *dst = &tile[rr][(idx & 15) * 4];
+    dst[0] = v.x, dst[1] = v.y, dst[2] = v.z, dst[3] = v.w;
+  }
+  __syncthreads();
+#pragma unroll
+  for (uint32_t i = 0; i < 4; ++i) {
+    const uint32_t idx = t + 256 * i, kk = idx >> 4, r = (idx & 15) * 4;
+    if (k0 + kk < kn && r0 + r < ld)
+      *reinterpret_cast<float4 *>(out + static_cast<size_t>(k0 + kk) * ld + r0 + r) =
+          make_float4(tile[r][kk], tile[r + 1][kk], tile[r + 2][kk], tile[r + 3][kk]);
+  }
+}
+
+// out (kn x ld, k-major) from in (rows x d, row-major), zero-padded rows.
+void transpose_pad(const float *in, uint32_t rows, uint32_t d, uint32_t kn, float *out, uint32_t ld,
+                   cudaStream_t st) {
+  if (d % 4 == 0 && ld % 32 == 0 && reinterpret_cast<uintptr_t>(in) % 16 == 0)
+    transpose_pad4_kernel<<<dim3(div_up(ld, 64), div_up(kn, 64)), 256, 0, st>>>(in, rows, d, kn, out,
+                                                                                ld);
+  else
+    transpose_pad_kernel<<<dim3(ld / 32, div_up(kn, 32)), 256, 0, st>>>(in, rows, d, kn, out, ld);
+}
+
 // The last d % 4 output columns: one chain over all d dimensions
 // (src/index.cpp:171-179, :247-257).
 __global__ void rotate_seq_kernel(const float *__restrict__ in, uint32_t nrows, uint32_t d,
@@ -272,16 +310,34 @@ size_t rotate_scratch_bytes(uint32_t nrows, uint32_t d) {
   return (ldx + ldr) * (d & ~15u) * 4 + 256;
 }
 
-int rotate_rows_kmajor(const float *in, uint32_t nrows, uint32_t d, const float *rot, void *scratch,
-                       float *out, cudaStream_t st) {
+size_t rotation_kmajor_bytes(uint32_t d) {
+  const size_t ldr = (static_cast<size_t>(d & ~3u) + 31) / 32 * 32;
+  return ldr * (d & ~15u) * 4;
+}
+
+int rotation_kmajor(const float *rot, uint32_t d, float *out, cudaStream_t st) {
+  const uint32_t d4 = d & ~3u, d16 = d & ~15u;
+  if (d16 == 0) return KATO_OK;
+  transpose_pad(rot, d4, d, d16, out, div_up(d4, 32) * 32, st);
+  KATO_LAUNCHED("transpose_pad_kernel");
+  return KATO_OK;
+}
+
+int rotate_rows_kmajor(const float *in, uint32_t nrows, uint32_t d, const float *rot,
+                       const float *rot_kmajor, void *scratch, float *out, cudaStream_t st) {
   if (nrows == 0) return KATO_OK;
   const uint32_t d4 = d & ~3u, d16 = d & ~15u;
   if (d16 == 0) return rotate_rows(in, nrows, d, rot, out, st);
   const uint32_t ldx = div_up(nrows, 32) * 32, ldr = div_up(d4, 32) * 32;
   float *xt = static_cast<float *>(scratch);
-  float *rt = xt + static_cast<size_t>(ldx) * d16;
-  transpose_pad_kernel<<<dim3(ldx / 32, div_up(d16, 32)), 256, 0, st>>>(in, nrows, d, d16, xt, ldx);
-  transpose_pad_kernel<<<dim3(ldr / 32, div_up(d16, 32)), 256, 0, st>>>(rot, d4, d, d16, rt, ldr);
+  const float *rt = rot_kmajor;
+  transpose_pad(in, nrows, d, d16, xt, ldx, st);
+  if (!rt) {  // no copy made at load: transpose the rotation here
+    float *t = xt + static_cast<size_t>(ldx) * d16;
+    transpose_pad(rot, d4, d, d16, t, ldr, st);
+    rt = t;
+  }
+  KATO_LAUNCHED("transpose_pad_kernel");
   dim3 grid(div_up(nrows, kRotRows), div_up(d4, kRotCols));
   rotate_lanes_kernel<true><<<grid, 256, 0, st>>>(in, nrows, d, rot, xt, ldx, rt, ldr, out);
   KATO_LAUNCHED("rotate_lanes_kernel");

@@ -707,8 +707,8 @@ int coarse_tc(const __half *ch, const __half *cl, const int64_t *cterm, uint32_t
               const __half *ql, const int64_t *qterm, uint32_t m, uint32_t dc, double step_sq,
               float *out, uint32_t *timeouts, unsigned long long *prof, cudaStream_t st);
 size_t rotate_scratch_bytes(uint32_t nrows, uint32_t d);
-int rotate_rows_kmajor(const float *in, uint32_t nrows, uint32_t d, const float *rot, void *scratch,
-                       float *out, cudaStream_t st);
+int rotate_rows_kmajor(const float *in, uint32_t nrows, uint32_t d, const float *rot,
+                       const float *rot_kmajor, void *scratch, float *out, cudaStream_t st);
 int select_topp_ex(const float *dists, uint32_t nq, uint32_t n, uint32_t p, uint32_t stride,
                    uint32_t *probed, unsigned long long *tie_count, const uint32_t *only,
                    uint32_t only_above, cudaStream_t st);
@@ -855,15 +855,21 @@ int coarse_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
   // 1. rotation and quantization of the queries (src/index.cpp:895-899, :917-943)
   const float *src = queries;
   if (ix->rotated) {
-    if ((rc = rotate_rows_kmajor(queries, nq, ix->dim, ix->d_rotation, ws + pl.off_rot, fq, st)))
+    if ((rc = rotate_rows_kmajor(queries, nq, ix->dim, ix->d_rotation, ix->d_rotation_t,
+                                 ws + pl.off_rot, fq, st)))
       return rc;
     src = fq;
   }
   if ((rc = quantize_rows(src, nq, ix->dim, dc, ix->lo, ix->inv_step, ix->head_dims, qhi, qlo, qn,
                           qhn, qh0, st)))
     return rc;
-  // rotation (two transposes and the product, plus the d % 4 columns), quantize, coarse, select
-  g_launches += (ix->rotated ? ((ix->dim & ~15u) ? 3 : 1) + ((ix->dim & 3) ? 1 : 0) : 0) + 1 + 2;
+  // rotation (the queries' transpose, the rotation's unless the index holds
+  // its k-major copy, and the product, plus the d % 4 columns), quantize,
+  // coarse, select
+  g_launches += (ix->rotated ? ((ix->dim & ~15u) ? (ix->d_rotation_t ? 2 : 3) : 1) +
+                                   ((ix->dim & 3) ? 1 : 0)
+                             : 0) +
+                1 + 2;
   mark(tm, 1, st);
   // 2. coarse product and top-nprobe (:846-877)
   if (pl.coarse_tc) {

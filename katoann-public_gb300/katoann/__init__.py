@@ -190,7 +190,8 @@ class GpuIndexView(C.Structure):
                 ("d_norm", C.c_void_p), ("d_hinorm", C.c_void_p), ("d_headnorm", C.c_void_p),
                 ("d_ids", C.c_void_p), ("d_list_off", C.c_void_p), ("d_chi", C.c_void_p),
                 ("d_clo", C.c_void_p), ("d_cnorm", C.c_void_p), ("d_chi16", C.c_void_p),
-                ("d_clo16", C.c_void_p), ("d_cterm", C.c_void_p)]
+                ("d_clo16", C.c_void_p), ("d_cterm", C.c_void_p),
+                ("d_rotation_t", C.c_void_p)]
 
 
 def device_to_host(ptr: int, nbytes: int, dtype) -> np.ndarray:

@@ -64,9 +64,18 @@ def test_sq16_kernels_on_reference_grid(torch):
 
 
 def test_dist_values_on_device(torch):
+    """The device's conversion (its single-precision path and the integer path
+    it falls back to) against float(double(l2) * step_sq), on random values and
+    on values a few units from float rounding midpoints."""
+    from test_dist_value_single import SCALES, near_midpoints
     rng = np.random.default_rng(3)
-    for step_sq in (1.76061467e-08, 2.98203776e-09, 1.0 / 65535.0 ** 2):
-        l2 = rng.integers(0, 1 << 45, 1 << 20, dtype=np.int64)
+    for step_sq in SCALES + [1.0 / 65535.0 ** 2 * 3.7]:
+        top = (1 << 46) - 1
+        l2 = np.concatenate([rng.integers(0, 1 << 45, 1 << 20, dtype=np.int64),
+                             np.exp2(rng.uniform(0, 46, 1 << 18)).astype(np.int64),
+                             near_midpoints(rng, step_sq, 1 << 16, max(step_sq * 64, 1e-30),
+                                            min(top * step_sq, 3e38))])
+        l2 = np.clip(l2, 0, top)
         l2[:64] = np.arange(64)
         d = torch.from_numpy(l2).cuda()
         out = torch.empty(len(l2), dtype=torch.float32, device="cuda")
@@ -85,6 +94,59 @@ def test_rotation_matches_reference_arithmetic(torch, d):
         xd, rd = torch.from_numpy(x).cuda(), torch.from_numpy(r).cuda()
         check(gpu().katoann_gpu_rotate_rows(dptr(xd), nrows, d, dptr(rd), dptr(out), None))
         assert np.array_equal(out.cpu().numpy(), oracle.rotate_with(x, r)), nrows
+
+
+def test_rotation_kmajor_layout(torch):
+    """katoann_gpu_rotation_kmajor: entry [k][j] = rot[j][k] for k < d & ~15,
+    j < d & ~3, rows padded with zeros to a multiple of 32 (both the 16-byte
+    and the 4-byte transpose)."""
+    g = gpu()
+    g.katoann_gpu_rotation_kmajor_bytes.restype = C.c_size_t
+    g.katoann_gpu_rotation_kmajor_bytes.argtypes = [C.c_uint32]
+    g.katoann_gpu_rotation_kmajor.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]
+    rng = np.random.default_rng(7)
+    for d in (4, 15, 16, 17, 33, 64, 100, 102, 1024):
+        r = rng.standard_normal((d, d)).astype(np.float32)
+        d4, d16 = d & ~3, d & ~15
+        ldr = (d4 + 31) // 32 * 32
+        nb = g.katoann_gpu_rotation_kmajor_bytes(d)
+        assert nb == ldr * d16 * 4, d
+        if nb == 0:
+            continue
+        rd = torch.from_numpy(r).cuda()
+        out = torch.full((nb // 4,), float("nan"), dtype=torch.float32, device="cuda")
+        check(g.katoann_gpu_rotation_kmajor(dptr(rd), d, dptr(out), None))
+        want = np.zeros((d16, ldr), np.float32)
+        want[:, :d4] = r[:d4, :d16].T
+        assert np.array_equal(out.cpu().numpy().reshape(d16, ldr), want), d
+
+
+@pytest.mark.parametrize("name", ["d1024", "d100", "d102", "pca"])
+def test_search_with_and_without_kmajor_rotation(torch, name):
+    """The host library gives the kernels the rotation's k-major copy; a view
+    without it (NULL) transposes per search. Both give the same bits."""
+    import katoann
+    spec, z, prefix, queries = fixture(name)
+    idx = katoann.Index()
+    idx.load(prefix)
+    v = view_of(idx)
+    assert v.rotated and v.d_rotation_t
+    bare = type(v).from_buffer_copy(v)
+    bare.d_rotation_t = None
+    nq, k, S = len(queries), 10, 32
+    p = min(8, v.nlist)
+    q = torch.from_numpy(np.ascontiguousarray(queries, np.float32)).cuda()
+    got = []
+    for view in (v, bare):
+        ws_bytes = gpu().katoann_gpu_search_workspace(C.addressof(view), nq, k, p, 1, S)
+        ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
+        ids = torch.empty((nq, k), dtype=torch.int32, device="cuda")
+        dists = torch.empty((nq, k), dtype=torch.float32, device="cuda")
+        check(gpu().katoann_gpu_search(C.addressof(view), dptr(q), nq, k, p, 1, S, nq, dptr(ws),
+                                       ws_bytes, dptr(ids), dptr(dists), None))
+        torch.cuda.synchronize()
+        got.append((ids.cpu().numpy(), dists.cpu().numpy()))
+    assert np.array_equal(got[0][0], got[1][0]) and np.array_equal(got[0][1], got[1][1])
 
 
 @pytest.mark.parametrize("name", FIXTURES)
