@@ -47,6 +47,9 @@ struct ServerStats {
   uint32_t peak_in_flight = 0;
   size_t peak_hbm_bytes = 0;      // device memory held by in-flight batches at most
   double mean_batch = 0;
+  // where a batch's time goes, at most (since construction or reset_peaks):
+  double max_enqueue_ms = 0;      // host: staging the queries and enqueuing copies and kernels
+  double max_batch_gpu_ms = 0;    // device: the batch's copies and search, on its stream
 };
 
 struct LoadReport {
@@ -56,6 +59,9 @@ struct LoadReport {
   double mean_batch = 0, mean_nprobe = 0;
   uint32_t peak_in_flight = 0;
   size_t peak_hbm_bytes = 0;
+  // a latency outlier's source: the client behind its schedule, a slow host
+  // enqueue, or a slow batch on the device (this run's maxima)
+  double max_lag_ms = 0, max_enqueue_ms = 0, max_batch_gpu_ms = 0;
 };
 
 class Server;
@@ -87,6 +93,9 @@ class Server {
   // Blocks until every submitted request is done.
   void drain();
   ServerStats stats() const;
+  // Restarts the maxima of stats(): in-flight batches and device memory (from
+  // their current values), enqueue and batch times (from zero).
+  void reset_peaks();
 
   struct Impl;
 

@@ -143,12 +143,14 @@ int katoann_server_wait(void *server, uint64_t id, uint32_t *ids, float *dists,
 int katoann_server_poll(void *server, uint64_t id, uint32_t *ids, float *dists,
                         uint32_t *nprobe, double *latency_ms, int *done);
 int katoann_server_drain(void *server);
-/* stats[5] = {requests, batches, peak_in_flight, peak_hbm_bytes, mean_batch x 1000} */
+/* stats[7] = {requests, batches, peak_in_flight, peak_hbm_bytes, mean_batch x 1000,
+ * max_enqueue_ms x 1000, max_batch_gpu_ms x 1000} */
 int katoann_server_stats(void *server, uint64_t *stats);
 /* katoann::run_load: n Poisson arrivals at `rate` from a native client, queries
- * round-robin from queries (nq x dim), k uniform over kmix. report[10] =
+ * round-robin from queries (nq x dim), k uniform over kmix. report[13] =
  * {achieved_qps, p50_ms, p95_ms, p99_ms, max_ms, batches, mean_batch,
- * mean_nprobe, peak_in_flight, peak_hbm_bytes}. */
+ * mean_nprobe, peak_in_flight, peak_hbm_bytes, max_lag_ms, max_enqueue_ms,
+ * max_batch_gpu_ms}. */
 int katoann_server_load(void *server, const float *queries, uint32_t nq, uint32_t dim, double rate,
                         uint32_t n, const uint32_t *kmix, uint32_t nk, uint64_t seed,
                         double *report);

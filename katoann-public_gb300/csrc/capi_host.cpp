@@ -265,11 +265,12 @@ int katoann_server_load(void *server, const float *queries, uint32_t nq, uint32_
     for (uint32_t i = 0; i < nq; ++i) pool[i] = i;
     const katoann::LoadReport r = katoann::run_load(*SV(server), queries, dim, pool, rate, n,
                                                     std::vector<uint32_t>(kmix, kmix + nk), seed);
-    const double v[10] = {r.achieved_qps, r.p50_ms,      r.p95_ms,
-                          r.p99_ms,       r.max_ms,      static_cast<double>(r.batches),
-                          r.mean_batch,   r.mean_nprobe, static_cast<double>(r.peak_in_flight),
-                          static_cast<double>(r.peak_hbm_bytes)};
-    std::copy(v, v + 10, report);
+    const double v[13] = {r.achieved_qps,   r.p50_ms,      r.p95_ms,
+                          r.p99_ms,         r.max_ms,      static_cast<double>(r.batches),
+                          r.mean_batch,     r.mean_nprobe, static_cast<double>(r.peak_in_flight),
+                          static_cast<double>(r.peak_hbm_bytes), r.max_lag_ms,
+                          r.max_enqueue_ms, r.max_batch_gpu_ms};
+    std::copy(v, v + 13, report);
   });
 }
 
@@ -281,6 +282,8 @@ int katoann_server_stats(void *server, uint64_t *stats) {
     stats[2] = s.peak_in_flight;
     stats[3] = s.peak_hbm_bytes;
     stats[4] = static_cast<uint64_t>(s.mean_batch * 1000.0);
+    stats[5] = static_cast<uint64_t>(s.max_enqueue_ms * 1000.0);
+    stats[6] = static_cast<uint64_t>(s.max_batch_gpu_ms * 1000.0);
   });
 }
 

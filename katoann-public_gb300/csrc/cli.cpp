@@ -368,11 +368,12 @@ int cmd_load(const Args &a) {
               "\"achieved_qps\": %.1f, \"p50_ms\": %.2f, \"p95_ms\": %.2f, \"p99_ms\": %.2f, "
               "\"max_ms\": %.2f, \"batches\": %llu, \"mean_batch\": %.1f, \"in_flight\": %u, "
               "\"peak_in_flight\": %u, \"peak_hbm_gb\": %.3f, \"learned\": %s, "
-              "\"mean_nprobe\": %.2f}\n",
+              "\"mean_nprobe\": %.2f, \"max_lag_ms\": %.2f, \"max_enqueue_ms\": %.2f, "
+              "\"max_batch_gpu_ms\": %.2f}\n",
               rate, n, so.nprobe, r.achieved_qps, r.p50_ms, r.p95_ms, r.p99_ms, r.max_ms,
               static_cast<unsigned long long>(r.batches), r.mean_batch, so.max_in_flight,
               r.peak_in_flight, r.peak_hbm_bytes / 1e9, so.budget ? "true" : "false",
-              r.mean_nprobe);
+              r.mean_nprobe, r.max_lag_ms, r.max_enqueue_ms, r.max_batch_gpu_ms);
   return 0;
 }
 

@@ -90,6 +90,7 @@ class Pool {
   }
   unsigned char *at(size_t off) const { return static_cast<unsigned char *>(base_) + off; }
   size_t peak() const { return peak_; }
+  void reset_peak() { peak_ = used_; }
 
  private:
   void *base_ = nullptr;
@@ -111,7 +112,8 @@ struct Entry {
 
 struct Slot {
   cudaStream_t stream = nullptr;
-  cudaEvent_t event = nullptr;
+  cudaEvent_t start = nullptr;  // recorded before the batch's copies (timing)
+  cudaEvent_t event = nullptr;  // after its results' copies (timing, blocking wait)
   float *hq = nullptr;       // pinned: max_batch x dim
   uint32_t *hids = nullptr;  // pinned: max_batch x max_k
   float *hd = nullptr;
@@ -125,6 +127,7 @@ struct Batch {
   size_t off, bytes;
   std::vector<Request> reqs;
   std::string err;           // a launch that failed
+  double enqueue_ms = 0;     // host time of launch()
 };
 
 }  // namespace
@@ -146,6 +149,7 @@ struct Server::Impl {
   std::deque<Batch> launched;
   uint64_t next_id = 1, pending = 0, submitted = 0, nbatches = 0, batched = 0;
   uint32_t in_flight = 0, peak_in_flight = 0;
+  double max_enqueue_ms = 0, max_batch_gpu_ms = 0;
   bool stop = false;
   std::thread dispatcher, completer;
 
@@ -175,6 +179,12 @@ struct Server::Impl {
   }
 
   void launch(Batch &b) {
+    const auto h0 = Clock::now();
+    struct Timed {  // enqueue time on every return path
+      Batch &b;
+      Clock::time_point h0;
+      ~Timed() { b.enqueue_ms = std::chrono::duration<double, std::milli>(Clock::now() - h0).count(); }
+    } timed{b, h0};
     Slot &s = *b.slot;
     const uint32_t n = b.n, k = b.k;
     for (uint32_t i = 0; i < n; ++i)
@@ -188,7 +198,12 @@ struct Server::Impl {
     uint32_t *dnp = reinterpret_cast<uint32_t *>(reinterpret_cast<unsigned char *>(dd) +
                                                  align256(size_t(n) * k * 4));
     const auto st = reinterpret_cast<katoann_stream_t>(s.stream);
-    cudaError_t e = cudaMemcpyAsync(dq, s.hq, size_t(n) * dim * 4, cudaMemcpyHostToDevice, s.stream);
+    cudaError_t e = cudaEventRecord(s.start, s.stream);
+    if (e != cudaSuccess) {
+      b.err = std::string("cudaEventRecord: ") + cudaGetErrorString(e);
+      return;
+    }
+    e = cudaMemcpyAsync(dq, s.hq, size_t(n) * dim * 4, cudaMemcpyHostToDevice, s.stream);
     if (e != cudaSuccess) {
       b.err = std::string("copy queries: ") + cudaGetErrorString(e);
       return;
@@ -268,6 +283,7 @@ struct Server::Impl {
       lk.unlock();
       launch(b);  // no lock held while the host copies and enqueues
       lk.lock();
+      max_enqueue_ms = std::max(max_enqueue_ms, b.enqueue_ms);
       launched.push_back(std::move(b));
       cv_complete.notify_one();
     }
@@ -284,9 +300,12 @@ struct Server::Impl {
       launched.pop_front();
       lk.unlock();
       std::string err = b.err;
+      float gpu_ms = 0;
       if (err.empty()) {
         const cudaError_t e = cudaEventSynchronize(b.slot->event);
         if (e != cudaSuccess) err = std::string("search: ") + cudaGetErrorString(e);
+        else if (cudaEventElapsedTime(&gpu_ms, b.slot->start, b.slot->event) != cudaSuccess)
+          gpu_ms = 0;
       } else {
         cudaStreamSynchronize(b.slot->stream);  // whatever was enqueued before the failure
       }
@@ -308,6 +327,7 @@ struct Server::Impl {
         en.res = std::move(res[i]);
       }
       pool.give(b.off, b.bytes);
+      max_batch_gpu_ms = std::max(max_batch_gpu_ms, static_cast<double>(gpu_ms));
       b.slot->busy = false;
       --in_flight;
       cv_done.notify_all();
@@ -349,8 +369,8 @@ Server::Server(const Index &index, const ServerOptions &opt) : m_(new Impl) {
   m.slots.resize(opt.max_in_flight);
   for (Slot &s : m.slots) {
     cuda_check(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking), "server stream");
-    cuda_check(cudaEventCreateWithFlags(&s.event, cudaEventDisableTiming | cudaEventBlockingSync),
-               "server event");
+    cuda_check(cudaEventCreate(&s.start), "server event");
+    cuda_check(cudaEventCreateWithFlags(&s.event, cudaEventBlockingSync), "server event");
     cuda_check(cudaMallocHost(&s.hq, size_t(m.max_batch) * m.dim * 4), "server pinned queries");
     cuda_check(cudaMallocHost(&s.hids, size_t(m.max_batch) * opt.max_k * 4), "server pinned ids");
     cuda_check(cudaMallocHost(&s.hd, size_t(m.max_batch) * opt.max_k * 4), "server pinned dists");
@@ -372,6 +392,7 @@ Server::~Server() {
   if (m.completer.joinable()) m.completer.join();
   for (Slot &s : m.slots) {
     if (s.event) cudaEventDestroy(s.event);
+    if (s.start) cudaEventDestroy(s.start);
     if (s.stream) cudaStreamDestroy(s.stream);
     if (s.hq) cudaFreeHost(s.hq);
     if (s.hids) cudaFreeHost(s.hids);
@@ -448,6 +469,7 @@ LoadReport run_load(Server &server, const float *queries, uint32_t dim,
     kof[i] = kmix[rng() % kmix.size()];
   }
   const ServerStats before = server.stats();
+  server.reset_peaks();
   std::vector<uint64_t> rid(n);
   const auto start = Clock::now();
   auto since = [&] { return std::chrono::duration<double>(Clock::now() - start).count(); };
@@ -486,6 +508,9 @@ LoadReport run_load(Server &server, const float *queries, uint32_t dim,
   rep.mean_nprobe = probes / n;
   rep.peak_in_flight = st.peak_in_flight;
   rep.peak_hbm_bytes = st.peak_hbm_bytes;
+  rep.max_lag_ms = *std::max_element(lag.begin(), lag.end()) * 1e3;
+  rep.max_enqueue_ms = st.max_enqueue_ms;
+  rep.max_batch_gpu_ms = st.max_batch_gpu_ms;
   return rep;
 }
 
@@ -498,7 +523,18 @@ ServerStats Server::stats() const {
   s.peak_in_flight = m.peak_in_flight;
   s.peak_hbm_bytes = m.pool.peak();
   s.mean_batch = m.nbatches ? double(m.batched) / double(m.nbatches) : 0;
+  s.max_enqueue_ms = m.max_enqueue_ms;
+  s.max_batch_gpu_ms = m.max_batch_gpu_ms;
   return s;
+}
+
+void Server::reset_peaks() {
+  Impl &m = *m_;
+  std::lock_guard<std::mutex> lk(m.mu);
+  m.peak_in_flight = m.in_flight;
+  m.pool.reset_peak();
+  m.max_enqueue_ms = 0;
+  m.max_batch_gpu_ms = 0;
 }
 
 }  // namespace katoann

@@ -661,18 +661,20 @@ class Server:
         if self.normalized:
             q = normalize_rows(q)
         ks = np.ascontiguousarray(kmix, dtype=np.uint32)
-        r = np.zeros(10, np.float64)
+        r = np.zeros(13, np.float64)
         _check(_lib.katoann_server_load(self._h, _ptr(q), q.shape[0], q.shape[1], float(rate),
                                         requests, _ptr(ks), ks.size, seed, _ptr(r)))
         keys = ("achieved_qps", "p50_ms", "p95_ms", "p99_ms", "max_ms", "batches", "mean_batch",
-                "mean_nprobe", "peak_in_flight", "peak_hbm_bytes")
+                "mean_nprobe", "peak_in_flight", "peak_hbm_bytes", "max_lag_ms",
+                "max_enqueue_ms", "max_batch_gpu_ms")
         out = dict(zip(keys, map(float, r)))
         for key in ("batches", "peak_in_flight", "peak_hbm_bytes"):
             out[key] = int(out[key])
         return out
 
     def stats(self) -> dict:
-        s = np.zeros(5, np.uint64)
+        s = np.zeros(7, np.uint64)
         _check(_lib.katoann_server_stats(self._h, _ptr(s)))
         return dict(requests=int(s[0]), batches=int(s[1]), peak_in_flight=int(s[2]),
-                    peak_hbm_bytes=int(s[3]), mean_batch=float(s[4]) / 1000.0)
+                    peak_hbm_bytes=int(s[3]), mean_batch=float(s[4]) / 1000.0,
+                    max_enqueue_ms=float(s[5]) / 1000.0, max_batch_gpu_ms=float(s[6]) / 1000.0)

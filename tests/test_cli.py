@@ -141,3 +141,7 @@ def test_load_serves_mixed_k_with_a_learned_budget(tmp_path):
     x = json_lines(p.stdout)[-1]
     assert x["requests"] == 2000 and x["learned"] is True and x["in_flight"] == 2
     assert 0 < x["p50_ms"] <= x["p99_ms"] and 1 <= x["mean_nprobe"] <= 32
+    # where the time went: every batch took device time; the client and the
+    # enqueue stay below the slowest request
+    assert 0 < x["max_batch_gpu_ms"] <= x["max_ms"] and 0 < x["max_enqueue_ms"]
+    assert 0 <= x["max_lag_ms"] <= x["max_ms"]

@@ -77,6 +77,7 @@ def test_results_in_the_mix_equal_alone(tmp_path, learned):
     stats = server.stats()
     assert stats["requests"] == len(queries) and stats["batches"] >= len(queries) / 64
     assert stats["peak_in_flight"] >= 1
+    assert stats["max_batch_gpu_ms"] > 0 and stats["max_enqueue_ms"] > 0
     assert all(r[3] > 0 for r in res)
     _check_alone(idx, queries, ks, res, nprobe=32, survivors=32, budget=model, threshold=0.9)
 
