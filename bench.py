@@ -273,9 +273,9 @@ class ClockSampler:
 SEED_ROWS = 1024  # rows behind each query's seed bound (the library default for survivors <= 128)
 
 # DRAM bytes per 128-row tile of the tensor-core ranking kernel, from one ncu
-# capture on the 2M x 1024 case (profiles/rank_tc_traffic_2m.md): 535.6 MB over
-# 20,278 tiles. The traffic of a launch scales with the tiles it scores.
-RANK_TC_DRAM_BYTES_PER_TILE = 535.6e6 / 20278
+# capture on the 2M x 1024 case (profiles/rank_tc_traffic_2m.md): 536.0 MB over
+# 20,279 tiles. The traffic of a launch scales with the tiles it scores.
+RANK_TC_DRAM_BYTES_PER_TILE = 536.0e6 / 20279
 
 
 def phase_work(phase: str, B: int, L: int, dc: int, d: int, nprobe: int, S: int, head: int,
