@@ -578,9 +578,6 @@ __device__ __forceinline__ uint32_t row_dot(const uint8_t *row, const uint32_t *
 // pre(i) - a per-row value the callback needs (e.g. the row's norm) - is
 // loaded at the start of the batch by the lane that later calls
 // f(i, dot, pre(i)), so that it arrives with the rows instead of after them.
-struct NoPre {
-  __device__ int64_t operator()(uint32_t) const { return 0; }
-};
 
 template <uint32_t G, typename F, typename Pre>
 __device__ __forceinline__ void rows_split(const uint8_t *__restrict__ x, uint32_t dc, uint32_t h,
@@ -633,10 +630,10 @@ __device__ __forceinline__ void rows_split(const uint8_t *__restrict__ x, uint32
   }
 }
 
-template <typename F, typename Pre = NoPre>
+template <typename F, typename Pre>
 __device__ __forceinline__ void for_rows_split(const uint8_t *__restrict__ x, uint32_t dc, uint32_t h,
                                                const uint32_t *qw, uint32_t r0, uint32_t n, F f,
-                                               Pre pre = Pre{}) {
+                                               Pre pre) {
   const uint32_t g = min(32u, h / 16);
   if (g == 16) rows_split<16>(x, dc, h, qw, r0, n, pre, f);
   else if (g == 32) rows_split<32>(x, dc, h, qw, r0, n, pre, f);

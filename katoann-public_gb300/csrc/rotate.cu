@@ -88,19 +88,19 @@ __global__ void __launch_bounds__(256, 2) rotate_lanes_kernel(const float *__res
         cp_async16(&rs[buf][c * kRotStride + q], rt + static_cast<size_t>(k0 + c) * ldr + j0 + q);
       }
       asm volatile("cp.async.commit_group;" ::: "memory");
-      return;
+    } else {
+      for (int idx = t; idx < kRotRows * kRotK; idx += 256) {
+        const int r = idx / kRotK, c = idx % kRotK;
+        const uint32_t gk = k0 + c;
+        const uint32_t gi = i0 + r, gj = j0 + r;
+        const bool okx = gi < nrows && gk < d16, okr = gj < d4 && gk < d16;
+        cp_async4(&xs[buf][c * kRotStride + r], okx ? in + static_cast<size_t>(gi) * d + gk : in,
+                  okx ? 4u : 0u);
+        cp_async4(&rs[buf][c * kRotStride + r], okr ? rot + static_cast<size_t>(gj) * d + gk : rot,
+                  okr ? 4u : 0u);
+      }
+      asm volatile("cp.async.commit_group;" ::: "memory");
     }
-    for (int idx = t; idx < kRotRows * kRotK; idx += 256) {
-      const int r = idx / kRotK, c = idx % kRotK;
-      const uint32_t gk = k0 + c;
-      const uint32_t gi = i0 + r, gj = j0 + r;
-      const bool okx = gi < nrows && gk < d16, okr = gj < d4 && gk < d16;
-      cp_async4(&xs[buf][c * kRotStride + r], okx ? in + static_cast<size_t>(gi) * d + gk : in,
-                okx ? 4u : 0u);
-      cp_async4(&rs[buf][c * kRotStride + r], okr ? rot + static_cast<size_t>(gj) * d + gk : rot,
-                okr ? 4u : 0u);
-    }
-    asm volatile("cp.async.commit_group;" ::: "memory");
   };
   int buf = 0;
   if (d16) stage(0, 0);
