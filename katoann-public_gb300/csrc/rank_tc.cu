@@ -954,20 +954,35 @@ __global__ void __launch_bounds__(1024) tc_scan_kernel(uint32_t *__restrict__ co
   }
 }
 
+// tile_hist (optional, 6 counters): the tiles of the items with 1-2, 3-4,
+// 5-8, 9-16, 17-32 and 33-64 queries.
 __global__ void tc_expand_kernel(const uint32_t *__restrict__ list_off, const uint32_t *__restrict__ counts,
-                                 uint32_t L, uint32_t N, uint32_t beta,
-                                 const uint32_t *__restrict__ nitems, TcItem *__restrict__ items,
-                                 uint32_t *__restrict__ tile_off, uint32_t *__restrict__ cost_off) {
+                                 const uint32_t *__restrict__ cnt, uint32_t L, uint32_t N,
+                                 uint32_t beta, const uint32_t *__restrict__ nitems,
+                                 TcItem *__restrict__ items, uint32_t *__restrict__ tile_off,
+                                 uint32_t *__restrict__ cost_off,
+                                 unsigned long long *__restrict__ tile_hist) {
   const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= L) return;
-  const uint32_t i0 = counts[c], i1 = c + 1 < L ? counts[c + 1] : *nitems;
-  const uint32_t tiles = (list_off[c + 1] - list_off[c] + kTcRows - 1) / kTcRows;
-  const uint32_t tb = counts[L + 1 + c];
-  for (uint32_t j = 0; j < i1 - i0; ++j) {
-    items[i0 + j] = TcItem{c, j * N, list_off[c], list_off[c + 1] - list_off[c]};
-    tile_off[i0 + j] = tb + j * tiles;
-    // every item before the last of its list is full (width N)
-    if (cost_off) cost_off[i0 + j] = counts[2 * (L + 1) + c] + j * tiles * (64 + beta * N);
+  uint32_t hist[6] = {0, 0, 0, 0, 0, 0};
+  if (c < L) {
+    const uint32_t i0 = counts[c], i1 = c + 1 < L ? counts[c + 1] : *nitems;
+    const uint32_t tiles = (list_off[c + 1] - list_off[c] + kTcRows - 1) / kTcRows;
+    const uint32_t tb = counts[L + 1 + c];
+    for (uint32_t j = 0; j < i1 - i0; ++j) {
+      items[i0 + j] = TcItem{c, j * N, list_off[c], list_off[c + 1] - list_off[c]};
+      tile_off[i0 + j] = tb + j * tiles;
+      // every item before the last of its list is full (width N)
+      if (cost_off) cost_off[i0 + j] = counts[2 * (L + 1) + c] + j * tiles * (64 + beta * N);
+      const uint32_t ne = min(N, cnt[c] - j * N);
+      hist[ne <= 2 ? 0 : ne <= 4 ? 1 : ne <= 8 ? 2 : ne <= 16 ? 3 : ne <= 32 ? 4 : 5] += tiles;
+    }
+  }
+  if (tile_hist) {  // whole warps take part: one add per warp and bin
+#pragma unroll
+    for (int b = 0; b < 6; ++b) {
+      const uint32_t v = __reduce_add_sync(0xffffffffu, hist[b]);
+      if ((threadIdx.x & 31) == 0 && v) atomicAdd(tile_hist + b, static_cast<unsigned long long>(v));
+    }
   }
 }
 
@@ -1102,13 +1117,13 @@ int rank_seed(const uint8_t *xhi, const int64_t *xnorm, const uint8_t *qhi, cons
 int rank_tc_prepare(const uint32_t *cnt, const uint32_t *list_off, uint32_t L, uint32_t N,
                     uint32_t B, uint32_t beta, uint32_t *scratch, TcItem *items,
                     uint32_t *tile_off, uint32_t *cost_off, uint32_t *nitems, uint32_t *qcount,
-                    uint32_t *qfill, cudaStream_t st) {
+                    uint32_t *qfill, unsigned long long *tile_hist, cudaStream_t st) {
   uint32_t *co = beta ? cost_off : nullptr;
   tc_count_kernel<<<div_up(std::max(std::max(L, B), 1u), 256), 256, 0, st>>>(
       cnt, list_off, L, N, B, beta, scratch, qcount, qfill);
   tc_scan_kernel<<<1, 1024, 0, st>>>(scratch, L, nitems, tile_off, co);
-  tc_expand_kernel<<<div_up(L, 256), 256, 0, st>>>(list_off, scratch, L, N, beta, nitems, items,
-                                                   tile_off, co);
+  tc_expand_kernel<<<div_up(L, 256), 256, 0, st>>>(list_off, scratch, cnt, L, N, beta, nitems,
+                                                   items, tile_off, co, tile_hist);
   KATO_LAUNCHED("ranking work preparation");
   return KATO_OK;
 }

@@ -99,7 +99,7 @@ int rank_seed(const uint8_t *xhi, const int64_t *xnorm, const uint8_t *qhi, cons
 int rank_tc_prepare(const uint32_t *cnt, const uint32_t *list_off, uint32_t L, uint32_t N,
                     uint32_t B, uint32_t beta, uint32_t *scratch, TcItem *items,
                     uint32_t *tile_off, uint32_t *cost_off, uint32_t *nitems, uint32_t *qcount,
-                    uint32_t *qfill, cudaStream_t st);
+                    uint32_t *qfill, unsigned long long *tile_hist, cudaStream_t st);
 // Process-wide knobs of the pass (0 = default): the largest item width and
 // the cost weight of the CTA split.
 extern std::atomic<uint32_t> g_tc_width, g_tc_beta;

@@ -985,7 +985,7 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
     uint32_t *cost_off = reinterpret_cast<uint32_t *>(ws + pl.off_costoff);
     if ((rc = rank_tc_prepare(cnt, ix->d_list_off, L, pl.tcs.N, nq, pl.beta,
                               reinterpret_cast<uint32_t *>(ws + pl.off_tcscratch), items, tile_off,
-                              cost_off, nitems, qcount, qfill, st)))
+                              cost_off, nitems, qcount, qfill, stats + 40, st)))
       return rc;
     RankTcArgs T{};
     T.qhi = qhi;

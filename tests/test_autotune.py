@@ -75,3 +75,45 @@ def test_autotune_keeps_results(tmp_path):
         lib.katoann_gpu_set_rank_schedule(0)
         lib.katoann_gpu_set_rank_width(0)
         lib.katoann_gpu_set_seed_rows(0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("width", [64, 32])
+def test_tile_histogram_counts_every_item(tmp_path, width):
+    """search_stats()["ranking_tiles_by_queries"]: the ranking pass's tiles by
+    the query count of their work item, recomputed from the oracle's probes
+    (an item is up to `width` of the queries probing one list; every item
+    scores all of its list's 128-row tiles)."""
+    import katoann
+    from _gpu import gpu
+    lib = gpu()
+    prefix = str(tmp_path / "x")
+    queries, _ = synth.materialize(SPEC, prefix)
+    idx = katoann.Index()
+    idx.load(prefix)
+    ref = oracle.OracleIndex(prefix)
+    knobs = (C.c_uint32 * 3)()
+    lib.katoann_gpu_rank_knobs(knobs)
+    p = 12
+    try:
+        assert lib.katoann_gpu_set_rank_width(width) == 0
+        idx.search(queries, k=10, nprobe=p, survivors=32)
+        st = idx.search_stats()
+    finally:
+        assert lib.katoann_gpu_set_rank_width(knobs[2]) == 0
+    q = ref.quantize(ref.rotate(queries))
+    probed = ref.coarse(q["hi"], q["lo"], q["norm"], p)
+    cnt = np.bincount(probed.ravel().astype(np.int64), minlength=ref.nlist)
+    sizes = np.diff(ref.list_offsets().astype(np.int64))
+    want = np.zeros(6, np.int64)
+    for c in range(ref.nlist):
+        if sizes[c] == 0:
+            continue
+        tiles = -(-sizes[c] // 128)
+        for j in range(-(-cnt[c] // width)):
+            ne = min(width, cnt[c] - j * width)
+            want[0 if ne <= 2 else 1 if ne <= 4 else 2 if ne <= 8 else 3 if ne <= 16 else
+                 4 if ne <= 32 else 5] += tiles
+    got = np.array(list(st["ranking_tiles_by_queries"].values()), np.int64)
+    assert np.array_equal(got, want), (got, want)
+    assert got.sum() == st["ranking_tiles"]
