@@ -273,16 +273,8 @@ __global__ void __launch_bounds__(kThreads, 1)
 }
 
 int encode_plane(CUtensorMap *map, const __half *base, uint32_t rows, uint32_t dc, uint32_t box_rows) {
-  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-  if (!encode) {
-    cudaDriverEntryPointQueryResult q{};
-    void *fn = nullptr;
-    KATO_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
-                                               cudaEnableDefault, &q));
-    if (q != cudaDriverEntryPointSuccess || !fn)
-      return cuda_status(cudaErrorNotSupported, "cuTensorMapEncodeTiled");
-    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
-  }
+  const PFN_cuTensorMapEncodeTiled_v12000 encode = tc::tensor_map_encoder();
+  if (!encode) return cuda_status(cudaErrorNotSupported, "cuTensorMapEncodeTiled");
   const cuuint64_t dims[2] = {dc, rows};
   const cuuint64_t strides[1] = {static_cast<cuuint64_t>(dc) * 2};
   const cuuint32_t box[2] = {kBK, box_rows};

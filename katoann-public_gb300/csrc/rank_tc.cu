@@ -1044,16 +1044,8 @@ bool rank_tc_plan(uint32_t h, uint32_t dc, TcShape *s) {
 
 int rank_tc(const RankTcArgs &A, const uint8_t *xhi, uint32_t npts, const TcShape &s,
             cudaStream_t st) {
-  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-  if (!encode) {
-    cudaDriverEntryPointQueryResult q{};
-    void *fn = nullptr;
-    KATO_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
-                                               cudaEnableDefault, &q));
-    if (q != cudaDriverEntryPointSuccess || !fn)
-      return cuda_status(cudaErrorNotSupported, "cuTensorMapEncodeTiled");
-    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
-  }
+  const PFN_cuTensorMapEncodeTiled_v12000 encode = tc::tensor_map_encoder();
+  if (!encode) return cuda_status(cudaErrorNotSupported, "cuTensorMapEncodeTiled");
   // the high-byte plane as a 2-D tensor of bytes: x = byte in row, y = row
   CUtensorMap tmap;
   const cuuint64_t dims[2] = {A.dc, npts};

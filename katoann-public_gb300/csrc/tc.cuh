@@ -13,12 +13,33 @@
 // of at most 2^14, so up to 1024 of them add up exactly in fp32 (|sum| <= 2^24).
 #pragma once
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_fp16.h>
+#include <cuda_runtime.h>
 
 #include <cstdint>
 
 namespace kato {
 namespace tc {
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library), looked up once per process; null if the
+// driver does not offer it.
+inline PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    cudaDriverEntryPointQueryResult q{};
+    void *p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      (void)cudaGetLastError();
+      p = nullptr;
+    }
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }();
+  return fn;
+}
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
