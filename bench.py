@@ -575,9 +575,13 @@ def main():
     probed[np.unique(top[keep])] = True
     p = int(round(float(per_query_np.mean())))
     probed_rows = float(list_sizes[probed].sum())
+    rows_source = "float coarse distances on the host (approximate)"
+    if search_stats.get("probed_rows"):  # the search's own count of the rows it reads
+        probed_rows = float(search_stats["probed_rows"])
+        rows_source = "the search's own count"
     skew = {"max_list": int(sizes.max()), "mean_list": round(float(sizes.mean()), 1),
             "p99_list": int(np.percentile(sizes, 99)), "empty_lists": int((sizes == 0).sum()),
-            "lists_probed": int(probed.sum())}
+            "lists_probed": int(search_stats.get("lists_probed") or probed.sum())}
     bound, work, unit = phase_work(dom, B, L, (d + 63) // 64 * 64, d, p, max(S, k), args.head,
                                    probed_rows, probed_rows)
     achieved = work / (per_launch[dom] / 1e3)
@@ -588,7 +592,7 @@ def main():
     roofline = {"kernel": dom, "bound": bound, "achieved": round(achieved, 2), "peak": peak,
                 "unit": unit, "frac": round(achieved / peak, 4), "traffic": traffic,
                 "traffic_unit": "GB per launch (scaled from the 2M capture by tiles scored)",
-                "algorithmic": round(work, 3),
+                "algorithmic": round(work, 3), "algorithmic_rows_from": rows_source,
                 "peak_source": peaks["source"] + (" burst bf16" if bound == "tensor" else " copy"),
                 "ms_per_launch": round(per_launch[dom], 4)}
 

@@ -248,7 +248,8 @@ int katoann_gpu_search_timed(const katoann_gpu_index *index, const float *d_quer
  * stages, total; MMA waiting for accumulators, for stages, total; first
  * epilogue warp waiting for accumulators, total; [40..45] the ranking pass's
  * tiles by the number of queries of their work item: 1-2, 3-4, 5-8, 9-16,
- * 17-32, 33-64. */
+ * 17-32, 33-64; [46] the distinct lists the batch probed (non-empty) and [47]
+ * their rows (the rows the ranking pass reads once each). */
 int katoann_gpu_workspace_stats(const void *d_ws, uint64_t *h_stats, uint32_t n,
                                 katoann_stream_t stream);
 

@@ -740,11 +740,11 @@ Index::Tuning Index::autotune(const float *queries, uint32_t nq, const SearchPar
 }
 
 std::vector<uint64_t> Index::last_search_stats() const {
-  std::vector<uint64_t> out(46, 0);
+  std::vector<uint64_t> out(48, 0);
   if (!s_ || !s_->ws.p) return out;
   std::lock_guard<std::mutex> lock(s_->mu);
   cuda_check(cudaEventSynchronize(s_->done), "stats");
-  gpu_check(katoann_gpu_workspace_stats(s_->ws.p, out.data(), 46,
+  gpu_check(katoann_gpu_workspace_stats(s_->ws.p, out.data(), 48,
                                         reinterpret_cast<katoann_stream_t>(s_->stream)));
   return out;
 }

@@ -904,25 +904,38 @@ __host__ __device__ __forceinline__ uint32_t item_width(uint32_t ne, uint32_t N)
   return ne <= 16 ? 16u : (ne <= 32 && N > 32 ? 32u : N);
 }
 
+// probed (optional, 2 counters): the distinct lists the batch probes (not
+// empty) and their rows, i.e. the rows the pass reads once each.
 __global__ void tc_count_kernel(const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ list_off,
                                 uint32_t L, uint32_t N, uint32_t B, uint32_t beta,
                                 uint32_t *__restrict__ counts, uint32_t *__restrict__ qcount,
-                                uint32_t *__restrict__ qfill) {
+                                uint32_t *__restrict__ qfill, unsigned long long *__restrict__ probed) {
   const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c < B) {
     qcount[c] = 0;
     qfill[c] = 0;
   }
-  if (c >= L) return;
-  const uint32_t n = list_off[c + 1] - list_off[c];
-  const uint32_t items = n ? (cnt[c] + N - 1) / N : 0;
-  const uint32_t tiles = (n + kTcRows - 1) / kTcRows;
-  counts[c] = items;
-  counts[L + 1 + c] = items * tiles;
-  if (beta) {  // full items first, then the remainder
-    const uint32_t full = n ? cnt[c] / N : 0, rem = n ? cnt[c] % N : 0;
-    counts[2 * (L + 1) + c] =
-        tiles * (full * (64 + beta * N) + (rem ? 64 + beta * item_width(rem, N) : 0));
+  uint32_t lists = 0, rows = 0;
+  if (c < L) {
+    const uint32_t n = list_off[c + 1] - list_off[c];
+    const uint32_t items = n ? (cnt[c] + N - 1) / N : 0;
+    const uint32_t tiles = (n + kTcRows - 1) / kTcRows;
+    counts[c] = items;
+    counts[L + 1 + c] = items * tiles;
+    if (beta) {  // full items first, then the remainder
+      const uint32_t full = n ? cnt[c] / N : 0, rem = n ? cnt[c] % N : 0;
+      counts[2 * (L + 1) + c] =
+          tiles * (full * (64 + beta * N) + (rem ? 64 + beta * item_width(rem, N) : 0));
+    }
+    if (items) lists = 1, rows = n;
+  }
+  if (probed) {  // whole warps take part: one add per warp and counter
+    const uint32_t wl = __reduce_add_sync(0xffffffffu, lists);
+    const uint32_t wr = __reduce_add_sync(0xffffffffu, rows);
+    if ((threadIdx.x & 31) == 0 && wl) {
+      atomicAdd(probed, static_cast<unsigned long long>(wl));
+      atomicAdd(probed + 1, static_cast<unsigned long long>(wr));
+    }
   }
 }
 
@@ -1111,8 +1124,9 @@ int rank_tc_prepare(const uint32_t *cnt, const uint32_t *list_off, uint32_t L, u
                     uint32_t *tile_off, uint32_t *cost_off, uint32_t *nitems, uint32_t *qcount,
                     uint32_t *qfill, unsigned long long *tile_hist, cudaStream_t st) {
   uint32_t *co = beta ? cost_off : nullptr;
+  // the distinct probed lists and rows go to the two counters after the histogram
   tc_count_kernel<<<div_up(std::max(std::max(L, B), 1u), 256), 256, 0, st>>>(
-      cnt, list_off, L, N, B, beta, scratch, qcount, qfill);
+      cnt, list_off, L, N, B, beta, scratch, qcount, qfill, tile_hist ? tile_hist + 6 : nullptr);
   tc_scan_kernel<<<1, 1024, 0, st>>>(scratch, L, nitems, tile_off, co);
   tc_expand_kernel<<<div_up(L, 256), 256, 0, st>>>(list_off, scratch, cnt, L, N, beta, nitems,
                                                    items, tile_off, co, tile_hist);

@@ -371,8 +371,8 @@ class Index:
 
     def search_stats(self) -> dict:
         """Diagnostics of the last search (see katoann_gpu_workspace_stats)."""
-        s = np.zeros(46, np.uint64)
-        _check(_lib.katoann_index_stats(self._h, _ptr(s), 46))
+        s = np.zeros(48, np.uint64)
+        _check(_lib.katoann_index_stats(self._h, _ptr(s), 48))
         return dict(coarse_boundary_ties=int(s[0]), survivor_boundary_ties=int(s[1]),
                     ranking_timeouts=int(s[3]), ranking_tiles=int(s[4]),
                     ranking_candidates=int(s[5]), ranking_rescans=int(s[6]),
@@ -386,7 +386,8 @@ class Index:
                         ("tma_wait", "tma_total", "mma_wait_acc", "mma_wait_stage", "mma_total",
                          "epi_wait", "epi_total"), (int(v) for v in s[32:39]))),
                     ranking_tiles_by_queries=dict(zip(
-                        ("1-2", "3-4", "5-8", "9-16", "17-32", "33-64"), (int(v) for v in s[40:46]))))
+                        ("1-2", "3-4", "5-8", "9-16", "17-32", "33-64"), (int(v) for v in s[40:46]))),
+                    lists_probed=int(s[46]), probed_rows=int(s[47]))
 
     def _info(self):
         info = np.zeros(8, np.uint32)

@@ -117,3 +117,6 @@ def test_tile_histogram_counts_every_item(tmp_path, width):
     got = np.array(list(st["ranking_tiles_by_queries"].values()), np.int64)
     assert np.array_equal(got, want), (got, want)
     assert got.sum() == st["ranking_tiles"]
+    # the distinct probed lists and their rows: what the pass reads once each
+    hit = (cnt > 0) & (sizes > 0)
+    assert st["lists_probed"] == int(hit.sum()) and st["probed_rows"] == int(sizes[hit].sum())
