@@ -1,0 +1,35 @@
+"""The arithmetic behind bench.py's roofline: the algorithmic work of each
+search phase for one launch (pure functions, no GPU)."""
+import pytest
+
+import bench
+
+B, L, DC, D, P, S, H = 4096, 16384, 1024, 1024, 72, 64, 256
+
+
+def test_ranking_pass_counts_each_probed_row_once():
+    rows = 8_880_000
+    bound, work, unit = bench.phase_work("ranking pass", B, L, DC, D, P, S, H, rows, rows)
+    assert (bound, unit) == ("hbm", "GB/s")
+    assert work == pytest.approx(rows * H / 1e9)  # h bytes per row: 2.27 GB at the bench's size
+
+
+def test_coarse_product_is_four_tensor_gemms():
+    bound, work, unit = bench.phase_work("coarse product", B, L, DC, D, P, S, H, 0, 0)
+    assert (bound, unit) == ("tensor", "TFLOP/s")
+    assert work == pytest.approx(8 * B * L * DC / 1e12)  # 550 GFLOP per batch
+
+
+def test_other_phases():
+    assert bench.phase_work("refine", B, L, DC, D, P, S, H, 0, 0)[1] == pytest.approx(
+        B * S * (2 * DC + 12) / 1e9)
+    assert bench.phase_work("coarse select", B, L, DC, D, P, S, H, 0, 0)[1] == pytest.approx(
+        B * L * 4 / 1e9)
+    assert bench.phase_work("seed bounds", B, L, DC, D, P, S, H, 0, 0)[1] == pytest.approx(
+        B * bench.SEED_ROWS * H / 1e9)
+
+
+def test_traffic_per_tile_is_the_capture():
+    # 536.0 MB over 20,279 tiles in the 2M x 1024 capture: 26.4 KB per tile
+    assert bench.RANK_TC_DRAM_BYTES_PER_TILE == pytest.approx(536.0e6 / 20279)
+    assert 26_000 < bench.RANK_TC_DRAM_BYTES_PER_TILE < 27_000
