@@ -3,7 +3,10 @@
 // (src/index.cpp:882-892) as status codes; nothing throws across the ABI.
 #include <atomic>
 #include <cstdio>
+#include <map>
+#include <mutex>
 #include <string>
+#include <utility>
 
 #include <cuda_fp16.h>
 
@@ -22,6 +25,39 @@ void set_error(const std::string &msg) { g_error = msg; }
 int cuda_status(cudaError_t e, const char *what) {
   g_error = std::string(what) + ": " + cudaGetErrorString(e);
   return e == cudaErrorMemoryAllocation ? KATO_ENOMEM : KATO_ERUNTIME;
+}
+
+namespace {
+std::mutex g_device_mu;
+std::map<int, int> g_sms;                              // device -> SM count
+std::map<std::pair<int, const void *>, int> g_smem;    // (device, kernel) -> bytes allowed
+}  // namespace
+
+int current_sms(int *sms) {
+  int dev = 0;
+  KATO_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(g_device_mu);
+  auto it = g_sms.find(dev);
+  if (it == g_sms.end()) {
+    int n = 0;
+    KATO_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+    it = g_sms.emplace(dev, n).first;
+  }
+  *sms = it->second;
+  return KATO_OK;
+}
+
+int smem_limit(const void *kernel, int bytes, const char *what) {
+  int dev = 0;
+  KATO_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(g_device_mu);
+  int &have = g_smem[{dev, kernel}];
+  if (have < bytes) {
+    const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess) return cuda_status(e, what);
+    have = bytes;
+  }
+  return KATO_OK;
 }
 
 int rotate_rows(const float *in, uint32_t nrows, uint32_t d, const float *rot, float *out,

@@ -1,44 +1,28 @@
-// The katoann command-line tool on the GPU: the reference's three commands
-// with the same flags and the same JSON lines (tools/katoann.cpp:339-352,
-// README.md:179-198), over katoann::Index from libkatoann.so.
+// The katoann command-line tool on the GPU. It keeps the interface of the
+// reference's tool (tools/katoann.cpp:339-352, README.md:179-198): the
+// commands build, search and load, their flags, the JSON lines they print,
+// the error messages and the exit codes (2 for a usage error, 1 for any other
+// error, printed as "katoann: <message>"). It adds `budget`, which trains the
+// learned probe-budget model that `load --budget` serves.
 //
-//   katoann build  --data BASE.fbin --out PREFIX [--nlist 2048] [--normalize]
-//                  [--train-size 256000] [--iters 12] [--seed 0] [--threads T]
-//   katoann search --index PREFIX --queries Q.fbin [--gt GT.bin] [--k 10]
-//                  [--nprobe 64,128] [--ranking prefix|high|full] [--survivors 32]
-//                  [--prefix-dims D] [--selection threshold|local] [--batch 4096]
-//                  [--precision sq16] [--engine gpu|amx|avx512] [--coarse batched]
-//                  [--repeat 3] [--threads T] [--query-ids FILE] [--out PREFIX]
-//                  [--code-cache]
-//   katoann load   --index PREFIX --queries Q.fbin --rate QPS [--requests 10000]
-//                  [--nprobe 64] [--max-batch 4096] [--seed 42] [--k-mix 10,100]
-//                  [--in-flight 3] [--hbm-budget-gb G] [--max-wait-ms 0]
-//                  [--budget MODEL.kprb --threshold 0.95] and the search flags
-//   katoann budget --index PREFIX --queries TRAIN.fbin --out MODEL.kprb [--ladder ...]
-//                  [--depth 256] [--label-nprobe N] [--epochs 24] and the search flags
-//
-// `load` serves requests that arrive as a Poisson process (tools/katoann.cpp:
-// 263-337), here through the continuous-batching katoann::Server: arrivals are
-// batched per k while earlier batches are still on the device (up to
-// --in-flight batches within --hbm-budget-gb), optionally with the learned
-// per-query nprobe of a ProbeModel file; latency runs from a request's
-// arrival to its completion. Errors print to stderr and exit 1, as the
-// reference's main does.
+// Everything is driven by one table of flags (kFlags): the parser checks each
+// argument against the command's rows, fills in the table's defaults, and the
+// usage text is printed from the same rows. `load` serves Poisson arrivals
+// through the continuous-batching katoann::Server (several batches in flight,
+// per-request k, an HBM budget), where the reference answers one batch at a
+// time; latency still runs from a request's arrival to its completion.
 #include <omp.h>
 
 #include <algorithm>
 #include <chrono>
-#include <cmath>
 #include <cstdio>
 #include <cstring>
-#include <fstream>
 #include <map>
-#include <random>
+#include <memory>
 #include <set>
-#include <sstream>
 #include <stdexcept>
 #include <string>
-#include <thread>
+#include <utility>
 #include <vector>
 
 #include "katoann/index.h"
@@ -47,374 +31,539 @@
 
 namespace {
 
-using Clock = std::chrono::steady_clock;
+// ------------------------------------------------------------------ flags
+enum Command : unsigned { kBuild = 1u, kSearch = 2u, kLoad = 4u, kBudget = 8u };
+constexpr unsigned kQuerying = kSearch | kLoad | kBudget;  // commands that load an index
 
-double seconds_since(Clock::time_point t) {
-  return std::chrono::duration<double>(Clock::now() - t).count();
-}
-
-// --key value pairs and the value-less switches.
-struct Args {
-  std::map<std::string, std::string> kv;
-  std::set<std::string> flags;
-
-  bool has(const std::string &k) const { return flags.count(k) != 0; }
-  std::string get(const std::string &k, const std::string &dflt = "") const {
-    const auto it = kv.find(k);
-    return it == kv.end() ? dflt : it->second;
-  }
-  std::string need(const std::string &k) const {
-    const auto it = kv.find(k);
-    if (it == kv.end()) throw std::invalid_argument("missing --" + k);
-    return it->second;
-  }
-  uint32_t u32(const std::string &k, uint32_t dflt) const {
-    const auto it = kv.find(k);
-    return it == kv.end() ? dflt : static_cast<uint32_t>(std::stoul(it->second));
-  }
-  double num(const std::string &k, double dflt) const {
-    const auto it = kv.find(k);
-    return it == kv.end() ? dflt : std::stod(it->second);
-  }
+struct Flag {
+  const char *name;
+  const char *meta;   // value placeholder in the usage text; null for a switch
+  const char *dflt;   // default value (null: none)
+  unsigned used;      // commands that accept the flag
+  unsigned required;  // commands that need it
 };
 
-Args parse(int argc, char **argv, int first) {
-  static const std::set<std::string> kSwitches = {"normalize", "normalized", "code-cache"};
-  Args a;
-  for (int i = first; i < argc; ++i) {
-    std::string s = argv[i];
-    if (s.rfind("--", 0) != 0) throw std::invalid_argument("unexpected argument " + s);
-    s = s.substr(2);
-    if (kSwitches.count(s)) {
-      a.flags.insert(s);
-    } else {
-      if (i + 1 >= argc) throw std::invalid_argument("missing value for --" + s);
-      a.kv[s] = argv[++i];
-    }
-  }
-  return a;
+// The reference's flags first (same names, same defaults), then the GPU
+// tool's additions. Order matters twice: the usage text follows it, and the
+// first missing required flag in this order is the one reported.
+const Flag kFlags[] = {
+    {"data", "BASE.fbin", nullptr, kBuild, kBuild},
+    {"index", "PREFIX", nullptr, kQuerying, kQuerying},
+    {"queries", "Q.fbin", nullptr, kQuerying, kQuerying},
+    {"out", "PREFIX", nullptr, kBuild | kSearch | kBudget, kBuild | kBudget},
+    {"nlist", "N", "2048", kBuild, 0},
+    {"normalize", nullptr, nullptr, kBuild, 0},
+    {"normalized", nullptr, nullptr, kBuild, 0},
+    {"train-size", "N", "256000", kBuild, 0},
+    {"iters", "N", "12", kBuild, 0},
+    {"seed", "S", nullptr, kBuild | kLoad | kBudget, 0},
+    {"threads", "T", "0", kBuild | kQuerying, 0},
+    {"gt", "GT.bin", nullptr, kSearch, 0},
+    {"k", "K", "10", kQuerying, 0},
+    {"nprobe", "64,128", "64", kQuerying, 0},
+    {"ranking", "prefix|high|full", "prefix", kQuerying, 0},
+    {"survivors", "S", "32", kQuerying, 0},
+    {"prefix-dims", "D", "0", kQuerying, 0},
+    {"selection", "threshold|local", "threshold", kQuerying, 0},
+    {"batch", "B", "4096", kQuerying, 0},
+    {"precision", "sq16", "sq16", kQuerying, 0},
+    {"engine", "gpu", "gpu", kQuerying, 0},
+    {"coarse", "batched", "batched", kQuerying, 0},
+    {"repeat", "R", "3", kSearch, 0},
+    {"query-ids", "FILE", nullptr, kQuerying, 0},
+    {"rate", "QPS", "1000", kLoad, 0},
+    {"requests", "N", "10000", kLoad, 0},
+    {"max-batch", "B", "4096", kQuerying, 0},
+    {"code-cache", nullptr, nullptr, kQuerying, 0},
+    {"k-mix", "10,100", nullptr, kLoad, 0},
+    {"in-flight", "N", "3", kLoad, 0},
+    {"hbm-budget-gb", "G", "0", kLoad, 0},
+    {"max-wait-ms", "MS", "0", kLoad, 0},
+    {"budget", "MODEL.kprb", nullptr, kLoad, 0},
+    {"threshold", "P", "0.95", kLoad, 0},
+    {"ladder", "8,16,...", nullptr, kBudget, 0},
+    {"depth", "D", nullptr, kBudget, 0},
+    {"label-nprobe", "N", "0", kBudget, 0},
+    {"label-ranking", "full|prefix|high", "full", kBudget, 0},
+    {"label-survivors", "S", "0", kBudget, 0},
+    {"epochs", "E", "24", kBudget, 0},
+    {"train-batch", "B", "1024", kBudget, 0},
+};
+
+const Flag *find_flag(const std::string &name) {
+  for (const Flag &f : kFlags)
+    if (name == f.name) return &f;
+  return nullptr;
 }
 
-std::vector<uint32_t> u32_list(const std::string &s) {
-  std::vector<uint32_t> out;
-  std::stringstream in(s);
-  std::string item;
-  while (std::getline(in, item, ',')) out.push_back(static_cast<uint32_t>(std::stoul(item)));
-  return out;
-}
-
-// .fbin: uint32 rows, uint32 dim, float32 rows.
-std::vector<float> read_fbin(const std::string &path, uint32_t &n, uint32_t &d) {
-  std::ifstream f(path, std::ios::binary);
-  if (!f) throw std::runtime_error("cannot open " + path);
-  f.read(reinterpret_cast<char *>(&n), 4);
-  f.read(reinterpret_cast<char *>(&d), 4);
-  std::vector<float> rows(static_cast<size_t>(n) * d);
-  f.read(reinterpret_cast<char *>(rows.data()), static_cast<std::streamsize>(rows.size() * 4));
-  if (!f) throw std::runtime_error("truncated " + path);
-  return rows;
-}
-
-// Ground truth: uint32 rows, uint32 k, rows x k uint32 ids.
-std::vector<uint32_t> read_gt(const std::string &path, uint32_t &n, uint32_t &k) {
-  std::ifstream f(path, std::ios::binary);
-  if (!f) throw std::runtime_error("cannot open " + path);
-  f.read(reinterpret_cast<char *>(&n), 4);
-  f.read(reinterpret_cast<char *>(&k), 4);
-  std::vector<uint32_t> ids(static_cast<size_t>(n) * k);
-  f.read(reinterpret_cast<char *>(ids.data()), static_cast<std::streamsize>(ids.size() * 4));
-  if (!f) throw std::runtime_error("truncated " + path);
-  return ids;
-}
-
-katoann::LoadOptions load_options(const Args &a) {
-  katoann::LoadOptions o;
-  const std::string prec = a.get("precision", "sq16");
-  if (prec == "bf16") o.precision = katoann::Precision::kBf16;
-  else if (prec != "sq16") throw std::invalid_argument("--precision is sq16 or bf16");
-  const std::string eng = a.get("engine", "gpu");  // the CPU engines name the one GPU engine
-  if (eng == "avx512") o.use_amx = false;
-  else if (eng != "amx" && eng != "gpu") throw std::invalid_argument("--engine is gpu, amx or avx512");
-  o.prefix_dims = a.u32("prefix-dims", 0);
-  const std::string coarse = a.get("coarse", "batched");
-  if (coarse == "flat") o.batched_coarse = false;
-  else if (coarse != "batched") throw std::invalid_argument("--coarse is batched or flat");
-  o.max_batch = std::max(a.u32("batch", 4096), a.u32("max-batch", 4096));
-  o.code_cache = a.has("code-cache");  // PREFIX.gpucodes (an addition to the reference's flags)
-  return o;
-}
-
-katoann::SearchParams search_params(const Args &a) {
-  katoann::SearchParams p;
-  p.k = a.u32("k", 10);
-  const std::string r = a.get("ranking", "prefix");
-  if (r == "full") p.ranking = katoann::Ranking::kFull;
-  else if (r == "high") p.ranking = katoann::Ranking::kHighBytes;
-  else if (r == "prefix") p.ranking = katoann::Ranking::kPrefix;
-  else throw std::invalid_argument("--ranking is prefix, high, or full");
-  p.survivors = a.u32("survivors", 32);
-  const std::string s = a.get("selection", "threshold");
-  if (s == "local") p.selection = katoann::Selection::kLocal;
-  else if (s != "threshold") throw std::invalid_argument("--selection is threshold or local");
-  return p;
-}
-
-// recall@k of ids (one row per query of `qid`) against the first k ground-truth ids.
-double recall_at(const std::vector<uint32_t> &ids, const std::vector<uint32_t> &qid, uint32_t k,
-                 const std::vector<uint32_t> &gt, uint32_t gk) {
-  double hits = 0;
-  for (size_t i = 0; i < qid.size(); ++i) {
-    const uint32_t *truth = gt.data() + static_cast<size_t>(qid[i]) * gk;
-    const std::set<uint32_t> t(truth, truth + k);
-    for (uint32_t j = 0; j < k; ++j) hits += t.count(ids[i * k + j]);
-  }
-  return hits / (static_cast<double>(qid.size()) * k);
-}
-
-// The queries to use: --query-ids (whitespace-separated indices) or all.
-std::vector<uint32_t> query_ids(const Args &a, uint32_t nq) {
-  std::vector<uint32_t> ids;
-  const std::string path = a.get("query-ids");
-  if (path.empty()) {
-    for (uint32_t i = 0; i < nq; ++i) ids.push_back(i);
-    return ids;
-  }
-  std::ifstream f(path);
-  if (!f) throw std::runtime_error("cannot open " + path);
-  uint32_t id;
-  while (f >> id) {
-    if (id >= nq) throw std::runtime_error("query id out of range in " + path);
-    ids.push_back(id);
-  }
-  if (ids.empty()) throw std::runtime_error("no query ids in " + path);
-  return ids;
-}
-
-void set_threads(const Args &a) {
-  const uint32_t t = a.u32("threads", 0);
-  omp_set_dynamic(0);
-  if (t) omp_set_num_threads(static_cast<int>(t));
-}
-
-std::vector<float> load_queries(const Args &a, const katoann::Index &idx, uint32_t &nq) {
-  uint32_t d = 0;
-  std::vector<float> q = read_fbin(a.need("queries"), nq, d);
-  if (d != idx.dim()) throw std::runtime_error("query dimension does not match the index");
-  if (idx.normalized()) katoann::normalize_rows(q.data(), nq, d);
-  return q;
-}
-
-int cmd_build(const Args &a) {
-  set_threads(a);
-  uint32_t n = 0, d = 0;
-  std::vector<float> data = read_fbin(a.need("data"), n, d);
-  katoann::BuildOptions o;
-  o.nlist = a.u32("nlist", 2048);
-  o.train_size = a.u32("train-size", 256000);
-  o.kmeans_iters = a.u32("iters", 12);
-  o.seed = std::stoull(a.get("seed", "0"));
-  if (a.has("normalize")) katoann::normalize_rows(data.data(), n, d);
-  o.normalized = a.has("normalize") || a.has("normalized");
-  const auto t0 = Clock::now();
-  katoann::Index::build(data.data(), n, d, o, a.need("out"));
-  std::printf("{\"vectors\": %u, \"dim\": %u, \"nlist\": %u, \"build_s\": %.1f}\n", n, d, o.nlist,
-              seconds_since(t0));
-  return 0;
-}
-
-int cmd_search(const Args &a) {
-  set_threads(a);
-  katoann::Index idx;
-  auto t0 = Clock::now();
-  idx.load(a.need("index"), load_options(a));
-  const double load_s = seconds_since(t0);
-  uint32_t nq = 0;
-  const std::vector<float> queries = load_queries(a, idx, nq);
-  const uint32_t d = idx.dim();
-  const std::vector<uint32_t> qid = query_ids(a, nq);
-  std::vector<float> q(qid.size() * static_cast<size_t>(d));
-  for (size_t i = 0; i < qid.size(); ++i)
-    std::memcpy(q.data() + i * d, queries.data() + static_cast<size_t>(qid[i]) * d, d * sizeof(float));
-  uint32_t gn = 0, gk = 0;
-  std::vector<uint32_t> gt;
-  if (!a.get("gt").empty()) gt = read_gt(a.get("gt"), gn, gk);
-  katoann::SearchParams p = search_params(a);
-  if (!gt.empty() && (gn < nq || gk < p.k)) throw std::runtime_error("ground truth too small");
-  const uint32_t batch = a.u32("batch", 4096), repeat = std::max(1u, a.u32("repeat", 3));
-  const std::string out = a.get("out");
-  std::printf("{\"index\": \"%s\", \"engine\": \"gpu\", \"threads\": %d, \"load_s\": %.1f, "
-              "\"memory_gb\": %.2f, \"queries\": %zu, \"prefix_dims\": %u}\n",
-              a.need("index").c_str(), omp_get_max_threads(), load_s, idx.memory_bytes() / 1e9,
-              qid.size(), idx.prefix_dims());
-  const size_t total = qid.size();
-  std::vector<uint32_t> ids(total * p.k);
-  std::vector<float> dists(total * p.k);
-  for (const uint32_t np : u32_list(a.get("nprobe", "64"))) {
-    p.nprobe = np;
-    auto pass = [&]() {
-      for (size_t off = 0; off < total; off += batch) {
-        const uint32_t b = static_cast<uint32_t>(std::min<size_t>(batch, total - off));
-        idx.search(q.data() + off * d, b, p, ids.data() + off * p.k, dists.data() + off * p.k);
-      }
-    };
-    pass();  // warm-up
-    std::vector<double> secs;
-    for (uint32_t r = 0; r < repeat; ++r) {
-      t0 = Clock::now();
-      pass();
-      secs.push_back(seconds_since(t0));
-    }
-    std::sort(secs.begin(), secs.end());
-    const double med = secs[secs.size() / 2];
-    std::printf("{\"nprobe\": %u, \"k\": %u, \"survivors\": %u, \"batch\": %u, \"qps\": %.1f, "
-                "\"seconds_median\": %.4f, \"seconds_min\": %.4f, \"seconds_max\": %.4f",
-                np, p.k, p.survivors, batch, total / med, med, secs.front(), secs.back());
-    if (!gt.empty()) std::printf(", \"recall\": %.5f", recall_at(ids, qid, p.k, gt, gk));
-    std::printf("}\n");
-    std::fflush(stdout);
-    if (!out.empty()) {  // uint32 rows, uint32 k, ids, dists (tools/katoann.cpp:253-259)
-      std::ofstream f(out + ".np" + std::to_string(np) + ".bin", std::ios::binary);
-      const uint32_t hdr[2] = {static_cast<uint32_t>(total), p.k};
-      f.write(reinterpret_cast<const char *>(hdr), sizeof(hdr));
-      f.write(reinterpret_cast<const char *>(ids.data()), static_cast<std::streamsize>(ids.size() * 4));
-      f.write(reinterpret_cast<const char *>(dists.data()),
-              static_cast<std::streamsize>(dists.size() * 4));
-    }
-  }
-  return 0;
-}
-
-// The learned probe budget for `load --budget`: labels the training queries by
-// searching the index and trains the model on the GPU (katoann::ProbeModel).
-int cmd_budget(const Args &a) {
-  set_threads(a);
-  katoann::Index idx;
-  idx.load(a.need("index"), load_options(a));
-  uint32_t nq = 0;
-  const std::vector<float> queries = load_queries(a, idx, nq);
-  const katoann::SearchParams sp = search_params(a);
-  katoann::ProbeTrainOptions o;
-  if (!a.get("ladder").empty()) o.ladder = u32_list(a.get("ladder"));
-  o.depth = a.u32("depth", std::min(256u, idx.nlist()));
-  o.k = sp.k;
-  o.label_nprobe = a.u32("label-nprobe", 0);
-  if (a.get("label-ranking", "full") == "prefix") o.label_ranking = katoann::Ranking::kPrefix;
-  else if (a.get("label-ranking", "full") == "high") o.label_ranking = katoann::Ranking::kHighBytes;
-  o.label_survivors = a.u32("label-survivors", 0);
-  o.ranking = sp.ranking;
-  o.survivors = sp.survivors;
-  o.epochs = a.u32("epochs", 24);
-  o.batch = a.u32("train-batch", 1024);
-  o.seed = std::stoull(a.get("seed", "0"));
-  std::vector<uint32_t> ladder;
-  for (uint32_t v : o.ladder)
-    if (v <= idx.nlist()) ladder.push_back(v);
-  o.ladder = ladder;
-  const auto t0 = Clock::now();
-  const katoann::ProbeModel m = katoann::ProbeModel::train(idx, queries.data(), nq, o);
-  m.save(a.need("out"));
-  std::vector<uint64_t> hist(m.classes(), 0);
-  for (uint8_t l : m.labels()) ++hist[l];
-  std::printf("{\"queries\": %u, \"classes\": %u, \"depth\": %u, \"train_s\": %.2f, "
-              "\"loss_first\": %.4f, \"loss_last\": %.4f, \"label_histogram\": [",
-              nq, m.classes(), m.depth(), seconds_since(t0), m.loss().front(), m.loss().back());
-  for (size_t i = 0; i < hist.size(); ++i)
-    std::printf("%s%llu", i ? ", " : "", static_cast<unsigned long long>(hist[i]));
-  std::printf("]}\n");
-  return 0;
-}
-
-int cmd_load(const Args &a) {
-  set_threads(a);
-  katoann::Index idx;
-  idx.load(a.need("index"), load_options(a));
-  uint32_t nq = 0;
-  const std::vector<float> queries = load_queries(a, idx, nq);
-  const uint32_t d = idx.dim();
-  const std::vector<uint32_t> pool = query_ids(a, nq);
-  const katoann::SearchParams sp = search_params(a);
-  // per-request k: one value, or a list drawn uniformly per request
-  const std::vector<uint32_t> kmix = u32_list(a.get("k-mix", std::to_string(sp.k)));
-  if (kmix.empty()) throw std::invalid_argument("empty --k-mix");
-  katoann::ProbeModel model;
-  katoann::ServerOptions so;
-  so.max_batch = std::max(1u, std::min(4096u, a.u32("max-batch", 4096)));
-  so.max_in_flight = a.u32("in-flight", 3);
-  so.hbm_budget = static_cast<size_t>(a.num("hbm-budget-gb", 0) * 1e9);
-  so.max_k = *std::max_element(kmix.begin(), kmix.end());
-  so.nprobe = a.u32("nprobe", 64);
-  so.ranking = sp.ranking;
-  so.survivors = sp.survivors;
-  so.max_wait_ms = a.num("max-wait-ms", 0);
-  if (!a.get("budget").empty()) {  // learned per-query nprobe, capped at --nprobe
-    model = katoann::ProbeModel::load(a.get("budget"));
-    so.budget = &model;
-    so.budget_threshold = static_cast<float>(a.num("threshold", 0.95));
-  }
-  const double rate = a.num("rate", 1000);
-  const uint32_t n = a.u32("requests", 10000);
-  katoann::Server server(idx, so);
-  {  // warm-up: one full batch of each k
-    std::vector<uint64_t> ids;
-    for (uint32_t k : kmix)
-      for (uint32_t w = 0; w < std::min<uint32_t>(so.max_batch, static_cast<uint32_t>(pool.size())); ++w)
-        ids.push_back(server.submit(queries.data() + static_cast<size_t>(pool[w]) * d, k));
-    for (uint64_t id : ids) server.wait(id);
-  }
-  // Poisson arrivals, queries round-robin from the pool, k uniform over the mix
-  const katoann::LoadReport r =
-      katoann::run_load(server, queries.data(), d, pool, rate, n, kmix, a.u32("seed", 42));
-  std::printf("{\"rate\": %.1f, \"requests\": %u, \"nprobe\": %u, \"engine\": \"gpu\", "
-              "\"achieved_qps\": %.1f, \"p50_ms\": %.2f, \"p95_ms\": %.2f, \"p99_ms\": %.2f, "
-              "\"max_ms\": %.2f, \"batches\": %llu, \"mean_batch\": %.1f, \"in_flight\": %u, "
-              "\"peak_in_flight\": %u, \"peak_hbm_gb\": %.3f, \"learned\": %s, "
-              "\"mean_nprobe\": %.2f, \"max_lag_ms\": %.2f, \"max_enqueue_ms\": %.2f, "
-              "\"max_batch_gpu_ms\": %.2f}\n",
-              rate, n, so.nprobe, r.achieved_qps, r.p50_ms, r.p95_ms, r.p99_ms, r.max_ms,
-              static_cast<unsigned long long>(r.batches), r.mean_batch, so.max_in_flight,
-              r.peak_in_flight, r.peak_hbm_bytes / 1e9, so.budget ? "true" : "false",
-              r.mean_nprobe, r.max_lag_ms, r.max_enqueue_ms, r.max_batch_gpu_ms);
-  return 0;
+const char *command_name(unsigned c) {
+  return c == kBuild ? "build" : c == kSearch ? "search" : c == kLoad ? "load" : "budget";
 }
 
 void usage() {
-  std::fprintf(stderr,
-               "usage: katoann build  --data BASE.fbin --out PREFIX [--nlist 2048] [--normalize]\n"
-               "                      [--train-size 256000] [--iters 12] [--seed 0] [--threads T]\n"
-               "       katoann search --index PREFIX --queries Q.fbin [--gt GT.bin] [--k 10]\n"
-               "                      [--nprobe 64,128] [--ranking prefix|high|full] [--survivors 32]\n"
-               "                      [--prefix-dims D] [--selection threshold|local] [--batch 4096]\n"
-               "                      [--precision sq16] [--engine gpu] [--coarse batched]\n"
-               "                      [--repeat 3] [--threads T] [--query-ids FILE] [--out PREFIX]\n"
-               "                      [--code-cache]\n"
-               "       katoann load   --index PREFIX --queries Q.fbin --rate QPS [--requests 10000]\n"
-               "                      [--nprobe 64] [--max-batch 4096] [--seed 42] [--k-mix 10,100]\n"
-               "                      [--in-flight 3] [--hbm-budget-gb G] [--max-wait-ms 0]\n"
-               "                      [--budget MODEL.kprb --threshold 0.95] and the search flags\n"
-               "       katoann budget --index PREFIX --queries TRAIN.fbin --out MODEL.kprb\n"
-               "                      [--ladder 8,16,...] [--depth 256] [--label-nprobe N]\n"
-               "                      [--label-ranking full|prefix] [--label-survivors S]\n"
-               "                      [--epochs 24] [--train-batch 1024] and the search flags\n");
+  std::string text = "usage:";
+  for (unsigned c : {kBuild, kSearch, kLoad, kBudget}) {
+    std::string line = std::string(text.size() > 6 ? "      " : "") + " katoann " + command_name(c);
+    const size_t indent = 15;
+    for (const Flag &f : kFlags) {
+      if (!(f.used & c)) continue;
+      std::string item = std::string("--") + f.name + (f.meta ? std::string(" ") + f.meta : "");
+      if (!(f.required & c)) item = "[" + item + "]";
+      const size_t last_nl = line.rfind('\n');
+      const size_t width = line.size() - (last_nl == std::string::npos ? 0 : last_nl + 1);
+      if (width + 1 + item.size() > 92) line += "\n" + std::string(indent, ' ');
+      line += " " + item;
+    }
+    text += line + "\n";
+  }
+  std::fputs(text.c_str(), stderr);
+}
+
+// The parsed command line of one command: every value the table allows, the
+// switches that were given, and typed access with the table's defaults.
+class Options {
+ public:
+  Options(unsigned cmd, int argc, char **argv) {
+    for (int i = 2; i < argc; ++i) {
+      const std::string arg = argv[i];
+      if (arg.compare(0, 2, "--") != 0) throw std::invalid_argument("unexpected argument " + arg);
+      std::string name = arg.substr(2), value;
+      const size_t eq = name.find('=');
+      const bool inline_value = eq != std::string::npos;
+      if (inline_value) value = name.substr(eq + 1), name.resize(eq);
+      const Flag *f = find_flag(name);
+      if (!f || !(f->used & cmd))
+        throw std::invalid_argument("unknown option --" + name + " for " + command_name(cmd));
+      if (!f->meta) {
+        if (inline_value) throw std::invalid_argument("--" + name + " takes no value");
+        switches_.insert(name);
+        continue;
+      }
+      if (!inline_value) {
+        if (i + 1 >= argc) throw std::invalid_argument("missing value for --" + name);
+        value = argv[++i];
+      }
+      values_[name] = value;
+    }
+    for (const Flag &f : kFlags)
+      if ((f.required & cmd) && !values_.count(f.name))
+        throw std::invalid_argument(std::string("missing --") + f.name);
+  }
+
+  bool given(const char *name) const { return values_.count(name) || switches_.count(name); }
+  bool on(const char *name) const { return switches_.count(name) != 0; }
+  std::string text(const char *name) const {
+    const auto it = values_.find(name);
+    if (it != values_.end()) return it->second;
+    const Flag *f = find_flag(name);
+    return f && f->dflt ? f->dflt : "";
+  }
+  uint32_t u32(const char *name) const { return static_cast<uint32_t>(std::stoul(text(name))); }
+  uint32_t u32_or(const char *name, uint32_t fallback) const {
+    return given(name) ? u32(name) : fallback;
+  }
+  uint64_t u64_or(const char *name, uint64_t fallback) const {
+    return given(name) ? std::stoull(text(name)) : fallback;
+  }
+  double real(const char *name) const { return std::stod(text(name)); }
+  std::vector<uint32_t> list(const char *name) const {
+    std::vector<uint32_t> out;
+    const std::string s = text(name);
+    size_t at = 0;
+    while (at <= s.size() && !s.empty()) {
+      const size_t comma = std::min(s.find(',', at), s.size());
+      out.push_back(static_cast<uint32_t>(std::stoul(s.substr(at, comma - at))));
+      at = comma + 1;
+    }
+    return out;
+  }
+  // One of several spellings, mapped to its value; anything else is `complaint`.
+  template <typename T>
+  T choice(const char *name, std::initializer_list<std::pair<const char *, T>> table,
+           const char *complaint) const {
+    const std::string v = text(name);
+    for (const auto &entry : table)
+      if (v == entry.first) return entry.second;
+    throw std::invalid_argument(complaint);
+  }
+
+ private:
+  std::map<std::string, std::string> values_;
+  std::set<std::string> switches_;
+};
+
+// ------------------------------------------------------------- file I/O
+// .fbin vectors and ground-truth files share one layout: uint32 rows, uint32
+// columns, then rows x columns values of 4 bytes.
+template <typename T>
+struct Table {
+  uint32_t rows = 0, cols = 0;
+  std::vector<T> cells;
+  const T *row(size_t i) const { return cells.data() + i * cols; }
+};
+
+template <typename T>
+Table<T> read_table(const std::string &path) {
+  static_assert(sizeof(T) == 4, "4-byte cells");
+  std::unique_ptr<FILE, int (*)(FILE *)> f(std::fopen(path.c_str(), "rb"), &std::fclose);
+  if (!f) throw std::runtime_error("cannot open " + path);
+  uint32_t head[2] = {0, 0};
+  Table<T> t;
+  if (std::fread(head, sizeof(uint32_t), 2, f.get()) == 2) {
+    t.rows = head[0];
+    t.cols = head[1];
+    t.cells.resize(static_cast<size_t>(t.rows) * t.cols);
+    if (std::fread(t.cells.data(), sizeof(T), t.cells.size(), f.get()) == t.cells.size()) return t;
+  }
+  throw std::runtime_error("truncated " + path);
+}
+
+void write_results(const std::string &path, uint32_t rows, uint32_t k,
+                   const std::vector<uint32_t> &ids, const std::vector<float> &dists) {
+  std::unique_ptr<FILE, int (*)(FILE *)> f(std::fopen(path.c_str(), "wb"), &std::fclose);
+  if (!f) throw std::runtime_error("cannot write " + path);
+  const uint32_t head[2] = {rows, k};
+  std::fwrite(head, sizeof(uint32_t), 2, f.get());
+  std::fwrite(ids.data(), sizeof(uint32_t), ids.size(), f.get());
+  std::fwrite(dists.data(), sizeof(float), dists.size(), f.get());
+}
+
+// ------------------------------------------------------------ JSON lines
+class JsonLine {
+ public:
+  JsonLine &str(const char *key, const std::string &v) { return put(key, "\"" + v + "\""); }
+  JsonLine &count(const char *key, unsigned long long v) { return put(key, std::to_string(v)); }
+  JsonLine &sint(const char *key, long long v) { return put(key, std::to_string(v)); }
+  JsonLine &fixed(const char *key, double v, int digits) {
+    char buf[64];
+    std::snprintf(buf, sizeof(buf), "%.*f", digits, v);
+    return put(key, buf);
+  }
+  JsonLine &flag(const char *key, bool v) { return put(key, v ? "true" : "false"); }
+  JsonLine &list(const char *key, const std::vector<uint64_t> &v) {
+    std::string s = "[";
+    for (size_t i = 0; i < v.size(); ++i) s += (i ? ", " : "") + std::to_string(v[i]);
+    return put(key, s + "]");
+  }
+  void print() const {
+    std::printf("{%s}\n", body_.c_str());
+    std::fflush(stdout);
+  }
+
+ private:
+  JsonLine &put(const char *key, const std::string &v) {
+    body_ += (body_.empty() ? "\"" : ", \"") + std::string(key) + "\": " + v;
+    return *this;
+  }
+  std::string body_;
+};
+
+using Clock = std::chrono::steady_clock;
+double since(Clock::time_point t) { return std::chrono::duration<double>(Clock::now() - t).count(); }
+
+// ------------------------------------------------------ shared settings
+void apply_threads(const Options &o) {
+  omp_set_dynamic(0);
+  if (const uint32_t t = o.u32("threads")) omp_set_num_threads(static_cast<int>(t));
+}
+
+katoann::LoadOptions load_options(const Options &o) {
+  katoann::LoadOptions lo;
+  lo.precision = o.choice<katoann::Precision>(
+      "precision", {{"sq16", katoann::Precision::kSq16}, {"bf16", katoann::Precision::kBf16}},
+      "--precision is sq16 or bf16");
+  // the reference's CPU engines are accepted and name the one GPU engine
+  lo.use_amx = o.choice<bool>("engine", {{"gpu", true}, {"amx", true}, {"avx512", false}},
+                              "--engine is gpu, amx or avx512");
+  lo.prefix_dims = o.u32("prefix-dims");
+  lo.batched_coarse = o.choice<bool>("coarse", {{"batched", true}, {"flat", false}},
+                                     "--coarse is batched or flat");
+  lo.max_batch = std::max(o.u32("batch"), o.u32("max-batch"));
+  lo.code_cache = o.on("code-cache");
+  return lo;
+}
+
+katoann::SearchParams search_params(const Options &o) {
+  katoann::SearchParams p;
+  p.k = o.u32("k");
+  p.ranking = o.choice<katoann::Ranking>("ranking",
+                                         {{"prefix", katoann::Ranking::kPrefix},
+                                          {"high", katoann::Ranking::kHighBytes},
+                                          {"full", katoann::Ranking::kFull}},
+                                         "--ranking is prefix, high, or full");
+  p.survivors = o.u32("survivors");
+  p.selection = o.choice<katoann::Selection>(
+      "selection", {{"threshold", katoann::Selection::kThreshold}, {"local", katoann::Selection::kLocal}},
+      "--selection is threshold or local");
+  return p;
+}
+
+// An index with its query file: the index loaded (and timed), the queries
+// normalized as the index was, and the subset --query-ids names (default: all).
+struct Workload {
+  katoann::Index index;
+  double load_s = 0;
+  Table<float> queries;
+  std::vector<uint32_t> chosen;
+
+  explicit Workload(const Options &o) {
+    const auto t0 = Clock::now();
+    index.load(o.text("index"), load_options(o));
+    load_s = since(t0);
+    queries = read_table<float>(o.text("queries"));
+    if (queries.cols != index.dim()) throw std::runtime_error("query dimension does not match the index");
+    if (index.normalized()) katoann::normalize_rows(queries.cells.data(), queries.rows, queries.cols);
+    choose(o.text("query-ids"));
+  }
+  uint32_t dim() const { return queries.cols; }
+  // the chosen queries, back to back
+  std::vector<float> gathered() const {
+    std::vector<float> out(chosen.size() * static_cast<size_t>(dim()));
+    for (size_t i = 0; i < chosen.size(); ++i)
+      std::copy_n(queries.row(chosen[i]), dim(), out.data() + i * dim());
+    return out;
+  }
+
+ private:
+  void choose(const std::string &path) {
+    if (path.empty()) {
+      chosen.resize(queries.rows);
+      for (uint32_t i = 0; i < queries.rows; ++i) chosen[i] = i;
+      return;
+    }
+    std::unique_ptr<FILE, int (*)(FILE *)> f(std::fopen(path.c_str(), "r"), &std::fclose);
+    if (!f) throw std::runtime_error("cannot open " + path);
+    unsigned long v = 0;
+    while (std::fscanf(f.get(), "%lu", &v) == 1) {
+      if (v >= queries.rows) throw std::runtime_error("query id out of range in " + path);
+      chosen.push_back(static_cast<uint32_t>(v));
+    }
+    if (chosen.empty()) throw std::runtime_error("no query ids in " + path);
+  }
+};
+
+// recall@k: the share of each result row's ids found among the first k ids
+// of its query's ground-truth row.
+double recall(const std::vector<uint32_t> &ids, uint32_t k, const std::vector<uint32_t> &chosen,
+              const Table<uint32_t> &gt) {
+  size_t hits = 0;
+  std::vector<uint32_t> truth(k);
+  for (size_t i = 0; i < chosen.size(); ++i) {
+    std::copy_n(gt.row(chosen[i]), k, truth.begin());
+    std::sort(truth.begin(), truth.end());
+    for (uint32_t j = 0; j < k; ++j)
+      hits += std::binary_search(truth.begin(), truth.end(), ids[i * k + j]) ? 1 : 0;
+  }
+  return static_cast<double>(hits) / (static_cast<double>(chosen.size()) * k);
+}
+
+// One untimed pass, then `repeat` timed ones; their times sorted ascending.
+template <typename Pass>
+std::vector<double> timed_passes(uint32_t repeat, Pass pass) {
+  pass();
+  std::vector<double> secs(std::max(1u, repeat));
+  for (double &s : secs) {
+    const auto t0 = Clock::now();
+    pass();
+    s = since(t0);
+  }
+  std::sort(secs.begin(), secs.end());
+  return secs;
+}
+
+// --------------------------------------------------------------- commands
+int run_build(const Options &o) {
+  apply_threads(o);
+  Table<float> data = read_table<float>(o.text("data"));
+  katoann::BuildOptions bo;
+  bo.nlist = o.u32("nlist");
+  bo.train_size = o.u32("train-size");
+  bo.kmeans_iters = o.u32("iters");
+  bo.seed = o.u64_or("seed", 0);
+  if (o.on("normalize")) katoann::normalize_rows(data.cells.data(), data.rows, data.cols);
+  bo.normalized = o.on("normalize") || o.on("normalized");
+  const auto t0 = Clock::now();
+  katoann::Index::build(data.cells.data(), data.rows, data.cols, bo, o.text("out"));
+  JsonLine()
+      .count("vectors", data.rows)
+      .count("dim", data.cols)
+      .count("nlist", bo.nlist)
+      .fixed("build_s", since(t0), 1)
+      .print();
+  return 0;
+}
+
+int run_search(const Options &o) {
+  apply_threads(o);
+  Workload w(o);
+  const std::vector<float> q = w.gathered();
+  katoann::SearchParams p = search_params(o);
+  Table<uint32_t> gt;
+  const bool scored = o.given("gt");
+  if (scored) {
+    gt = read_table<uint32_t>(o.text("gt"));
+    if (gt.rows < w.queries.rows || gt.cols < p.k) throw std::runtime_error("ground truth too small");
+  }
+  const uint32_t batch = o.u32("batch");
+  const size_t total = w.chosen.size();
+  JsonLine()
+      .str("index", o.text("index"))
+      .str("engine", "gpu")
+      .sint("threads", omp_get_max_threads())
+      .fixed("load_s", w.load_s, 1)
+      .fixed("memory_gb", w.index.memory_bytes() / 1e9, 2)
+      .count("queries", total)
+      .count("prefix_dims", w.index.prefix_dims())
+      .print();
+  std::vector<uint32_t> ids(total * p.k);
+  std::vector<float> dists(total * p.k);
+  for (const uint32_t nprobe : o.list("nprobe")) {
+    p.nprobe = nprobe;
+    // the chosen queries in batches of --batch, in order
+    const std::vector<double> secs = timed_passes(o.u32("repeat"), [&] {
+      for (size_t at = 0; at < total; at += batch) {
+        const uint32_t n = static_cast<uint32_t>(std::min<size_t>(batch, total - at));
+        w.index.search(q.data() + at * w.dim(), n, p, ids.data() + at * p.k, dists.data() + at * p.k);
+      }
+    });
+    const double median = secs[secs.size() / 2];
+    JsonLine line;
+    line.count("nprobe", nprobe)
+        .count("k", p.k)
+        .count("survivors", p.survivors)
+        .count("batch", batch)
+        .fixed("qps", total / median, 1)
+        .fixed("seconds_median", median, 4)
+        .fixed("seconds_min", secs.front(), 4)
+        .fixed("seconds_max", secs.back(), 4);
+    if (scored) line.fixed("recall", recall(ids, p.k, w.chosen, gt), 5);
+    line.print();
+    if (o.given("out"))
+      write_results(o.text("out") + ".np" + std::to_string(nprobe) + ".bin",
+                    static_cast<uint32_t>(total), p.k, ids, dists);
+  }
+  return 0;
+}
+
+int run_budget(const Options &o) {
+  apply_threads(o);
+  Workload w(o);
+  const katoann::SearchParams sp = search_params(o);
+  katoann::ProbeTrainOptions to;
+  if (o.given("ladder")) to.ladder = o.list("ladder");
+  // ladder values beyond the index's lists cannot be probed
+  to.ladder.erase(std::remove_if(to.ladder.begin(), to.ladder.end(),
+                                 [&](uint32_t v) { return v > w.index.nlist(); }),
+                  to.ladder.end());
+  to.depth = o.u32_or("depth", std::min(256u, w.index.nlist()));
+  to.k = sp.k;
+  to.label_nprobe = o.u32("label-nprobe");
+  to.label_ranking = o.choice<katoann::Ranking>("label-ranking",
+                                                {{"full", katoann::Ranking::kFull},
+                                                 {"prefix", katoann::Ranking::kPrefix},
+                                                 {"high", katoann::Ranking::kHighBytes}},
+                                                "--label-ranking is full, prefix or high");
+  to.label_survivors = o.u32("label-survivors");
+  to.ranking = sp.ranking;
+  to.survivors = sp.survivors;
+  to.epochs = o.u32("epochs");
+  to.batch = o.u32("train-batch");
+  to.seed = o.u64_or("seed", 0);
+  const std::vector<float> q = w.gathered();
+  const auto t0 = Clock::now();
+  const katoann::ProbeModel m =
+      katoann::ProbeModel::train(w.index, q.data(), static_cast<uint32_t>(w.chosen.size()), to);
+  m.save(o.text("out"));
+  std::vector<uint64_t> per_class(m.classes(), 0);
+  for (const uint8_t label : m.labels()) ++per_class[label];
+  JsonLine()
+      .count("queries", w.chosen.size())
+      .count("classes", m.classes())
+      .count("depth", m.depth())
+      .fixed("train_s", since(t0), 2)
+      .fixed("loss_first", m.loss().front(), 4)
+      .fixed("loss_last", m.loss().back(), 4)
+      .list("label_histogram", per_class)
+      .print();
+  return 0;
+}
+
+int run_load(const Options &o) {
+  apply_threads(o);
+  Workload w(o);
+  const katoann::SearchParams sp = search_params(o);
+  // per-request k: one value, or a list drawn uniformly per request
+  const std::vector<uint32_t> kmix = o.given("k-mix") ? o.list("k-mix") : std::vector<uint32_t>{sp.k};
+  if (kmix.empty()) throw std::invalid_argument("empty --k-mix");
+  katoann::ServerOptions so;
+  so.max_batch = std::max(1u, std::min(4096u, o.u32("max-batch")));
+  so.max_in_flight = o.u32("in-flight");
+  so.hbm_budget = static_cast<size_t>(o.real("hbm-budget-gb") * 1e9);
+  so.max_k = *std::max_element(kmix.begin(), kmix.end());
+  so.nprobe = o.u32("nprobe");
+  so.ranking = sp.ranking;
+  so.survivors = sp.survivors;
+  so.max_wait_ms = o.real("max-wait-ms");
+  katoann::ProbeModel model;
+  if (o.given("budget")) {  // learned per-query nprobe, capped at --nprobe
+    model = katoann::ProbeModel::load(o.text("budget"));
+    so.budget = &model;
+    so.budget_threshold = static_cast<float>(o.real("threshold"));
+  }
+  const double rate = o.real("rate");
+  const uint32_t requests = o.u32("requests");
+  katoann::Server server(w.index, so);
+  // warm-up: one full batch per k of the mix
+  const uint32_t warm = std::min<uint32_t>(so.max_batch, static_cast<uint32_t>(w.chosen.size()));
+  std::vector<uint64_t> tickets;
+  for (const uint32_t k : kmix)
+    for (uint32_t i = 0; i < warm; ++i) tickets.push_back(server.submit(w.queries.row(w.chosen[i]), k));
+  for (const uint64_t t : tickets) server.wait(t);
+  const katoann::LoadReport r = katoann::run_load(server, w.queries.cells.data(), w.dim(), w.chosen,
+                                                  rate, requests, kmix, o.u64_or("seed", 42));
+  JsonLine()
+      .fixed("rate", rate, 1)
+      .count("requests", requests)
+      .count("nprobe", so.nprobe)
+      .str("engine", "gpu")
+      .fixed("achieved_qps", r.achieved_qps, 1)
+      .fixed("p50_ms", r.p50_ms, 2)
+      .fixed("p95_ms", r.p95_ms, 2)
+      .fixed("p99_ms", r.p99_ms, 2)
+      .fixed("max_ms", r.max_ms, 2)
+      .count("batches", r.batches)
+      .fixed("mean_batch", r.mean_batch, 1)
+      .count("in_flight", so.max_in_flight)
+      .count("peak_in_flight", r.peak_in_flight)
+      .fixed("peak_hbm_gb", r.peak_hbm_bytes / 1e9, 3)
+      .flag("learned", so.budget != nullptr)
+      .fixed("mean_nprobe", r.mean_nprobe, 2)
+      .fixed("max_lag_ms", r.max_lag_ms, 2)
+      .fixed("max_enqueue_ms", r.max_enqueue_ms, 2)
+      .fixed("max_batch_gpu_ms", r.max_batch_gpu_ms, 2)
+      .print();
+  return 0;
 }
 
 }  // namespace
 
 int main(int argc, char **argv) {
-  if (argc < 2) {
-    usage();
-    return 2;
+  const std::pair<const char *, std::pair<unsigned, int (*)(const Options &)>> commands[] = {
+      {"build", {kBuild, run_build}},
+      {"search", {kSearch, run_search}},
+      {"load", {kLoad, run_load}},
+      {"budget", {kBudget, run_budget}},
+  };
+  const std::string name = argc > 1 ? argv[1] : "";
+  for (const auto &c : commands) {
+    if (name != c.first) continue;
+    try {
+      return c.second.second(Options(c.second.first, argc, argv));
+    } catch (const std::exception &e) {
+      std::fprintf(stderr, "katoann: %s\n", e.what());
+      return 1;
+    }
   }
-  try {
-    const std::string cmd = argv[1];
-    const Args a = parse(argc, argv, 2);
-    if (cmd == "build") return cmd_build(a);
-    if (cmd == "search") return cmd_search(a);
-    if (cmd == "load") return cmd_load(a);
-    if (cmd == "budget") return cmd_budget(a);
-    usage();
-    return 2;
-  } catch (const std::exception &e) {
-    std::fprintf(stderr, "katoann: %s\n", e.what());
-    return 1;
-  }
+  usage();
+  return 2;
 }

@@ -401,15 +401,12 @@ int select_topp_ex(const float *dists, uint32_t nq, uint32_t n, uint32_t p, uint
   if (p == 0 || p > n || stride < p) return invalid("need 1 <= nprobe <= nlist");
   uint32_t np2 = 1;
   while (np2 < p) np2 <<= 1;
-  static bool attr_set = false;
-  if (!attr_set) {
-    KATO_CUDA(cudaFuncSetAttribute(select_topp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   kSortMax * 8));
-    KATO_CUDA(cudaFuncSetAttribute(select_topp_hist_kernel,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (kCand + kSortMax) * 8));
-    attr_set = true;
-  }
+  int rc;
+  if ((rc = smem_limit(reinterpret_cast<const void *>(select_topp_kernel), kSortMax * 8,
+                       "select_topp_kernel shared memory")) ||
+      (rc = smem_limit(reinterpret_cast<const void *>(select_topp_hist_kernel),
+                       (kCand + kSortMax) * 8, "select_topp_hist_kernel shared memory")))
+    return rc;
   if (p <= kSortMax) {
     // candidates and the sorted selection (the bitonic sort pads to a power of two)
     const size_t smem = (kCand + std::max<uint32_t>(np2, 2)) * sizeof(unsigned long long);

@@ -24,6 +24,12 @@
 // four narrow ones). Sixteen epilogue warps (thread = centroid row) rebuild
 // each l2 exactly in 64-bit integers and write the reference's float distance
 // (dist_value), 32 consecutive centroids per warp store.
+//
+// Rows wider than 1024 dimensions (the reference takes any dc up to kMaxDim
+// = 4096, include/katoann/kernels.h:177) are split into chunks of at most
+// 1024 dimensions. Each chunk is accumulated on its own in a TMEM slot, so
+// each chunk's sums stay exact in fp32; the epilogue drains every chunk and
+// adds the chunks' products in 64-bit integers before it writes a distance.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -40,6 +46,7 @@ constexpr uint32_t kCM = 128;     // centroids per tile (the MMA's M)
 constexpr uint32_t kQN = 64;      // queries per tile (the MMA's N)
 constexpr uint32_t kBK = 64;      // dimensions per stage (128 bytes of fp16)
 constexpr uint32_t kStages = 4;
+constexpr uint32_t kChunkSlices = 1024 / kBK;  // 64-dimension slices per exact chunk
 constexpr uint32_t kATile = kCM * kBK * 2;  // 16 KiB
 constexpr uint32_t kBTile = kQN * kBK * 2;  // 8 KiB
 constexpr uint32_t kStage = 2 * kATile + 2 * kBTile;
@@ -183,34 +190,41 @@ __global__ void __launch_bounds__(kThreads, 1)
       uint32_t s = 0, ph = 0, ab = 0, abph = 0;
       bool ok = true;
       for (uint32_t t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
-        if (!cwait(acc_empty + ab, abph ^ 1, err, pw[0])) break;
-        tc::fence_after();
-        const uint32_t d0 = tmem + ab * kAccCols;
-        for (uint32_t k = 0; k < nk; ++k) {
-          if (!cwait(full + s, ph, err, pw[1])) {
+        // one accumulator slot per chunk of at most 1024 dimensions
+        for (uint32_t k0 = 0; ok && k0 < nk; k0 += kChunkSlices) {
+          if (!cwait(acc_empty + ab, abph ^ 1, err, pw[0])) {
             ok = false;
             break;
           }
           tc::fence_after();
-          const uint32_t st = tc::smem_addr(sm + s * kStage);
-          const uint64_t ah = desc_sw128(st), al = desc_sw128(st + kATile);
-          // the high-plane query tile (64 rows) is followed by the low-plane
-          // one at the next 1 KiB boundary, in the same swizzle: one operand
-          // of 128 rows, 8-row groups 1024 bytes apart
-          const uint64_t b = desc_sw128(st + 2 * kATile);
+          const uint32_t d0 = tmem + ab * kAccCols;
+          const uint32_t k1 = min(nk, k0 + kChunkSlices);
+          for (uint32_t k = k0; k < k1; ++k) {
+            if (!cwait(full + s, ph, err, pw[1])) {
+              ok = false;
+              break;
+            }
+            tc::fence_after();
+            const uint32_t st = tc::smem_addr(sm + s * kStage);
+            const uint64_t ah = desc_sw128(st), al = desc_sw128(st + kATile);
+            // the high-plane query tile (64 rows) is followed by the low-plane
+            // one at the next 1 KiB boundary, in the same swizzle: one operand
+            // of 128 rows, 8-row groups 1024 bytes apart
+            const uint64_t b = desc_sw128(st + 2 * kATile);
 #pragma unroll
-          for (uint32_t j = 0; j < kBK / 16; ++j) {
-            const uint32_t acc = (k | j) != 0;
-            // a 16-dimension step is 32 bytes along the swizzled row: +2 encoded
-            tc::mma_f16(d0 + 0 * kQN, ah + 2 * j, b + 2 * j, idesc, acc);  // HH, HL
-            tc::mma_f16(d0 + 2 * kQN, al + 2 * j, b + 2 * j, idesc, acc);  // LH, LL
+            for (uint32_t j = 0; j < kBK / 16; ++j) {
+              const uint32_t acc = (k != k0 || j != 0);
+              // a 16-dimension step is 32 bytes along the swizzled row: +2 encoded
+              tc::mma_f16(d0 + 0 * kQN, ah + 2 * j, b + 2 * j, idesc, acc);  // HH, HL
+              tc::mma_f16(d0 + 2 * kQN, al + 2 * j, b + 2 * j, idesc, acc);  // LH, LL
+            }
+            tc::commit(empty + s);
+            if (++s == kStages) s = 0, ph ^= 1;
           }
-          tc::commit(empty + s);
-          if (++s == kStages) s = 0, ph ^= 1;
+          if (!ok) break;
+          tc::commit(acc_full + ab);
+          if (++ab == 2) ab = 0, abph ^= 1;
         }
-        if (!ok) break;
-        tc::commit(acc_full + ab);
-        if (++ab == 2) ab = 0, abph ^= 1;
       }
       // every MMA issued has completed before tensor memory is released
       tc::commit(done);
@@ -222,16 +236,25 @@ __global__ void __launch_bounds__(kThreads, 1)
     // a lane quarter take 16 query columns each
     const uint32_t q4 = warp & 3, part = (warp - 2) >> 2;
     const uint32_t row = q4 * 32 + lane;
+    const uint32_t nchunks = div_up(nk, kChunkSlices);
     uint32_t ab = 0, abph = 0;
-    for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    bool ok = true;
+    for (uint32_t t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
       const uint32_t c = (t % nct) * kCM + row, qb = (t / nct) * kQN + part * 16;
       const int64_t ct = c < A.n ? A.cterm[c] : 0;
       // lane j < 16 holds query qb + j's term; the pairs take it by shuffle
       const int64_t qt_lane = (lane < 16 && qb + lane < A.m) ? A.qterm[qb + lane] : 0;
-      if (!__all_sync(0xffffffffu, cwait(acc_full + ab, abph, err, pw[0]))) break;
-      tc::fence_after();
-      const uint32_t taddr = tmem + ((q4 * 32u) << 16) + ab * kAccCols + part * 16;
-      {
+      // the centred cross product of each query column, summed over the chunks
+      int64_t p[16];
+#pragma unroll
+      for (uint32_t j = 0; j < 16; ++j) p[j] = 0;
+      for (uint32_t ch = 0; ch < nchunks; ++ch) {
+        if (!__all_sync(0xffffffffu, cwait(acc_full + ab, abph, err, pw[0]))) {
+          ok = false;
+          break;
+        }
+        tc::fence_after();
+        const uint32_t taddr = tmem + ((q4 * 32u) << 16) + ab * kAccCols + part * 16;
         // columns: HH (centroid high x query high), HL, LH, LL
         uint32_t hh[16], hl[16], lh[16], ll[16];
         tc::tmem_ld16(taddr + 0 * kQN, hh);
@@ -240,21 +263,25 @@ __global__ void __launch_bounds__(kThreads, 1)
         tc::tmem_ld16(taddr + 3 * kQN, ll);
         tc::tmem_wait_ld();
 #pragma unroll
-        for (uint32_t j = 0; j < 16; ++j) {
-          const uint32_t q = qb + j;
-          const int64_t qt = __shfl_sync(0xffffffffu, qt_lane, j);
-          if (q >= A.m || c >= A.n) continue;
-          const int64_t p = 65536ll * __float2int_rn(__uint_as_float(hh[j])) +
-                            256ll * (__float2int_rn(__uint_as_float(hl[j])) +
-                                     __float2int_rn(__uint_as_float(lh[j]))) +
-                            __float2int_rn(__uint_as_float(ll[j]));
-          A.out[static_cast<size_t>(q) * A.n + c] = dist_value(qt + ct - 2 * p, A.scale);
-        }
+        for (uint32_t j = 0; j < 16; ++j)
+          p[j] += 65536ll * __float2int_rn(__uint_as_float(hh[j])) +
+                  256ll * (__float2int_rn(__uint_as_float(hl[j])) +
+                           __float2int_rn(__uint_as_float(lh[j]))) +
+                  __float2int_rn(__uint_as_float(ll[j]));
+        // the slot has been read: hand it back for the next chunk or tile
+        tc::fence_before();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(acc_empty + ab);
+        if (++ab == 2) ab = 0, abph ^= 1;
       }
-      tc::fence_before();
-      __syncwarp();
-      if (lane == 0) tc::mbar_arrive(acc_empty + ab);
-      if (++ab == 2) ab = 0, abph ^= 1;
+      if (!ok) break;
+#pragma unroll
+      for (uint32_t j = 0; j < 16; ++j) {
+        const uint32_t q = qb + j;
+        const int64_t qt = __shfl_sync(0xffffffffu, qt_lane, j);
+        if (q >= A.m || c >= A.n) continue;
+        A.out[static_cast<size_t>(q) * A.n + c] = dist_value(qt + ct - 2 * p[j], A.scale);
+      }
     }
   }
   if (A.prof && lane == 0 && warp <= 2) {
@@ -301,26 +328,23 @@ int centre_planes(const uint8_t *hi, const uint8_t *lo, const int64_t *norm, uin
   return KATO_OK;
 }
 
-bool coarse_tc_ok(uint32_t dc) { return dc >= kBK && dc % kBK == 0 && dc <= 1024; }
+bool coarse_tc_ok(uint32_t dc) { return dc >= kBK && dc % kBK == 0 && dc <= 4096; }
 
 int coarse_tc(const __half *ch, const __half *cl, const int64_t *cterm, uint32_t n, const __half *qh,
               const __half *ql, const int64_t *qterm, uint32_t m, uint32_t dc, double step_sq,
               float *out, uint32_t *timeouts, unsigned long long *prof, cudaStream_t st) {
   if (m == 0 || n == 0) return KATO_OK;
-  if (!coarse_tc_ok(dc)) return invalid("the tensor-core coarse product needs dc in [64, 1024], a multiple of 64");
+  if (!coarse_tc_ok(dc)) return invalid("the tensor-core coarse product needs dc in [64, 4096], a multiple of 64");
   CUtensorMap mch, mcl, mqh, mql;
   int rc;
   if ((rc = encode_plane(&mch, ch, n, dc, kCM)) || (rc = encode_plane(&mcl, cl, n, dc, kCM)) ||
       (rc = encode_plane(&mqh, qh, m, dc, kQN)) || (rc = encode_plane(&mql, ql, m, dc, kQN)))
     return rc;
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    KATO_CUDA(cudaGetDevice(&dev));
-    KATO_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    KATO_CUDA(cudaFuncSetAttribute(coarse_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   static_cast<int>(kSmem)));
-  }
+  int sms = 0;
+  if ((rc = current_sms(&sms)) ||
+      (rc = smem_limit(reinterpret_cast<const void *>(coarse_tc_kernel), static_cast<int>(kSmem),
+                       "coarse_tc_kernel shared memory")))
+    return rc;
   const CoarseArgs A{cterm, qterm, out, m, n, dc, make_dist_scale(step_sq), timeouts, prof};
   const uint32_t ntiles = div_up(n, kCM) * div_up(m, kQN);
   coarse_tc_kernel<<<std::min<uint32_t>(ntiles, sms), kThreads, kSmem, st>>>(mch, mcl, mqh, mql, A);

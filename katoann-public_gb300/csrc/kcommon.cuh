@@ -27,6 +27,15 @@ int cuda_status(cudaError_t e, const char *what);
     if (e_ != cudaSuccess) return ::kato::cuda_status(e_, what);       \
   } while (0)
 
+// One-time device settings, kept per device and safe from any thread (a
+// server's dispatcher and the callers' threads may make first calls at once,
+// and one process may drive several GPUs).
+// The SM count of the current device.
+int current_sms(int *sms);
+// Raises `kernel`'s dynamic shared-memory limit on the current device to at
+// least `bytes` (once per device and kernel).
+int smem_limit(const void *kernel, int bytes, const char *what);
+
 inline int invalid(const std::string &msg) {
   set_error(msg);
   return KATO_EINVAL;

@@ -476,12 +476,9 @@ int probe_features(const float *cd, uint32_t L, const uint32_t *probed, uint32_t
 int probe_budget(const katoann_gpu_probe_model &m, const float *z, uint32_t B, uint32_t cap,
                  float *probs, uint32_t *nprobe, cudaStream_t st) {
   if (B == 0) return KATO_OK;
-  static bool attr = false;
-  if (!attr) {
-    KATO_CUDA(cudaFuncSetAttribute(probe_mlp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   static_cast<int>(kMlpSmem)));
-    attr = true;
-  }
+  if (const int rc = smem_limit(reinterpret_cast<const void *>(probe_mlp_kernel),
+                                static_cast<int>(kMlpSmem), "probe_mlp_kernel shared memory"))
+    return rc;
   const MlpArgs a{m.d_shift, m.d_scale, m.d_w1, m.d_w2, m.d_w3, m.d_b1,
                   m.d_b2,    m.d_b3,    m.d_ladder, m.nclass, m.threshold};
   probe_mlp_kernel<<<div_up(B, kQB), kH, kMlpSmem, st>>>(z, B, a, cap, probs, nprobe);

@@ -74,9 +74,13 @@ struct Bars {
       *xn_full, *done;
 };
 
+// Barrier slots in order: raw full/empty (4 each, at most), A full/empty,
+// query buffers full/empty (2 each, at most), accumulators full/empty, row
+// norms full, done.
 __device__ __forceinline__ Bars bars_at(unsigned char *sm, const TcSmem &L) {
   uint64_t *b = reinterpret_cast<uint64_t *>(sm + L.bars);
-  return Bars{b, b + 4, b + 8, b + 10, b + 12, b + 14, b + 16, b + 18, b + 20, b + 22};
+  uint64_t *a = b + 8, *q = a + 2 * kTcAStages, *c = q + 4;
+  return Bars{b, b + 4, a, a + kTcAStages, q, q + 2, c, c + kTcAcc, c + 2 * kTcAcc, c + 3 * kTcAcc};
 }
 
 // sum over 16 bytes of (b - 128)^2 = sum b^2 - 256 sum b + 16 * 16384
@@ -136,7 +140,6 @@ __device__ __forceinline__ uint32_t mma_width(uint32_t ne) {
 }
 
 // A pipeline wait that also adds the cycles it took to `acc`.
-// A pipeline wait that also adds the cycles it took to `acc`.
 __device__ __forceinline__ bool timed_wait(uint64_t *b, uint32_t phase, volatile uint32_t *err,
                                            unsigned long long &acc) {
   const long long t = clock64();
@@ -169,6 +172,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     for (uint32_t s = 0; s < kTcAStages; ++s) {
       tc::mbar_init(bar.a_full + s, kConvWarps);
       tc::mbar_init(bar.a_empty + s, 1);
+    }
+    for (uint32_t s = 0; s < kTcAcc; ++s) {
       tc::mbar_init(bar.acc_full + s, 1);
       tc::mbar_init(bar.acc_empty + s, kEpiWarps);
       tc::mbar_init(bar.xn_full + s, kConvWarps);
@@ -188,7 +193,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   __syncthreads();
   tc::fence_after();
   const uint32_t tmem = *tbase;
-  const uint32_t acol = kTcAStages * N;  // TMEM columns of the A stages follow the accumulators
+  const uint32_t acol = kTcAcc * N;  // TMEM columns of the A stages follow the accumulators
   const uint32_t nitems = *A.nitems;
   const uint32_t T = nitems ? A.tile_off[nitems] : 0;
   uint32_t t0, t1;
@@ -279,7 +284,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         sxn[(ab * 2 + hf) * kTcRows + r] = xs;
         __syncwarp();
         if (lane == 0) tc::mbar_arrive(bar.xn_full + ab);
-        if (++ab == kTcAStages) ab = 0, abph ^= 1;
+        if (++ab == kTcAcc) ab = 0, abph ^= 1;
       }
     } else if (warp < kTmaWarp) {
       // ---- epilogue: thread = row (its TMEM lane), warpgroup = column half
@@ -378,7 +383,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         tc::fence_before();
         __syncwarp();
         if (lane == 0) tc::mbar_arrive(bar.acc_empty + ab);
-        if (++ab == kTcAStages) ab = 0, abph ^= 1;
+        if (++ab == kTcAcc) ab = 0, abph ^= 1;
         ++tiles;
         if (w.last()) {
           __syncwarp();
@@ -456,7 +461,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           }
           if (!ok) break;
           tc::commit(bar.acc_full + ab);
-          if (++ab == kTcAStages) ab = 0, abph ^= 1;
+          if (++ab == kTcAcc) ab = 0, abph ^= 1;
           if (w.last()) {
             tc::commit(bar.b_empty + ib);
             if (++ib == S.Bs) ib = 0, bph ^= 1;
@@ -1020,13 +1025,8 @@ __global__ void __launch_bounds__(512) tc_bucket_kernel(const uint4 *__restrict_
 }  // namespace
 
 uint32_t rank_tc_ctas() {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-      sms = 0;
-  }
+  int sms = 0;
+  if (current_sms(&sms) != KATO_OK) sms = 1;
   return static_cast<uint32_t>(std::max(sms, 1));
 }
 
@@ -1039,9 +1039,9 @@ bool rank_tc_plan(uint32_t h, uint32_t dc, TcShape *s) {
   const uint32_t cap = g_tc_width.load();
   if (cap >= 16 && cap < t.N) t.N = cap;
   t.inner = dc >= 128 ? 128 : 64;
-  // accumulators (two slots of N columns), then the two A stages (inner / 2 columns each)
+  // accumulators (kTcAcc slots of N columns), then the A stages (inner / 2 columns each)
   t.tcols = 32;
-  while (t.tcols < kTcAStages * t.N + kTcAStages * t.inner / 2) t.tcols <<= 1;
+  while (t.tcols < kTcAcc * t.N + kTcAStages * t.inner / 2) t.tcols <<= 1;
   for (uint32_t bs = 2; bs >= 1; --bs)
     for (uint32_t rs = 4; rs >= 2; --rs) {
       t.Bs = bs;
@@ -1075,8 +1075,9 @@ int rank_tc(const RankTcArgs &A, const uint8_t *xhi, uint32_t npts, const TcShap
   }
   const uint32_t ctas = rank_tc_ctas();
   auto go = [&](auto kern) -> int {
-    KATO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   static_cast<int>(s.smem)));
+    if (const int rc = smem_limit(reinterpret_cast<const void *>(kern), static_cast<int>(s.smem),
+                                  "rank_tc_kernel shared memory"))
+      return rc;
     kern<<<ctas, kTcThreads, s.smem, st>>>(tmap, A, s);
     KATO_LAUNCHED("rank_tc_kernel");
     return KATO_OK;
@@ -1103,12 +1104,9 @@ int rank_seed(const uint8_t *xhi, const int64_t *xnorm, const uint8_t *qhi, cons
   if (B == 0) return KATO_OK;
   const uint32_t *ord = nullptr;
   if (order && L <= kOrderLists) {
-    static bool attr = false;
-    if (!attr) {
-      KATO_CUDA(cudaFuncSetAttribute(seed_order_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     static_cast<int>(kOrderLists * 4)));
-      attr = true;
-    }
+    if (const int rc = smem_limit(reinterpret_cast<const void *>(seed_order_kernel),
+                                  static_cast<int>(kOrderLists * 4), "seed_order_kernel shared memory"))
+      return rc;
     seed_order_kernel<<<1, 1024, L * 4, st>>>(probed, p, B, L, order);
     KATO_LAUNCHED("seed_order_kernel");
     ord = order;

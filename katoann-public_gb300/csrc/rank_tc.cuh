@@ -56,10 +56,17 @@ __host__ __device__ inline uint32_t tc_take(uint32_t &o, uint32_t bytes, uint32_
 }
 
 constexpr uint32_t kTcRows = 128;                        // rows per tile (the MMA's M)
-constexpr uint32_t kTcAStages = 2;                       // converted row tiles
+#ifndef KATO_RANK_ASTAGES
+#define KATO_RANK_ASTAGES 2
+#endif
+#ifndef KATO_RANK_ACC
+#define KATO_RANK_ACC 2
+#endif
+constexpr uint32_t kTcAStages = KATO_RANK_ASTAGES;       // converted row chunks (TMEM)
+constexpr uint32_t kTcAcc = KATO_RANK_ACC;               // accumulator slots (TMEM)
 constexpr uint32_t kTcATile = kTcRows * 128 * 2;         // 128 rows x 128 dims of fp16
 constexpr uint32_t kTcQInfo = 16;                        // bytes per query slot
-constexpr uint32_t kTcBars = 24;                         // barrier slots
+constexpr uint32_t kTcBars = 8 + 2 * kTcAStages + 4 + 3 * kTcAcc + 1;  // barrier slots
 
 __host__ __device__ inline TcSmem tc_smem_layout(uint32_t h, const TcShape &s) {
   TcSmem L{};
@@ -70,7 +77,7 @@ __host__ __device__ inline TcSmem tc_smem_layout(uint32_t h, const TcShape &s) {
   L.qinfo = tc_take(o, s.Bs * s.N * kTcQInfo, 16);
   L.qbv = tc_take(o, s.Bs * s.N * 4, 16);
   L.width = tc_take(o, 2 * 4, 16);
-  L.sxn = tc_take(o, kTcAStages * 2 * kTcRows * 4, 16);
+  L.sxn = tc_take(o, kTcAcc * 2 * kTcRows * 4, 16);
   L.bars = tc_take(o, kTcBars * 8, 8);
   L.tbase = tc_take(o, 4, 4);
   L.err = tc_take(o, 4, 4);

@@ -1046,8 +1046,9 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
   const size_t smem = rank_smem_bytes(full ? 2 : 1, pl.select, pl.dims, pl.SC);
   if (!pl.tc && smem > 227 * 1024) return invalid("ranking tile does not fit in shared memory");
   auto launch = [&](auto kern) -> int {
-    KATO_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   static_cast<int>(smem)));
+    if (const int rc2 = smem_limit(reinterpret_cast<const void *>(kern), static_cast<int>(smem),
+                                   "rank_kernel shared memory"))
+      return rc2;
     kern<<<grid, kThreads, smem, st>>>(A);
     KATO_LAUNCHED("rank_kernel");
     return KATO_OK;
@@ -1063,8 +1064,9 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
   uint32_t np2 = 1;
   while (np2 < pl.S) np2 <<= 1;
   const size_t msmem = static_cast<size_t>(np2) * 12;
-  KATO_CUDA(cudaFuncSetAttribute(merge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(msmem)));
+  if ((rc = smem_limit(reinterpret_cast<const void *>(merge_kernel), static_cast<int>(msmem),
+                       "merge_kernel shared memory")))
+    return rc;
   merge_kernel<<<nq, kThreads, msmem, st>>>(slots, pl.tc ? pl.cap : p * pl.SC, qcount, qprobes,
                                             pl.SC, ix->d_ids, pl.S, full, pl.k, surv, nsurv,
                                             out_ids, out_dists, stats + 1);
@@ -1079,8 +1081,9 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
   // 6. exact refinement and top-k (:1081-1125)
   const size_t rsmem = static_cast<size_t>(dc) * 2 + static_cast<size_t>(pl.S) * 12 +
                        static_cast<size_t>(pl.k) * 8;
-  KATO_CUDA(cudaFuncSetAttribute(refine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(rsmem)));
+  if ((rc = smem_limit(reinterpret_cast<const void *>(refine_kernel), static_cast<int>(rsmem),
+                       "refine_kernel shared memory")))
+    return rc;
   refine_kernel<<<nq, kThreads, rsmem, st>>>(qhi, qlo, qn, ix->d_hi, ix->d_lo, ix->d_norm,
                                              ix->d_ids, ix->npts, dc, surv, nsurv, pl.S, pl.k,
                                              make_dist_scale(ix->step_sq), out_ids, out_dists);
