@@ -17,6 +17,7 @@
 #include <mutex>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "katoann/index.h"
@@ -317,76 +318,101 @@ void Index::load(const std::string &prefix, const LoadOptions &opt) {
   }
 }
 
+namespace {
+
+// One index file read front to back. take() fills its target completely or
+// reports a short read; the file is closed with the reader.
+class FileIn {
+ public:
+  explicit FileIn(std::string path) : path_(std::move(path)), f_(std::fopen(path_.c_str(), "rb")) {}
+  ~FileIn() {
+    if (f_) std::fclose(f_);
+  }
+  FileIn(const FileIn &) = delete;
+  FileIn &operator=(const FileIn &) = delete;
+  bool open() const { return f_ != nullptr; }
+  const std::string &path() const { return path_; }
+  template <typename T>
+  bool take(T *dst, size_t count) {
+    return count == 0 || std::fread(dst, sizeof(T), count, f_) == count;
+  }
+  // A file the index cannot do without: "cannot open <path>" if it is absent.
+  FileIn &required() {
+    if (!f_) throw std::runtime_error("cannot open " + path_);
+    return *this;
+  }
+
+ private:
+  std::string path_;
+  FILE *f_;
+};
+
+}  // namespace
+
+// The reference's index files (src/index.cpp:482-505 and :535-545 write them):
+//   .meta       u32 dim, nlist, rows [, metric (0 = L2), normalized]
+//   .centroids  nlist x dim f32
+//   .invlist    per list: u32 size, size u32 ids, size x dim f32 vectors
+//   .dimc       u32 magic, version, dim, nlist, rows, head dims, rotated, 0
+//               [, dim x dim f32 rotation]  (optional file)
 void Index::load_files(const std::string &prefix, const LoadOptions &opt) {
   IndexArrays a;
   std::vector<float> centroids, vectors, rotation;
   std::vector<uint32_t> sizes, ids;
-  {
-    std::ifstream f(prefix + ".meta", std::ios::binary);
-    if (!f) throw std::runtime_error("cannot open " + prefix + ".meta");
-    uint32_t meta[3] = {0, 0, 0};
-    f.read(reinterpret_cast<char *>(meta), sizeof(meta));
-    if (!f) throw std::runtime_error("truncated " + prefix + ".meta");
-    a.dim = meta[0];
-    a.nlist = meta[1];
-    a.npts = meta[2];
-    uint32_t extra[2] = {0, 0};
-    f.read(reinterpret_cast<char *>(extra), sizeof(extra));
-    if (f.gcount() == static_cast<std::streamsize>(sizeof(extra))) {
-      if (extra[0] != 0) throw std::runtime_error("only the L2 metric is supported");
-      a.normalized = extra[1] != 0;
-    }
+
+  FileIn meta(prefix + ".meta");
+  meta.required();
+  uint32_t head[5] = {0, 0, 0, 0, 0};
+  if (!meta.take(head, 3)) throw std::runtime_error("truncated " + meta.path());
+  if (meta.take(head + 3, 2)) {  // the metric and normalization words came later
+    if (head[3] != 0) throw std::runtime_error("only the L2 metric is supported");
+    a.normalized = head[4] != 0;
   }
+  a.dim = head[0];
+  a.nlist = head[1];
+  a.npts = head[2];
   if (a.dim == 0 || a.dim > kMaxDim || a.nlist == 0)
-    throw std::runtime_error("bad header in " + prefix + ".meta");
-  centroids.assign(static_cast<size_t>(a.nlist) * a.dim, 0.0f);
-  {
-    std::ifstream f(prefix + ".centroids", std::ios::binary);
-    f.read(reinterpret_cast<char *>(centroids.data()), centroids.size() * sizeof(float));
-    if (!f) throw std::runtime_error("cannot read " + prefix + ".centroids");
+    throw std::runtime_error("bad header in " + meta.path());
+
+  FileIn cen(prefix + ".centroids");
+  centroids.resize(static_cast<size_t>(a.nlist) * a.dim);
+  if (!cen.open() || !cen.take(centroids.data(), centroids.size()))
+    throw std::runtime_error("cannot read " + cen.path());
+
+  // lists in file order; the sizes must add up to the rows of .meta exactly
+  FileIn inv(prefix + ".invlist");
+  inv.required();
+  sizes.assign(a.nlist, 0);
+  ids.reserve(a.npts);
+  vectors.reserve(static_cast<size_t>(a.npts) * a.dim);
+  uint64_t rows = 0;
+  bool whole = true;
+  for (uint32_t c = 0; c < a.nlist && whole; ++c) {
+    uint32_t n = 0;
+    whole = inv.take(&n, 1) && rows + n <= a.npts;
+    if (!whole) break;
+    ids.resize(rows + n);
+    vectors.resize((rows + n) * a.dim);
+    whole = inv.take(ids.data() + rows, n) && inv.take(vectors.data() + rows * a.dim, size_t{n} * a.dim);
+    sizes[c] = n;
+    rows += n;
   }
-  {
-    std::ifstream f(prefix + ".invlist", std::ios::binary);
-    if (!f) throw std::runtime_error("cannot open " + prefix + ".invlist");
-    sizes.assign(a.nlist, 0);
-    uint64_t total = 0;
-    for (uint32_t c = 0; c < a.nlist && f; ++c) {
-      uint32_t sz = 0;
-      f.read(reinterpret_cast<char *>(&sz), sizeof(sz));
-      if (!f) break;
-      if (total + sz > a.npts) {
-        total += sz;
-        break;
-      }
-      sizes[c] = sz;
-      const size_t r0 = ids.size();
-      ids.resize(r0 + sz);
-      f.read(reinterpret_cast<char *>(ids.data() + r0), static_cast<std::streamsize>(sz) * 4);
-      vectors.resize((r0 + sz) * static_cast<size_t>(a.dim));
-      f.read(reinterpret_cast<char *>(vectors.data() + r0 * a.dim),
-             static_cast<std::streamsize>(sz) * a.dim * sizeof(float));
-      total += sz;
-    }
-    if (!f || total != a.npts) throw std::runtime_error("truncated " + prefix + ".invlist");
-  }
-  {
-    std::ifstream f(prefix + ".dimc", std::ios::binary);
-    if (f) {
-      uint32_t hdr[8] = {0};
-      f.read(reinterpret_cast<char *>(hdr), sizeof(hdr));
-      if (!f || hdr[0] != kDimcMagic || (hdr[1] != 1u && hdr[1] != 2u))
-        throw std::runtime_error("bad header in " + prefix + ".dimc");
-      if (hdr[2] != a.dim || hdr[3] != a.nlist || hdr[4] != a.npts)
-        throw std::runtime_error(prefix + ".dimc does not match the index");
-      a.has_dimc = true;
-      a.head_dims = hdr[5];
-      if (hdr[6] == 1u) {
-        rotation.resize(static_cast<size_t>(a.dim) * a.dim);
-        f.read(reinterpret_cast<char *>(rotation.data()),
-               static_cast<std::streamsize>(rotation.size() * sizeof(float)));
-        if (!f) throw std::runtime_error("truncated rotation in " + prefix + ".dimc");
-        a.rotation = rotation.data();
-      }
+  if (!whole || rows != a.npts) throw std::runtime_error("truncated " + inv.path());
+
+  FileIn dimc(prefix + ".dimc");  // optional: without it, no rotation and no prefix ranking
+  if (dimc.open()) {
+    uint32_t h[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // magic, version, dim, nlist, rows, head, rotated, 0
+    if (!dimc.take(h, 8) || h[0] != kDimcMagic || h[1] < 1u || h[1] > 2u)
+      throw std::runtime_error("bad header in " + dimc.path());
+    if (h[2] != a.dim || h[3] != a.nlist || h[4] != a.npts)
+      throw std::runtime_error(dimc.path() + " does not match the index");
+    a.has_dimc = true;
+    a.head_dims = h[5];
+    if (h[6] == 1u) {
+      rotation.resize(static_cast<size_t>(a.dim) * a.dim);
+      if (!dimc.take(rotation.data(), rotation.size()))
+        throw std::runtime_error("truncated rotation in " + dimc.path());
+      a.rotation = rotation.data();
     }
   }
   a.centroids = centroids.data();

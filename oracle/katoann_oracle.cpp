@@ -68,33 +68,50 @@ inline float mul_add(float s, float x, float r) {
 // elements at a time with the products rounded before each in-order add, and
 // the remaining (length % 4) elements are fused. Dimensions that are a
 // multiple of 16 never reach either chain.
-inline float rotate_dot(const float *x, const float *r, uint32_t d, bool lanes) {
-  if (!lanes) {
-    float s = 0.0f;
-    const uint32_t m = d & ~3u;
-    uint32_t k = 0;
-    for (; k < m; ++k) s = mul_add(s, x[k], r[k]);
-    for (; k < d; ++k) s = std::fmaf(x[k], r[k], s);
-    return s;
-  }
-  float acc[16] = {0};
-  uint32_t k = 0;
-  for (; k + 16 <= d; k += 16)
-    for (int l = 0; l < 16; ++l) acc[l] = std::fmaf(x[k + l], r[k + l], acc[l]);
-  float s = reduce16(acc);
+// The scalar chain over dimensions [k, d) after the lanes: products rounded
+// before each add for the first (d - k) & ~3 of them, fused for the rest.
+inline float dot_tail(const float *x, const float *r, uint32_t k, uint32_t d, float s) {
   const uint32_t m = k + ((d - k) & ~3u);
   for (; k < m; ++k) s = mul_add(s, x[k], r[k]);
   for (; k < d; ++k) s = std::fmaf(x[k], r[k], s);
   return s;
 }
 
+inline float rotate_dot(const float *x, const float *r, uint32_t d, bool lanes) {
+  if (!lanes) return dot_tail(x, r, 0, d, 0.0f);
+  float acc[16] = {0};
+  uint32_t k = 0;
+  for (; k + 16 <= d; k += 16)
+    for (int l = 0; l < 16; ++l) acc[l] = std::fmaf(x[k + l], r[k + l], acc[l]);
+  return dot_tail(x, r, k, d, reduce16(acc));
+}
+
+// Every output is rotate_dot's arithmetic. For speed (a 10M-row index is
+// coded here), four rows share each pass over a rotation row, and a thread
+// walks 32 rows against all columns so that their values stay in cache.
 void rotate_rows(const float *in, float *out, size_t nrows, uint32_t d, const float *rot) {
-  const uint32_t d4 = d & ~3u;
-#pragma omp parallel for schedule(static)
-  for (int64_t i = 0; i < static_cast<int64_t>(nrows); ++i)
-    for (uint32_t j = 0; j < d; ++j)
-      out[static_cast<size_t>(i) * d + j] =
-          rotate_dot(in + static_cast<size_t>(i) * d, rot + static_cast<size_t>(j) * d, d, j < d4);
+  const uint32_t d4 = d & ~3u, d16 = d & ~15u;
+  constexpr size_t kTile = 32, kSub = 4;
+  const int64_t tiles = static_cast<int64_t>((nrows + kTile - 1) / kTile);
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int64_t t = 0; t < tiles; ++t) {
+    const size_t i0 = static_cast<size_t>(t) * kTile, i1 = std::min(nrows, i0 + kTile);
+    for (uint32_t j = 0; j < d; ++j) {
+      const float *r = rot + static_cast<size_t>(j) * d;
+      size_t i = i0;
+      for (; j < d4 && i + kSub <= i1; i += kSub) {
+        const float *x[kSub];
+        for (size_t u = 0; u < kSub; ++u) x[u] = in + (i + u) * d;
+        float acc[kSub][16] = {};
+        for (uint32_t k = 0; k < d16; k += 16)
+          for (size_t u = 0; u < kSub; ++u)
+            for (int l = 0; l < 16; ++l) acc[u][l] = std::fmaf(x[u][k + l], r[k + l], acc[u][l]);
+        for (size_t u = 0; u < kSub; ++u)
+          out[(i + u) * d + j] = dot_tail(x[u], r, d16, d, reduce16(acc[u]));
+      }
+      for (; i < i1; ++i) out[i * d + j] = rotate_dot(in + i * d, r, d, j < d4);
+    }
+  }
 }
 
 // Quantization of one value, src/index.cpp:669-670 (also :735-736, :925-926).
@@ -191,10 +208,10 @@ void read_files(Index &x, const std::string &prefix, std::vector<float> &raw, ui
 
 // Coding of an index whose files have been read (src/index.cpp:613-750,
 // :777-807): raw holds the unrotated vectors in list order.
-void code_index(Index *x, std::vector<float> &raw, uint32_t dims) {
+void code_index(Index *x, std::vector<float> &raw, uint32_t dims, bool raw_rotated = false) {
   const uint32_t d = x->dim;
   const size_t n = x->npts;
-  if (x->rotated && n) {
+  if (x->rotated && n && !raw_rotated) {
     std::vector<float> tmp(raw.size());
     rotate_rows(raw.data(), tmp.data(), n, d, x->rotation.data());
     raw.swap(tmp);
@@ -531,6 +548,64 @@ void *oracle_load_arrays(uint32_t dim, uint32_t nlist, uint32_t npts, const floa
         std::vector<float> raw(vectors, vectors + static_cast<size_t>(npts) * dim);
         oracle::code_index(x.get(), raw, head_dims);
         out = x.release();
+      }))
+    return nullptr;
+  return out;
+}
+
+// An oracle index coded from rows handed over in pieces, so that a large
+// index never needs a second full copy of its unrotated vectors:
+// oracle_code_begin takes the index's shape, oracle_code_rows rotates rows
+// [row0, row0 + nrows) into place, oracle_code_finish codes them all.
+struct PendingIndex {
+  std::unique_ptr<Index> x;
+  std::vector<float> raw;  // rotated (or copied) rows
+  uint32_t head_dims = 0;
+};
+
+void *oracle_code_begin(uint32_t dim, uint32_t nlist, uint32_t npts, const float *centroids,
+                        const uint32_t *list_sizes, const uint32_t *ids, const float *rotation,
+                        uint32_t head_dims) {
+  PendingIndex *out = nullptr;
+  if (oracle::guarded([&] {
+        auto p = std::make_unique<PendingIndex>();
+        p->x = std::make_unique<Index>();
+        Index *x = p->x.get();
+        x->dim = dim;
+        x->nlist = nlist;
+        x->npts = npts;
+        x->centroids.assign(centroids, centroids + static_cast<size_t>(nlist) * dim);
+        x->list_off.assign(nlist + 1, 0);
+        for (uint32_t c = 0; c < nlist; ++c) x->list_off[c + 1] = x->list_off[c] + list_sizes[c];
+        x->ids.assign(ids, ids + npts);
+        x->has_dimc = true;
+        x->rotated = rotation != nullptr;
+        if (x->rotated) x->rotation.assign(rotation, rotation + static_cast<size_t>(dim) * dim);
+        p->raw.resize(static_cast<size_t>(npts) * dim);
+        p->head_dims = head_dims;
+        out = p.release();
+      }))
+    return nullptr;
+  return out;
+}
+
+int oracle_code_rows(void *h, uint32_t row0, uint32_t nrows, const float *vectors) {
+  auto *p = static_cast<PendingIndex *>(h);
+  return oracle::guarded([&] {
+    const uint32_t d = p->x->dim;
+    if (static_cast<uint64_t>(row0) + nrows > p->x->npts) throw std::invalid_argument("rows out of range");
+    float *dst = p->raw.data() + static_cast<size_t>(row0) * d;
+    if (p->x->rotated) oracle::rotate_rows(vectors, dst, nrows, d, p->x->rotation.data());
+    else std::copy(vectors, vectors + static_cast<size_t>(nrows) * d, dst);
+  });
+}
+
+void *oracle_code_finish(void *h) {
+  std::unique_ptr<PendingIndex> p(static_cast<PendingIndex *>(h));
+  Index *out = nullptr;
+  if (oracle::guarded([&] {
+        oracle::code_index(p->x.get(), p->raw, p->head_dims, true);
+        out = p->x.release();
       }))
     return nullptr;
   return out;

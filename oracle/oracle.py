@@ -31,6 +31,11 @@ def lib():
         _lib.oracle_load.argtypes = [C.c_char_p, U32]
         _lib.oracle_load.restype = P
         _lib.oracle_free.argtypes = [P]
+        _lib.oracle_code_begin.argtypes = [U32, U32, U32, P, P, P, P, U32]
+        _lib.oracle_code_begin.restype = P
+        _lib.oracle_code_rows.argtypes = [P, U32, U32, P]
+        _lib.oracle_code_finish.argtypes = [P]
+        _lib.oracle_code_finish.restype = P
         _lib.oracle_load_codes.argtypes = [P] * 13
         _lib.oracle_load_codes.restype = P
         _lib.oracle_load_arrays.argtypes = [U32, U32, U32, P, P, P, P, P, U32]
@@ -69,9 +74,15 @@ class OracleIndex:
     """The restated reference index: codes, norms and search on the CPU."""
 
     def __init__(self, prefix: str | None, prefix_dims: int = 0, codes: dict | None = None,
-                 arrays: dict | None = None):
+                 arrays: dict | None = None, pieces=None):
+        """From index files (prefix), coded arrays (codes), arrays in the file
+        layout (arrays: centroids, list_sizes, ids, vectors, rotation,
+        head_dims), or the same with the vectors handed over in pieces
+        (arrays without "vectors", pieces: an iterable of (first row, rows))."""
         keep = []
-        if codes is not None:
+        if pieces is not None:
+            self.h = self._from_pieces(arrays, pieces)
+        elif codes is not None:
             self.h = self._from_codes(codes)
         elif arrays is not None:
             a = {k: (np.ascontiguousarray(v) if isinstance(v, np.ndarray) else v)
@@ -88,6 +99,24 @@ class OracleIndex:
         if not self.h:
             raise RuntimeError(lib().oracle_last_error().decode())
         self._read_info()
+
+    @staticmethod
+    def _from_pieces(a: dict, pieces):
+        cen = np.ascontiguousarray(a["centroids"], dtype=np.float32)
+        sizes = np.ascontiguousarray(a["list_sizes"], dtype=np.uint32)
+        ids = np.ascontiguousarray(a["ids"], dtype=np.uint32)
+        rot = a.get("rotation")
+        rot = np.ascontiguousarray(rot, dtype=np.float32) if rot is not None else None
+        h = lib().oracle_code_begin(cen.shape[1], cen.shape[0], len(ids), _p(cen), _p(sizes), _p(ids),
+                                    _p(rot) if rot is not None else None, int(a.get("head_dims", 0)))
+        if not h:
+            raise RuntimeError(lib().oracle_last_error().decode())
+        for row0, rows in pieces:
+            rows = np.ascontiguousarray(rows, dtype=np.float32)
+            if lib().oracle_code_rows(h, int(row0), rows.shape[0], _p(rows)):
+                lib().oracle_code_finish(h)
+                raise RuntimeError(lib().oracle_last_error().decode())
+        return lib().oracle_code_finish(h)
 
     @staticmethod
     def _from_codes(c: dict):
