@@ -33,8 +33,49 @@ for _p in (os.path.join(ROOT, "katoann-public_gb300"), os.path.join(ROOT, "oracl
     if _p not in sys.path:
         sys.path.insert(0, _p)
 
-METRIC = "QPS at recall@10 >= 0.99, 10M x 1024 IVF, learned vs fixed nprobe, batch 4096, 1 GB300"
-PUBLISHED_QPS_099 = 6294.0  # README.md:84 (BioASQ-1024-10M, 28-core Xeon, nlist 8192)
+# The workloads. "learned" (the default line) is the headline: 10M x 1024 with
+# skewed lists, learned vs fixed nprobe. The others are the plain method on the
+# other quoted shapes: the small CPU-runnable case, 1M x 1024, and 990k x 3072
+# (the shape of the reference's OpenAI-3072-1M).
+WORKLOADS = {
+    "learned": dict(n=10_000_000, dim=1024, nlist=16384, batch=4096, head=256, ncomp=10000,
+                    kind="spectral", power=1.2, zipf=1.1, learned=True,
+                    data="synthetic: seeded power-law spectrum (i^-1.2) + 10,000-component Zipf(1.1) "
+                         "mixture, unit norm; stands in for BioASQ-1024-10M"),
+    "small": dict(n=100_000, dim=128, nlist=256, batch=1024, head=64, ncomp=100, kind="mixture",
+                  learned=False,
+                  data="synthetic: seeded 100-component Gaussian mixture (centres N(0,1), sigma 0.3, "
+                       "dimension j scaled by 1/sqrt(j+1)), L2-normalised"),
+    "plain": dict(n=1_000_000, dim=1024, nlist=4096, batch=4096, head=128, ncomp=1000,
+                  kind="spectral", power=1.2, zipf=None, learned=False,
+                  data="synthetic: seeded power-law spectrum (i^-1.2) + 1,000-component mixture, "
+                       "unit norm"),
+    "wide": dict(n=990_000, dim=3072, nlist=4096, batch=4096, head=256, ncomp=2000,
+                 kind="spectral", power=1.0, zipf=None, learned=False,
+                 data="synthetic: seeded power-law spectrum (i^-1.0) + 2,000-component mixture, "
+                      "unit norm; stands in for OpenAI-3072-1M"),
+}
+
+
+L2_BYTES = 129 << 20  # GB300's L2 (about 129 MB)
+
+
+def size_name(n: int) -> str:
+    return f"{n // 1000000}M" if n % 1000000 == 0 else f"{n / 1000:g}k"
+
+
+def workload_name(n: int, d: int, L: int, B: int, k: int) -> str:
+    return f"{size_name(n)} x {d} IVF, nlist {L}, batch {B}, k {k}"
+
+
+def metric_name(w: str, n: int, d: int, B: int) -> str:
+    size = size_name(n)
+    path = "learned vs fixed nprobe" if WORKLOADS[w]["learned"] else "fixed nprobe"
+    return f"QPS at recall@10 >= 0.99, {size} x {d} IVF, {path}, batch {B}, 1 GB300"
+
+
+PUBLISHED_QPS = {"learned": (6294.0, "README.md:84, BioASQ-1024-10M on a 28-core Xeon (CPU)"),
+                 "wide": (16449.0, "README.md:81, OpenAI-3072-1M on a 28-core Xeon (CPU)")}
 LADDER = (8, 12, 16, 24, 32, 48, 64, 96, 128, 192, 256, 384, 512)  # learned nprobe choices
 THRESHOLDS = (0.3, 0.5, 0.7, 0.8, 0.82, 0.84, 0.86, 0.88, 0.9, 0.92, 0.94, 0.96, 0.97, 0.98,
               0.985, 0.99, 0.995, 0.999)
@@ -42,17 +83,19 @@ THRESHOLDS = (0.3, 0.5, 0.7, 0.8, 0.82, 0.84, 0.86, 0.88, 0.9, 0.92, 0.94, 0.96,
 
 def parse_args():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--config", choices=sorted(WORKLOADS), default="learned",
+                    help="workload: learned (10M x 1024, the default line), small, plain or wide")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--n", type=int, default=10_000_000)
-    ap.add_argument("--dim", type=int, default=1024)
-    ap.add_argument("--nlist", type=int, default=16384)
-    ap.add_argument("--ncomp", type=int, default=10000)
-    ap.add_argument("--batch", type=int, default=4096)
+    ap.add_argument("--n", type=int, default=None)
+    ap.add_argument("--dim", type=int, default=None)
+    ap.add_argument("--nlist", type=int, default=None)
+    ap.add_argument("--ncomp", type=int, default=None)
+    ap.add_argument("--batch", type=int, default=None)
     ap.add_argument("--k", type=int, default=10)
-    ap.add_argument("--head", type=int, default=256)
+    ap.add_argument("--head", type=int, default=None)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--kmeans-iters", type=int, default=6)
     ap.add_argument("--train", type=int, default=262144)
@@ -77,7 +120,15 @@ def parse_args():
                     help="coarse ranks the probe model's features read")
     ap.add_argument("--serve-seconds", type=float, default=1.5,
                     help="arrivals per serving run (seconds of the Poisson stream)")
-    return ap.parse_args()
+    args = ap.parse_args()
+    w = WORKLOADS[args.config]
+    for key in ("n", "dim", "nlist", "ncomp", "batch", "head"):
+        if getattr(args, key) is None:
+            setattr(args, key, w[key])
+    if not w["learned"]:
+        args.no_learned = True
+        args.no_serving = True  # the serving block belongs to the headline index
+    return args
 
 
 def fixed_grid(L: int) -> list[tuple[int, int]]:
@@ -125,26 +176,36 @@ def from_rank0(dist, i: int) -> int:
 
 
 # ----------------------------------------------------------------- data
-def make_data(torch, n, d, ncomp, seed, queries, train_queries=0, qseed=None, dev="cuda"):
-    """Unit vectors: mixture centres and per-point noise share an anisotropic
-    spectrum (eigenvalue_i ~ i^-1.2) in a random orthogonal basis; component
-    weights follow Zipf(1.1), so the inverted lists come out skewed. Returns
-    the base, the evaluation queries and (another stream of the same
+def make_data(torch, n, d, ncomp, seed, queries, train_queries=0, qseed=None, dev="cuda",
+              kind="spectral", power=1.2, zipf=1.1):
+    """Unit vectors of one of two families:
+      spectral: mixture centres and per-point noise share an anisotropic
+        spectrum (eigenvalue_i ~ i^-power) in a random orthogonal basis;
+        component weights follow Zipf(zipf) (skewed lists) or are uniform;
+      mixture: centres N(0, 1), per-component sigma 0.3, dimension j scaled
+        by 1/sqrt(j + 1), L2-normalised.
+    Returns the base, the evaluation queries and (another stream of the same
     distribution) the probe-budget training queries. `seed` fixes the
     distribution, the base and the training queries; `qseed` (default: seed)
     the evaluation queries, so that replicas share an index and differ in
     their queries."""
     g = torch.Generator(device=dev).manual_seed(seed)
-    # random orthogonal basis (QR on the host: torch's linear-algebra library is
-    # not needed on the device path)
-    A = torch.randn(d, d, generator=g, device=dev).double().cpu().numpy()
-    Qn, Rn = np.linalg.qr(A)
-    Q = torch.from_numpy(Qn * np.sign(np.diag(Rn))[None, :]).float().to(dev)
-    lam = torch.arange(1, d + 1, device=dev, dtype=torch.float32) ** -1.2
-    B = torch.sqrt(lam / lam.sum())[:, None] * Q.T
-    centres = torch.randn(ncomp, d, generator=g, device=dev) @ B
-    w = torch.arange(1, ncomp + 1, device=dev, dtype=torch.float64) ** -1.1
-    cdf = torch.cumsum(w / w.sum(), 0).float()
+    if kind == "mixture":
+        centres = torch.randn(ncomp, d, generator=g, device=dev)
+        scale = 1.0 / torch.sqrt(torch.arange(d, device=dev, dtype=torch.float32) + 1.0)
+        cdf = torch.arange(1, ncomp + 1, device=dev, dtype=torch.float32) / ncomp
+    else:
+        # random orthogonal basis (QR on the host: torch's linear-algebra
+        # library is not needed on the device path)
+        A = torch.randn(d, d, generator=g, device=dev).double().cpu().numpy()
+        Qn, Rn = np.linalg.qr(A)
+        Q = torch.from_numpy(Qn * np.sign(np.diag(Rn))[None, :]).float().to(dev)
+        lam = torch.arange(1, d + 1, device=dev, dtype=torch.float32) ** -power
+        B = torch.sqrt(lam / lam.sum())[:, None] * Q.T
+        centres = torch.randn(ncomp, d, generator=g, device=dev) @ B
+        w = (torch.arange(1, ncomp + 1, device=dev, dtype=torch.float64) ** -zipf if zipf
+             else torch.ones(ncomp, device=dev, dtype=torch.float64))
+        cdf = torch.cumsum(w / w.sum(), 0).float()
     cdf[-1] = 1.0
 
     def sample(m, gen):
@@ -152,7 +213,10 @@ def make_data(torch, n, d, ncomp, seed, queries, train_queries=0, qseed=None, de
         for s in range(0, m, 1 << 20):
             e = min(m, s + (1 << 20))
             comp = torch.searchsorted(cdf, torch.rand(e - s, generator=gen, device=dev)).clamp_(max=ncomp - 1)
-            x = centres[comp] + 0.5 * (torch.randn(e - s, d, generator=gen, device=dev) @ B)
+            if kind == "mixture":
+                x = (centres[comp] + 0.3 * torch.randn(e - s, d, generator=gen, device=dev)) * scale
+            else:
+                x = centres[comp] + 0.5 * (torch.randn(e - s, d, generator=gen, device=dev) @ B)
             out[s:e] = x / x.norm(dim=1, keepdim=True)
         return out
 
@@ -342,8 +406,10 @@ def main():
     t0 = time.time()
     n, d, L, B, k = args.n, args.dim, args.nlist, args.batch, args.k
     ntrain = 0 if (args.no_learned or args.nprobe or args.impl == "reference") else args.train_queries
+    wl = WORKLOADS[args.config]
     base, queries, train_q = make_data(torch, n, d, args.ncomp, args.seed, B, ntrain,
-                                       qseed=query_seed(args.seed, rank))
+                                       qseed=query_seed(args.seed, rank), kind=wl["kind"],
+                                       power=wl.get("power", 1.2), zipf=wl.get("zipf"))
     cen = kmeans(torch, base, L, args.kmeans_iters, min(args.train, n), args.seed)
     rot = pca_rotation(torch, base, min(100000, n), args.seed)
     a = assign(torch, base, cen)
@@ -489,14 +555,31 @@ def main():
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
+    code_bytes = n * ((d + 63) // 64 * 64) * 2
+    flush = None
+    if code_bytes < 2 * L2_BYTES:
+        # the index fits in L2: a buffer larger than L2 is written between
+        # the timed steps, outside their events
+        flush = torch.empty(2 * L2_BYTES, dtype=torch.uint8, device="cuda")
     with ClockSampler(local) as clocks:
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(args.steps):
-            search(cfg, timer=timer)
-        e1.record()
-        torch.cuda.synchronize()
-        elapsed_ms = e0.elapsed_time(e1)
+        if flush is None:
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(args.steps):
+                search(cfg, timer=timer)
+            e1.record()
+            torch.cuda.synchronize()
+            elapsed_ms = e0.elapsed_time(e1)
+        else:
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                  for _ in range(args.steps)]
+            for a0, a1 in ev:
+                flush.zero_()
+                a0.record()
+                search(cfg, timer=timer)
+                a1.record()
+            torch.cuda.synchronize()
+            elapsed_ms = sum(a0.elapsed_time(a1) for a0, a1 in ev)
     if dist:
         dist.barrier()
     phases, passes = timer.read()
@@ -608,23 +691,25 @@ def main():
         cpu, parity = cpu_baseline(args, torch, idx, queries, fixed99, cfg, k)
 
     clk = clocks.summary()
+    pub = PUBLISHED_QPS.get(args.config) if (n, d) == (wl["n"], wl["dim"]) else None
     out = {
-        "metric": METRIC,
+        "metric": metric_name(args.config, n, d, B),
         "value": round(value, 1), "unit": "queries/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
         "scaling": "weak",
-        "vs_baseline": round(value / PUBLISHED_QPS_099, 2),
-        "baseline_published": {"value": PUBLISHED_QPS_099, "unit": "queries/s",
-                               "source": "README.md:84, BioASQ-1024-10M on a 28-core Xeon (CPU)"},
+        "vs_baseline": round(value / pub[0], 2) if pub else None,
+        "baseline_published": ({"value": pub[0], "unit": "queries/s", "source": pub[1]} if pub else None),
         "dtype": "u8",
-        "data": "synthetic: seeded power-law spectrum (i^-1.2) + 10,000-component Zipf(1.1) mixture, "
-                "unit norm; stands in for BioASQ-1024-10M",
-        "config": {"workload": f"{n // 1000000}M x {d} IVF, nlist {L}, batch {B}, k {k}",
+        "data": wl["data"],
+        "config": {"workload": workload_name(n, d, L, B, k),
                    "nprobe_path": chosen["path"],
                    **{kk: v for kk, v in summary(chosen).items() if kk not in ("qps", "recall")},
                    "prefix_dims": args.head,
                    "ranking": "prefix",
-                   "l2_policy": "inputs larger than L2 (index codes 20.5 GB per pass)"},
+                   "l2_policy": (f"inputs larger than L2 (index codes {code_bytes / 1e9:.1f} GB per pass)"
+                                 if flush is None else
+                                 f"L2 flushed between steps (a {2 * L2_BYTES >> 20} MiB write outside "
+                                 f"the timed events; index codes {code_bytes / 1e6:.0f} MB)")},
         "recall": chosen["recall"],
         "qps_at_recall_0.999": (round(b999["qps"], 1) if b999 else None),
         "setting_at_recall_0.999": ({"path": b999["path"], **summary(b999)} if b999 else None),
@@ -800,13 +885,14 @@ def run_reference(args, torch, vectors, order, cen, rot, sizes, queries, gt, set
     sample = (f"the whole {len(q)}-query batch per step" if m == len(q) else
               f"{m} of the {len(q)} batch queries per step (whole batches would exceed "
               f"{args.ref_seconds:.0f} s)")
-    out = {"impl": "reference", "metric": METRIC, "value": round(value, 1), "unit": "queries/s",
+    out = {"impl": "reference", "metric": metric_name(args.config, args.n, args.dim, B),
+           "value": round(value, 1), "unit": "queries/s",
            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": round(tot_t / args.steps * 1e3, 3), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "u8",
-           "data": "synthetic (same seeded workload as the GPU arm)",
-           "config": {"workload": f"{args.n // 1000000}M x {args.dim} IVF, nlist {args.nlist}, "
-                                  f"batch {B}, k {k}", "nprobe_path": "fixed",
+           "data": WORKLOADS[args.config]["data"] + " (the same seeded workload as the GPU arm)",
+           "config": {"workload": workload_name(args.n, args.dim, args.nlist, B, k),
+                      "nprobe_path": "fixed",
                       "nprobe": p, "survivors": S, "prefix_dims": args.head,
                       "setting_rule": "fastest fixed setting at recall@10 >= 0.99 over the sweep"},
            "recall": pick["recall"],

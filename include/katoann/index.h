@@ -104,6 +104,17 @@ struct IndexArrays {
   bool on_device = false;
 };
 
+// A partition as Index::build computes it, before any file is written.
+struct BuildResult {
+  std::vector<float> centroids;  // nlist x dim
+  std::vector<uint32_t> assign;  // per vector: its list
+  std::vector<float> rotation;   // dim x dim (row j = basis j); empty without one
+  uint32_t head_dims = 0;        // the default prefix dims (src/index.cpp:512)
+};
+
+// min(max(64, round_up(dim / 4, 64)), dim rounded up to 64).
+uint32_t default_head_dims(uint32_t dim);
+
 class Index {
  public:
   Index();
@@ -117,6 +128,11 @@ class Index {
   // and computes the rotation for the prefix ranking pass.
   static void build(const float *data, uint32_t n, uint32_t dim, const BuildOptions &opt,
                     const std::string &prefix);
+  // The same partition, on the GPU, without writing files (data may be
+  // device memory): k-means on a strided training sample, every vector's
+  // list, and the PCA rotation with the default head dims.
+  static BuildResult partition(const float *data, uint32_t n, uint32_t dim, const BuildOptions &opt,
+                               bool on_device = false);
 
   void load(const std::string &prefix, const LoadOptions &opt = {});
   void load_arrays(const IndexArrays &a, const LoadOptions &opt = {});

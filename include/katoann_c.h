@@ -26,6 +26,17 @@ int katoann_build(const float *data, uint32_t n, uint32_t dim, uint32_t nlist,
                   uint32_t train_size, uint32_t kmeans_iters, uint64_t seed, int normalized,
                   uint32_t rotation_sample, uint32_t jacobi_sweeps, const char *prefix);
 
+/* The partition katoann_build writes, computed on the GPU without writing
+ * files (no counterpart in the reference's module): data (n x dim, host
+ * memory, or device memory when on_device) -> centroids (host, nlist x dim),
+ * assign (host, n: each vector's list), rotation (host, dim x dim; *rotated
+ * is 0 when none was computed) and *head_dims (the default prefix dims). */
+int katoann_build_partition(const float *data, int on_device, uint32_t n, uint32_t dim,
+                            uint32_t nlist, uint32_t train_size, uint32_t kmeans_iters,
+                            uint64_t seed, uint32_t rotation_sample, uint32_t jacobi_sweeps,
+                            float *centroids, uint32_t *assign, float *rotation,
+                            uint32_t *rotated, uint32_t *head_dims);
+
 void *katoann_index_new(void);
 void katoann_index_free(void *index);
 

@@ -390,6 +390,48 @@ int katoann_gpu_autotune(const katoann_gpu_index *index, const float *d_queries,
                          const katoann_gpu_probe_model *model, void *d_ws, size_t ws_bytes,
                          katoann_stream_t stream, uint32_t *h_out);
 
+/* ---- Index build on the device (replaces the host k-means of
+ * src/kmeans.cpp and the covariance of pca_rotation, src/index.cpp:276-312).
+ * Row arrays are fp32, row-major with a stride of ld floats: ld a multiple
+ * of 32, at least the dimension, the padding zero; bases 16-byte aligned. */
+
+/* The nearest centroid of each of n rows (replaces closest_centers,
+ * src/kmeans.cpp:191-237): d_assign[i] = argmin_c |c|^2 - 2 x_i.c over the L
+ * rows of d_cen (ties to the smaller c), on the tensor cores in TF32 with an
+ * fp32 accumulator. d_cnorm[c] = |c|^2 (katoann_gpu_row_norms). d_best (may be
+ * NULL) gets the minimum. d_timeouts (one zeroed word) counts CTAs whose
+ * bounded pipeline wait ran out. */
+int katoann_gpu_kmeans_assign(const float *d_x, uint32_t n, uint32_t ld, const float *d_cen,
+                              const float *d_cnorm, uint32_t L, uint32_t *d_assign, float *d_best,
+                              uint32_t *d_timeouts, katoann_stream_t stream);
+/* d_out[i] = |x_i|^2 over ld floats. */
+int katoann_gpu_row_norms(const float *d_x, uint32_t n, uint32_t ld, float *d_out,
+                          katoann_stream_t stream);
+/* One Lloyd update (the centre step of src/kmeans.cpp:73-187): each centroid
+ * with members becomes their mean (summed in double); an empty one keeps its
+ * value. Scratch: d_sums (L x ld doubles), d_counts (L). Also refreshes
+ * d_cnorm. */
+int katoann_gpu_kmeans_update(const float *d_x, uint32_t n, uint32_t ld, const uint32_t *d_assign,
+                              uint32_t L, double *d_sums, uint32_t *d_counts, float *d_cen,
+                              float *d_cnorm, katoann_stream_t stream);
+/* k-means++ seeding (src/kmeans.cpp:280-321): centre 0 is row `first`; centre
+ * m + 1 is drawn with probability proportional to the squared distance to
+ * the nearest of centres 0..m, with d_u[m] (L - 1 uniforms in [0, 1), the
+ * caller's seeded stream) as the draw. Writes L rows of d_cen and their row
+ * indices to d_chosen. Scratch: d_dist (n floats) and
+ * katoann_gpu_kmeanspp_scratch(n) bytes at d_part. */
+size_t katoann_gpu_kmeanspp_scratch(uint32_t n);
+int katoann_gpu_kmeanspp(const float *d_x, uint32_t n, uint32_t ld, uint32_t L, uint32_t first,
+                         const double *d_u, float *d_cen, float *d_dist, void *d_part,
+                         uint32_t *d_chosen, katoann_stream_t stream);
+/* d_dst row i (stride ld, zero past d) = d_src row d_rows[i] (stride d). */
+int katoann_gpu_gather_rows(const float *d_src, uint32_t d, const uint32_t *d_rows, uint32_t m,
+                            uint32_t ld, float *d_dst, katoann_stream_t stream);
+/* Mean-centred covariance of n rows over their first d columns, in double
+ * (src/index.cpp:276-312): d_mean (d), d_cov (d x d, symmetric). */
+int katoann_gpu_covariance(const float *d_x, uint32_t n, uint32_t ld, uint32_t d, double *d_mean,
+                           double *d_cov, katoann_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

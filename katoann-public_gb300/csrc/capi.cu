@@ -97,6 +97,18 @@ uint32_t last_launches();
 int centre_planes(const uint8_t *hi, const uint8_t *lo, const int64_t *norm, uint32_t rows,
                   uint32_t dc, __half *hi16, __half *lo16, int64_t *term, cudaStream_t st);
 bool coarse_tc_ok(uint32_t dc);
+int kmeans_assign(const float *x, uint32_t n, uint32_t ld, const float *cen, const float *cnorm,
+                  uint32_t L, uint32_t *assign, float *best, uint32_t *timeouts, cudaStream_t st);
+int row_norms(const float *x, uint32_t n, uint32_t ld, float *out, cudaStream_t st);
+int kmeans_update(const float *x, uint32_t n, uint32_t ld, const uint32_t *assign, uint32_t L,
+                  double *sums, uint32_t *counts, float *cen, float *cnorm, cudaStream_t st);
+size_t kmeanspp_scratch(uint32_t n);
+int gather_rows(const float *src, uint32_t d, const uint32_t *rows, uint32_t m, uint32_t ld,
+                float *dst, cudaStream_t st);
+int kmeanspp(const float *x, uint32_t n, uint32_t ld, uint32_t L, uint32_t first, const double *u,
+             float *cen, float *dist, double *part, uint32_t *chosen, cudaStream_t st);
+int covariance(const float *x, uint32_t n, uint32_t ld, uint32_t d, double *mean, double *cov,
+               cudaStream_t st);
 int coarse_tc(const __half *ch, const __half *cl, const int64_t *cterm, uint32_t n, const __half *qh,
               const __half *ql, const int64_t *qterm, uint32_t m, uint32_t dc, double step_sq,
               float *out, uint32_t *timeouts, unsigned long long *prof, cudaStream_t st);
@@ -375,6 +387,53 @@ int katoann_gpu_copy_to_host(void *h_dst, const void *d_src, size_t n) {
 int katoann_gpu_dist_values(const int64_t *d_l2, uint32_t n, double step_sq, float *d_out,
                             katoann_stream_t stream) {
   return kato::dist_values(d_l2, n, step_sq, d_out, as_stream(stream));
+}
+
+
+// ---- index build on the device
+int katoann_gpu_kmeans_assign(const float *d_x, uint32_t n, uint32_t ld, const float *d_cen,
+                              const float *d_cnorm, uint32_t L, uint32_t *d_assign, float *d_best,
+                              uint32_t *d_timeouts, katoann_stream_t stream) {
+  return kato::kmeans_assign(d_x, n, ld, d_cen, d_cnorm, L, d_assign, d_best, d_timeouts,
+                             as_stream(stream));
+}
+
+int katoann_gpu_row_norms(const float *d_x, uint32_t n, uint32_t ld, float *d_out,
+                          katoann_stream_t stream) {
+  if (n && (!d_x || !d_out || ld == 0)) return kato::invalid("row norms: bad arguments");
+  return kato::row_norms(d_x, n, ld, d_out, as_stream(stream));
+}
+
+int katoann_gpu_kmeans_update(const float *d_x, uint32_t n, uint32_t ld, const uint32_t *d_assign,
+                              uint32_t L, double *d_sums, uint32_t *d_counts, float *d_cen,
+                              float *d_cnorm, katoann_stream_t stream) {
+  if (L == 0 || ld == 0 || !d_sums || !d_counts || !d_cen || !d_cnorm || (n && (!d_x || !d_assign)))
+    return kato::invalid("k-means update: bad arguments");
+  return kato::kmeans_update(d_x, n, ld, d_assign, L, d_sums, d_counts, d_cen, d_cnorm,
+                             as_stream(stream));
+}
+
+size_t katoann_gpu_kmeanspp_scratch(uint32_t n) { return kato::kmeanspp_scratch(n); }
+
+int katoann_gpu_kmeanspp(const float *d_x, uint32_t n, uint32_t ld, uint32_t L, uint32_t first,
+                         const double *d_u, float *d_cen, float *d_dist, void *d_part,
+                         uint32_t *d_chosen, katoann_stream_t stream) {
+  if (!d_x || !d_u || !d_cen || !d_dist || !d_part || !d_chosen || ld == 0)
+    return kato::invalid("k-means++: bad arguments");
+  return kato::kmeanspp(d_x, n, ld, L, first, d_u, d_cen, d_dist, static_cast<double *>(d_part),
+                        d_chosen, as_stream(stream));
+}
+
+int katoann_gpu_gather_rows(const float *d_src, uint32_t d, const uint32_t *d_rows, uint32_t m,
+                            uint32_t ld, float *d_dst, katoann_stream_t stream) {
+  if (m && (!d_src || !d_rows || !d_dst || ld < d)) return kato::invalid("gather rows: bad arguments");
+  return kato::gather_rows(d_src, d, d_rows, m, ld, d_dst, as_stream(stream));
+}
+
+int katoann_gpu_covariance(const float *d_x, uint32_t n, uint32_t ld, uint32_t d, double *d_mean,
+                           double *d_cov, katoann_stream_t stream) {
+  if (!d_x || !d_mean || !d_cov || ld < d) return kato::invalid("covariance: bad arguments");
+  return kato::covariance(d_x, n, ld, d, d_mean, d_cov, as_stream(stream));
 }
 
 }  // extern "C"

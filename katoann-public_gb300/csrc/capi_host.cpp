@@ -90,6 +90,28 @@ int katoann_build(const float *data, uint32_t n, uint32_t dim, uint32_t nlist, u
   });
 }
 
+int katoann_build_partition(const float *data, int on_device, uint32_t n, uint32_t dim,
+                            uint32_t nlist, uint32_t train_size, uint32_t kmeans_iters,
+                            uint64_t seed, uint32_t rotation_sample, uint32_t jacobi_sweeps,
+                            float *centroids, uint32_t *assign, float *rotation,
+                            uint32_t *rotated, uint32_t *head_dims) {
+  return guarded([&] {
+    katoann::BuildOptions o;
+    o.nlist = nlist;
+    o.train_size = train_size;
+    o.kmeans_iters = kmeans_iters;
+    o.seed = seed;
+    o.rotation_sample = rotation_sample;
+    o.jacobi_sweeps = jacobi_sweeps;
+    const katoann::BuildResult b = katoann::Index::partition(data, n, dim, o, on_device != 0);
+    std::copy(b.centroids.begin(), b.centroids.end(), centroids);
+    std::copy(b.assign.begin(), b.assign.end(), assign);
+    *rotated = b.rotation.empty() ? 0u : 1u;
+    if (!b.rotation.empty()) std::copy(b.rotation.begin(), b.rotation.end(), rotation);
+    *head_dims = b.head_dims;
+  });
+}
+
 void *katoann_index_new(void) { return new katoann::Index(); }
 void katoann_index_free(void *index) { delete I(index); }
 

@@ -343,34 +343,39 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
             for (uint32_t j = 0; j < G; ++j) mask |= static_cast<uint32_t>(pass(j)) << j;
             if (!valid) mask = 0;
-            // records (query, l2, row) go to this CTA's list through a shared
-            // slot counter; the per-query count is a fire-and-forget global
-            // add. Kept rolled (one iteration per column with any) to stay small.
-            uint32_t any = __reduce_or_sync(0xffffffffu, mask);
-            while (any) {
-              const uint32_t j = __ffs(any) - 1;
-              any &= any - 1;
+            // records (query, l2, row) go to this CTA's list: one shared slot
+            // reservation per warp (a warp scan of the lanes' hit counts),
+            // then each lane writes its own records; the per-query count is a
+            // fire-and-forget global add per record
+            const uint32_t mine = __popc(mask);
+            uint32_t incl = mine;
+#pragma unroll
+            for (uint32_t o = 1; o < 32; o <<= 1) {
+              const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+              if (lane >= o) incl += t;
+            }
+            const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+            uint32_t at = 0;
+            if (lane == 0) {
+              at = atomicAdd(rcount, total);
+              found += total;
+            }
+            at = __shfl_sync(0xffffffffu, at, 0) + incl - mine;
+            while (mask) {
+              const uint32_t j = __ffs(mask) - 1;
+              mask &= mask - 1;
               uint32_t dj = 0;
 #pragma unroll
               for (uint32_t k = 0; k < G; ++k) dj = k == j ? d[k] : dj;
-              const bool take = (mask >> j) & 1u;
-              const uint32_t bal = __ballot_sync(0xffffffffu, take);
               const QInfo q = qi[c0 + g + j];
-              uint32_t at = 0;
-              if (lane == 0) {
-                at = atomicAdd(rcount, static_cast<uint32_t>(__popc(bal)));
-                atomicAdd(A.qcount + q.qid, static_cast<uint32_t>(__popc(bal)));
-                found += __popc(bal);
+              atomicAdd(A.qcount + q.qid, 1u);
+              if (at < A.rec_cap) {
+                const int32_t l2 = q.qn + xn - 2 * __float2int_rn(__uint_as_float(dj));
+                rec[at] = make_uint4(q.qid, static_cast<uint32_t>(l2), grow, 0);
+              } else {
+                atomicOr(A.qcount + q.qid, kDropped);
               }
-              at = __shfl_sync(0xffffffffu, at, 0) + __popc(bal & ((1u << lane) - 1u));
-              if (take) {
-                if (at < A.rec_cap) {
-                  const int32_t l2 = q.qn + xn - 2 * __float2int_rn(__uint_as_float(dj));
-                  rec[at] = make_uint4(q.qid, static_cast<uint32_t>(l2), grow, 0);
-                } else {
-                  atomicOr(A.qcount + q.qid, kDropped);
-                }
-              }
+              ++at;
             }
           }
         };

@@ -44,6 +44,8 @@ def _load():
     P, U32, I32, U64, D, S = C.c_void_p, C.c_uint32, C.c_int, C.c_uint64, C.c_double, C.c_size_t
     lib.katoann_last_error.restype = C.c_char_p
     lib.katoann_build.argtypes = [P, U32, U32, U32, U32, U32, U64, I32, U32, U32, C.c_char_p]
+    lib.katoann_build_partition.argtypes = [P, I32, U32, U32, U32, U32, U32, U64, U32, U32, P, P, P,
+                                            P, P]
     lib.katoann_index_new.restype = P
     lib.katoann_index_free.argtypes = [P]
     lib.katoann_index_load.argtypes = [P, C.c_char_p, I32, I32, U32, I32, U32]
@@ -138,6 +140,28 @@ def build(data, prefix: str, nlist: int = 2048, train_size: int = 256000, kmeans
     _check(_lib.katoann_build(_ptr(data), data.shape[0], data.shape[1], nlist, train_size,
                               kmeans_iters, seed, int(normalized), rotation_sample, jacobi_sweeps,
                               prefix.encode()))
+
+
+def build_partition(data, nlist: int = 2048, train_size: int = 256000, kmeans_iters: int = 12,
+                    seed: int = 0, rotation_sample: int = 100000, jacobi_sweeps: int = 8):
+    """The partition build() writes, computed on the GPU without writing
+    files: (centroids [nlist, dim] float32, assign [n] uint32, rotation
+    [dim, dim] float32 or None, head_dims). `data` is a float32 array or a
+    CUDA tensor (then the vectors stay on the device)."""
+    on_device = hasattr(data, "is_cuda") and data.is_cuda
+    keep = data.contiguous() if on_device else np.ascontiguousarray(data, dtype=np.float32)
+    if len(keep.shape) != 2:
+        raise ValueError("data must be 2-D")
+    n, dim = int(keep.shape[0]), int(keep.shape[1])
+    ptr = C.c_void_p(keep.data_ptr()) if on_device else _ptr(keep)
+    cen = np.zeros((nlist, dim), np.float32)
+    assign = np.zeros(n, np.uint32)
+    rot = np.zeros((dim, dim), np.float32)
+    rotated, head = C.c_uint32(0), C.c_uint32(0)
+    _check(_lib.katoann_build_partition(ptr, int(on_device), n, dim, nlist, train_size, kmeans_iters,
+                                        seed, rotation_sample, jacobi_sweeps, _ptr(cen), _ptr(assign),
+                                        _ptr(rot), C.byref(rotated), C.byref(head)))
+    return cen, assign, (rot if rotated.value else None), int(head.value)
 
 
 def normalize_rows(x: np.ndarray) -> np.ndarray:

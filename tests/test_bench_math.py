@@ -33,3 +33,28 @@ def test_traffic_per_tile_is_the_capture():
     # 536.0 MB over 20,279 tiles in the 2M x 1024 capture: 26.4 KB per tile
     assert bench.RANK_TC_DRAM_BYTES_PER_TILE == pytest.approx(536.0e6 / 20279)
     assert 26_000 < bench.RANK_TC_DRAM_BYTES_PER_TILE < 27_000
+
+
+def test_workloads_and_metric_names():
+    """The four workloads the bench runs, and the metric names of their lines."""
+    w = bench.WORKLOADS
+    assert (w["learned"]["n"], w["learned"]["dim"], w["learned"]["nlist"]) == (10_000_000, 1024, 16384)
+    assert (w["small"]["n"], w["small"]["dim"], w["small"]["nlist"], w["small"]["batch"]) == (100_000, 128, 256, 1024)
+    assert (w["plain"]["n"], w["plain"]["dim"], w["plain"]["nlist"]) == (1_000_000, 1024, 4096)
+    assert (w["wide"]["n"], w["wide"]["dim"], w["wide"]["head"]) == (990_000, 3072, 256)
+    # prefix dims are multiples of 64 within the padded dimension (src/index.cpp:695-696)
+    assert all(x["head"] % 64 == 0 and x["head"] <= (x["dim"] + 63) // 64 * 64 for x in w.values())
+    assert bench.metric_name("learned", 10_000_000, 1024, 4096) == \
+        "QPS at recall@10 >= 0.99, 10M x 1024 IVF, learned vs fixed nprobe, batch 4096, 1 GB300"
+    assert bench.metric_name("wide", 990_000, 3072, 4096) == \
+        "QPS at recall@10 >= 0.99, 990k x 3072 IVF, fixed nprobe, batch 4096, 1 GB300"
+
+
+def test_fixed_grid_rows_ascend():
+    """Both arms sweep the same settings; within a survivors value nprobe
+    ascends (the reference arm stops a row at its first point at the target)."""
+    g = bench.fixed_grid(16384)
+    for s in {x[1] for x in g}:
+        row = [p for p, t in g if t == s]
+        assert row == sorted(row) and len(row) == len(set(row))
+    assert all(p <= 256 for p, _ in bench.fixed_grid(256))

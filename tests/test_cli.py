@@ -1,6 +1,6 @@
 """The katoann command-line tool (tools/katoann.cpp of the reference): the same
-commands, flags, JSON lines and exit codes. build runs on the host; search and
-load need the GPU."""
+commands, flags, JSON lines and exit codes. build, search and load need the
+GPU."""
 import json
 import os
 import platform
@@ -61,8 +61,9 @@ def test_usage_and_argument_errors():
     assert p.returncode == 1 and "katoann:" in p.stderr
 
 
+@pytest.mark.gpu
 def test_build_writes_an_index_the_oracle_loads(tmp_path):
-    """build partitions on the host and writes the reference's file format."""
+    """build partitions on the GPU and writes the reference's file format."""
     xi = synth.mixture_ints(5, 10, 3000, 48, 10)
     data = synth.to_f32(xi)
     write_fbin(tmp_path / "base.fbin", data)
