@@ -161,8 +161,9 @@ def test_gather_rows_pads_with_zeros(torch):
     x = rng.standard_normal((500, 45)).astype(np.float32)
     rows = np.array([499, 0, 7, 7, 250], np.int32)
     out = torch.full((5, 64), 9.0, dtype=torch.float32, device="cuda")
-    check(gpu().katoann_gpu_gather_rows(dptr(torch.from_numpy(x).cuda()), 45,
-                                        dptr(torch.from_numpy(rows).cuda()), 5, 64, dptr(out), None))
+    xd, rd = torch.from_numpy(x).cuda(), torch.from_numpy(rows).cuda()  # alive until the copy ran
+    check(gpu().katoann_gpu_gather_rows(dptr(xd), 45, dptr(rd), 5, 64, dptr(out), None))
+    torch.cuda.synchronize()
     got = out.cpu().numpy()
     assert np.array_equal(got[:, :45], x[rows]) and np.all(got[:, 45:] == 0)
 
