@@ -115,8 +115,6 @@ def parse_args():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default knobs of the ranking pass (profiling runs)")
-    ap.add_argument("--rank-small", type=int, default=-1,
-                    help="items of at most this many queries on the CUDA cores (default: the library's)")
     ap.add_argument("--probe-epochs", type=int, default=24, help="training epochs of the probe model")
     ap.add_argument("--probe-depth", type=int, default=128,
                     help="coarse ranks the probe model's features read")
@@ -429,8 +427,6 @@ def main():
         return
 
     import katoann
-    if args.rank_small >= 0:
-        katoann.set_rank_small(args.rank_small)
     work_stream = torch.cuda.Stream()
     torch.cuda.synchronize()
     torch.cuda.set_stream(work_stream)  # every launch of the timed path on one stream

@@ -219,12 +219,6 @@ int katoann_gpu_set_rank_width(uint32_t width);
 int katoann_gpu_set_rank_schedule(uint32_t beta);
 /* The current knobs: h_out[3] = {seed rows (0 = default), split weight, item width}. */
 void katoann_gpu_rank_knobs(uint32_t *h_out);
-/* Items of at most `queries` queries (0 to 8; default 4) are scored inside the
- * ranking pass on the CUDA cores (dp4a on the raw bytes) instead of the
- * tensor cores, which spend as long on a tile of two queries as of 64.
- * Process-wide; results never depend on it. The autotuner tries 0, 4 and 8. */
-int katoann_gpu_set_rank_small(uint32_t queries);
-uint32_t katoann_gpu_rank_small(void);
 
 /* katoann_gpu_search that also records phase events into `timer` (may be
  * NULL, then identical to katoann_gpu_search). */

@@ -276,14 +276,6 @@ void katoann_gpu_rank_knobs(uint32_t *h_out) {
   h_out[2] = kato::g_tc_width.load();
 }
 
-int katoann_gpu_set_rank_small(uint32_t queries) {
-  if (queries > kato::kTcSmallMax) return kato::invalid("small-item limit must be at most 8 queries");
-  kato::g_tc_small = queries;
-  return KATO_OK;
-}
-
-uint32_t katoann_gpu_rank_small(void) { return kato::g_tc_small.load(); }
-
 int katoann_gpu_set_rank_schedule(uint32_t beta) {
   if (beta > 8) return kato::invalid("rank schedule weight must be at most 8");
   kato::g_tc_beta = beta;

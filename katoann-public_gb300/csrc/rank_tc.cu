@@ -180,7 +180,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
     for (uint32_t s = 0; s < S.Bs; ++s) {
       tc::mbar_init(bar.b_full + s, kQueryWarps);
-      tc::mbar_init(bar.b_empty + s, 1 + kEpiWarps + kConvWarps);
+      tc::mbar_init(bar.b_empty + s, 1 + kEpiWarps);
     }
     tc::mbar_init(bar.done, 1);
     *rcount = 0;
@@ -229,119 +229,62 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     w.init(A.tile_off, A.items, nitems, t0, t1);
     if (warp < kConvWarps) {
       // ---- converters: raw stage -> fp16 A stage and the row's centred
-      // norm; two threads per row, each half of every chunk's 16-byte columns.
-      // A tile of a small item (at most A.small queries) is scored here
-      // instead, on the CUDA cores: each thread's half-row against the
-      // item's query bytes (dp4a), partial dot products and the row's raw
-      // norm into the accumulator slot's shared-memory twin for the epilogue.
+      // norm; two threads per row, each half of every chunk's 16-byte columns
       const uint32_t r = tid & (kTcRows - 1), hf = tid >> 7, swm = S.inner == 128 ? 7u : 3u;
       const uint32_t nuh = S.inner / 32;  // 16-byte columns per half of a full chunk
-      int32_t *sdot = reinterpret_cast<int32_t *>(sm + L.sdot);
-      const uint32_t *qwords = reinterpret_cast<const uint32_t *>(sm + L.qbytes);
-      uint32_t rs = 0, rph = 0, as = 0, aph = 0, ab = 0, abph = 0, ib = 0, bph = 0;
+      uint32_t rs = 0, rph = 0, as = 0, aph = 0, ab = 0, abph = 0;
       bool ok = true;
       for (; ok && w.t < t1; ++w.t) {
-        w.step();
-        const uint32_t ne = tc_item_queries(w.cur);
-        const bool small = ne <= A.small;
-        // the item's query buffer: waited at its first tile, released at its last
-        if (w.first() && !__all_sync(0xffffffffu, timed_wait(bar.b_full + ib, bph, err, pw[0]))) break;
         int32_t xs = 0;
-        if (small) {
-          uint32_t dots[kTcSmallMax];
-#pragma unroll
-          for (uint32_t j = 0; j < kTcSmallMax; ++j) dots[j] = 0;
-          uint32_t xsq = 0;  // sum of the raw bytes squared
-          const uint32_t *qw = qwords + ib * kTcSmallMax * (h / 4);
-          for (uint32_t kc = 0; kc < nkc; ++kc) {
-            if (!__all_sync(0xffffffffu, timed_wait(bar.raw_full + rs, rph, err, pw[0]))) {
-              ok = false;
-              break;
-            }
-            const unsigned char *raw = sm + L.raw + rs * rtile;
-            const uint32_t nu = min(S.inner, h - kc * S.inner) / 16;
-#pragma unroll
-            for (uint32_t i = 0; i < 4; ++i) {
-              const uint32_t u = hf * nuh + i;
-              if (i < nuh && u < nu) {
-                const uint32_t o = r * S.inner + u * 16;
-                const uint4 v = *reinterpret_cast<const uint4 *>(raw + (o ^ (((o >> 7) & swm) << 4)));
-                xsq = dp4(v.x, v.x, dp4(v.y, v.y, dp4(v.z, v.z, dp4(v.w, v.w, xsq))));
-                const uint32_t wq = (kc * S.inner + u * 16) / 4;  // the query words of these bytes
-#pragma unroll
-                for (uint32_t j = 0; j < kTcSmallMax; ++j)
-                  if (j < ne) {
-                    const uint4 q = *reinterpret_cast<const uint4 *>(qw + j * (h / 4) + wq);
-                    dots[j] = dp4(v.x, q.x, dp4(v.y, q.y, dp4(v.z, q.z, dp4(v.w, q.w, dots[j]))));
-                  }
-              }
-            }
-            __syncwarp();
-            if (lane == 0) tc::mbar_arrive(bar.raw_empty + rs);
-            if (++rs == S.Rs) rs = 0, rph ^= 1;
+        for (uint32_t kc = 0; kc < nkc; ++kc) {
+          // warp-uniform waits: a warp arrives once for all its lanes below
+          if (!__all_sync(0xffffffffu, timed_wait(bar.raw_full + rs, rph, err, pw[0]) &&
+                                           timed_wait(bar.a_empty + as, aph ^ 1, err, pw[1]))) {
+            ok = false;
+            break;
           }
-          if (!ok) break;
-          if (!__all_sync(0xffffffffu, timed_wait(bar.acc_empty + ab, abph ^ 1, err, pw[1]))) break;
+          tc::fence_after();  // the MMAs that read A stage `as` before have completed
+          const unsigned char *raw = sm + L.raw + rs * rtile;
+          const uint32_t nu = min(S.inner, h - kc * S.inner) / 16;
+          // the row's half of the chunk as fp16 pairs: 16 dimensions = 8 columns
+          uint32_t cols[32];
 #pragma unroll
-          for (uint32_t j = 0; j < kTcSmallMax; ++j)
-            if (j < ne) sdot[((ab * 2 + hf) * kTcSmallMax + j) * kTcRows + r] = static_cast<int32_t>(dots[j]);
-          xs = static_cast<int32_t>(xsq);
-        } else {
-          for (uint32_t kc = 0; kc < nkc; ++kc) {
-            // warp-uniform waits: a warp arrives once for all its lanes below
-            if (!__all_sync(0xffffffffu, timed_wait(bar.raw_full + rs, rph, err, pw[0]) &&
-                                             timed_wait(bar.a_empty + as, aph ^ 1, err, pw[1]))) {
-              ok = false;
-              break;
+          for (uint32_t i = 0; i < 4; ++i) {
+            const uint32_t u = hf * nuh + i;
+            uint4 lo = make_uint4(0, 0, 0, 0), hi = lo;
+            if (i < nuh && u < nu) {
+              const uint32_t o = r * S.inner + u * 16;
+              const uint4 v = *reinterpret_cast<const uint4 *>(raw + (o ^ (((o >> 7) & swm) << 4)));
+              tc::bytes_to_half16(v, bias, lo, hi);
+              xs += centred_sq_sum16(v);
             }
-            tc::fence_after();  // the MMAs that read A stage `as` before have completed
-            const unsigned char *raw = sm + L.raw + rs * rtile;
-            const uint32_t nu = min(S.inner, h - kc * S.inner) / 16;
-            // the row's half of the chunk as fp16 pairs: 16 dimensions = 8 columns
-            uint32_t cols[32];
-#pragma unroll
-            for (uint32_t i = 0; i < 4; ++i) {
-              const uint32_t u = hf * nuh + i;
-              uint4 lo = make_uint4(0, 0, 0, 0), hi = lo;
-              if (i < nuh && u < nu) {
-                const uint32_t o = r * S.inner + u * 16;
-                const uint4 v = *reinterpret_cast<const uint4 *>(raw + (o ^ (((o >> 7) & swm) << 4)));
-                tc::bytes_to_half16(v, bias, lo, hi);
-                xs += centred_sq_sum16(v);
-              }
-              cols[8 * i + 0] = lo.x, cols[8 * i + 1] = lo.y, cols[8 * i + 2] = lo.z, cols[8 * i + 3] = lo.w;
-              cols[8 * i + 4] = hi.x, cols[8 * i + 5] = hi.y, cols[8 * i + 6] = hi.z, cols[8 * i + 7] = hi.w;
-            }
-            __syncwarp();
-            if (lane == 0) tc::mbar_arrive(bar.raw_empty + rs);  // the raw stage has been read
-            // into this row's TMEM lane: A stage `as`, the half's columns
-            if (hf * nuh < nu) {
-              const uint32_t taddr =
-                  tmem + (((warp & 3) * 32u) << 16) + acol + as * (S.inner / 2) + hf * nuh * 8;
-              if (nuh == 4) tc::tmem_st32(taddr, cols);
-              else tc::tmem_st16(taddr, *reinterpret_cast<const uint32_t(*)[16]>(cols));
-            }
-            tc::tmem_wait_st();
-            tc::fence_before();
-            __syncwarp();
-            if (lane == 0) tc::mbar_arrive(bar.a_full + as);
-            if (++rs == S.Rs) rs = 0, rph ^= 1;
-            if (++as == kTcAStages) as = 0, aph ^= 1;
+            cols[8 * i + 0] = lo.x, cols[8 * i + 1] = lo.y, cols[8 * i + 2] = lo.z, cols[8 * i + 3] = lo.w;
+            cols[8 * i + 4] = hi.x, cols[8 * i + 5] = hi.y, cols[8 * i + 6] = hi.z, cols[8 * i + 7] = hi.w;
           }
-          if (!ok) break;
-          // the row norms of this tile's accumulator slot, once the epilogue
-          // has finished with the slot's previous tile
-          if (!__all_sync(0xffffffffu, timed_wait(bar.acc_empty + ab, abph ^ 1, err, pw[1]))) break;
+          __syncwarp();
+          if (lane == 0) tc::mbar_arrive(bar.raw_empty + rs);  // the raw stage has been read
+          // into this row's TMEM lane: A stage `as`, the half's columns
+          if (hf * nuh < nu) {
+            const uint32_t taddr =
+                tmem + (((warp & 3) * 32u) << 16) + acol + as * (S.inner / 2) + hf * nuh * 8;
+            if (nuh == 4) tc::tmem_st32(taddr, cols);
+            else tc::tmem_st16(taddr, *reinterpret_cast<const uint32_t(*)[16]>(cols));
+          }
+          tc::tmem_wait_st();
+          tc::fence_before();
+          __syncwarp();
+          if (lane == 0) tc::mbar_arrive(bar.a_full + as);
+          if (++rs == S.Rs) rs = 0, rph ^= 1;
+          if (++as == kTcAStages) as = 0, aph ^= 1;
         }
+        if (!ok) break;
+        // the row norms of this tile's accumulator slot, once the epilogue
+        // has finished with the slot's previous tile
+        if (!__all_sync(0xffffffffu, timed_wait(bar.acc_empty + ab, abph ^ 1, err, pw[1]))) break;
         sxn[(ab * 2 + hf) * kTcRows + r] = xs;
         __syncwarp();
         if (lane == 0) tc::mbar_arrive(bar.xn_full + ab);
         if (++ab == kTcAcc) ab = 0, abph ^= 1;
-        if (w.last()) {
-          __syncwarp();
-          if (lane == 0) tc::mbar_arrive(bar.b_empty + ib);
-          if (++ib == S.Bs) ib = 0, bph ^= 1;
-        }
       }
     } else if (warp < kTmaWarp) {
       // ---- epilogue: thread = row (its TMEM lane), warpgroup = column half
@@ -370,60 +313,6 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           break;
         tc::fence_after();
         const int32_t xn = sxn[ab * 2 * kTcRows + row] + sxn[(ab * 2 + 1) * kTcRows + row];
-        const uint32_t ne_item = tc_item_queries(w.cur);
-        if (ne_item <= A.small) {
-          // a tile the converters scored on the CUDA cores: xn is the row's
-          // raw sum of squares and the slot's twin in shared memory holds
-          // the two halves' raw dot products; QInfo holds the raw query norm
-          // and the bound less it. This warpgroup takes queries half,
-          // half + 2, ...
-          const int32_t *sd = reinterpret_cast<const int32_t *>(sm + L.sdot);
-          constexpr uint32_t kPer = kTcSmallMax / 2;
-          uint32_t mask = 0;
-          int32_t l2v[kPer];
-#pragma unroll
-          for (uint32_t t = 0; t < kPer; ++t) {
-            const uint32_t j = half + 2 * t;
-            l2v[t] = 0;
-            if (j < ne_item && valid) {
-              const int32_t dot = sd[((ab * 2) * kTcSmallMax + j) * kTcRows + row] +
-                                  sd[((ab * 2 + 1) * kTcSmallMax + j) * kTcRows + row];
-              const int32_t v = xn - 2 * dot;
-              if (v <= qi[j].qb) {
-                mask |= 1u << t;
-                l2v[t] = qi[j].qn + v;
-              }
-            }
-          }
-          if (__any_sync(0xffffffffu, mask != 0)) {
-            const uint32_t mine = __popc(mask);
-            uint32_t incl = mine;
-#pragma unroll
-            for (uint32_t o = 1; o < 32; o <<= 1) {
-              const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-              if (lane >= o) incl += t;
-            }
-            const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-            uint32_t at = 0;
-            if (lane == 0) {
-              at = atomicAdd(rcount, total);
-              found += total;
-            }
-            at = __shfl_sync(0xffffffffu, at, 0) + incl - mine;
-            while (mask) {
-              const uint32_t t = __ffs(mask) - 1;
-              mask &= mask - 1;
-              int32_t l2 = 0;
-#pragma unroll
-              for (uint32_t k = 0; k < kPer; ++k) l2 = k == t ? l2v[k] : l2;
-              const uint32_t qid = qi[half + 2 * t].qid;
-              atomicAdd(A.qcount + qid, 1u);
-              if (at < A.rec_cap) rec[at] = make_uint4(qid, static_cast<uint32_t>(l2), grow, 0);
-              else atomicOr(A.qcount + qid, kDropped);
-              ++at;
-            }
-          }
-        } else {
         const uint32_t taddr = tmem + ((q4 * 32u) << 16) + ab * N;
         const float xnf = static_cast<float>(xn);
         // this warpgroup's columns: half of the item's MMA width. In groups
@@ -495,7 +384,6 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         } else if constexpr (CH >= 16) {
           for (uint32_t g = 0; g < cph; g += 16) process(std::integral_constant<uint32_t, 16>{}, g);
         }
-        }
         // the slot's accumulators and row norms have been read: hand it back
         tc::fence_before();
         __syncwarp();
@@ -555,16 +443,6 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           }
           if (!timed_wait(bar.acc_empty + ab, abph ^ 1, err, pw[1])) break;
           tc::fence_after();
-          if (tc_item_queries(w.cur) <= A.small) {
-            // the converters score this tile: hand the slot on without MMAs
-            tc::mbar_arrive(bar.acc_full + ab);
-            if (++ab == kTcAcc) ab = 0, abph ^= 1;
-            if (w.last()) {
-              tc::commit(bar.b_empty + ib);
-              if (++ib == S.Bs) ib = 0, bph ^= 1;
-            }
-            continue;
-          }
           const uint32_t bbase = tc::smem_addr(sm + L.b + ib * btile);
           for (uint32_t kc = 0; kc < nkc; ++kc) {
             if (!timed_wait(bar.a_full + as, aph, err, pw[2])) {
@@ -609,25 +487,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         w.step();
         if (!w.first()) continue;
         if (!__all_sync(0xffffffffu, timed_wait(bar.b_empty + ib, bph ^ 1, err, pw[0]))) break;
-        const uint32_t ne = tc_item_queries(w.cur);
-        if (ne <= A.small) {
-          // a small item: the raw query bytes (words) for the converters, and
-          // per query its raw norm and the bound less it
-          if (j < ne) {
-            QInfo q{0, 0, INT_MIN, -INFINITY};
-            q.qid = A.entries[A.off[w.cur.list] + tc_item_first(w.cur) + j] / A.nprobe;
-            const uint4 *src = reinterpret_cast<const uint4 *>(A.qhi + static_cast<size_t>(q.qid) * A.dc);
-            uint4 *dst = reinterpret_cast<uint4 *>(sm + L.qbytes) + (ib * kTcSmallMax + j) * (h / 16);
-            for (uint32_t u = 0; u < h / 16; ++u) dst[u] = __ldg(src + u);
-            const int64_t qn = A.qnorm[q.qid];
-            q.qn = static_cast<int32_t>(qn);
-            q.qb = static_cast<int32_t>(static_cast<int64_t>(A.bound[q.qid]) - qn);
-            q.qbf = static_cast<float>(q.qb);
-            qinfo[ib * N + j] = q;
-          }
-          if (j == 0) swidth[ib] = ne;
-        } else if (j < N) {
-          const uint32_t e0 = A.off[w.cur.list] + tc_item_first(w.cur);
+        if (j < N) {
+          const uint32_t e0 = A.off[w.cur.list] + w.cur.qfirst;
+          const uint32_t ne = min(N, A.off[w.cur.list + 1] - e0);
           if (j == 0) swidth[ib] = ne;
           unsigned char *b = sm + L.b + ib * btile;
           QInfo q{0, 0, INT_MIN, -INFINITY};
@@ -1130,8 +992,7 @@ __global__ void tc_expand_kernel(const uint32_t *__restrict__ list_off, const ui
     const uint32_t tiles = (list_off[c + 1] - list_off[c] + kTcRows - 1) / kTcRows;
     const uint32_t tb = counts[L + 1 + c];
     for (uint32_t j = 0; j < i1 - i0; ++j) {
-      items[i0 + j] = TcItem{c, (min(N, cnt[c] - j * N) << 24) | (j * N), list_off[c],
-                             list_off[c + 1] - list_off[c]};
+      items[i0 + j] = TcItem{c, j * N, list_off[c], list_off[c + 1] - list_off[c]};
       tile_off[i0 + j] = tb + j * tiles;
       // every item before the last of its list is full (width N)
       if (cost_off) cost_off[i0 + j] = counts[2 * (L + 1) + c] + j * tiles * (64 + beta * N);
@@ -1174,7 +1035,7 @@ uint32_t rank_tc_ctas() {
   return static_cast<uint32_t>(std::max(sms, 1));
 }
 
-std::atomic<uint32_t> g_tc_width{0}, g_tc_beta{0}, g_tc_small{4};
+std::atomic<uint32_t> g_tc_width{0}, g_tc_beta{0};
 
 bool rank_tc_plan(uint32_t h, uint32_t dc, TcShape *s) {
   if (h == 0 || h % 64 || h > 1024 || h > dc || dc % 64) return false;

@@ -10,19 +10,11 @@
 
 namespace kato {
 
-// One work item: a list and up to N of the queries that probe it; its tiles
-// are the list's rows, 128 each. qfirst packs the item's first probe entry
-// within the list (bits 0-23: entries [off[list] + first, + queries)) and its
-// query count (bits 24-31).
+// One work item: a list and up to N of the queries that probe it (probe
+// entries [off[list] + qfirst, +N)); its tiles are the list's rows, 128 each.
 struct TcItem {
   uint32_t list, qfirst, row0, nrows;
 };
-__host__ __device__ inline uint32_t tc_item_first(const TcItem &it) { return it.qfirst & 0xFFFFFFu; }
-__host__ __device__ inline uint32_t tc_item_queries(const TcItem &it) { return it.qfirst >> 24; }
-
-// Items of at most this many queries can be scored on the CUDA cores (dp4a)
-// inside the ranking pass instead of on the tensor cores (RankTcArgs::small).
-constexpr uint32_t kTcSmallMax = 8;
 
 struct RankTcArgs {
   const uint8_t *qhi;        // B x dc query high bytes
@@ -42,7 +34,6 @@ struct RankTcArgs {
   unsigned long long *counters;  // [0] 128-row tiles scored, [1] candidates found
   unsigned long long *prof;      // optional: 14 cycle counters of the warp roles
   uint32_t dc, h, nprobe;
-  uint32_t small;            // items of at most this many queries go to the CUDA cores (0: none)
   DistScale scale;
 };
 
@@ -54,7 +45,7 @@ struct TcShape {
 
 // Shared-memory carve-up of the ranking CTA.
 struct TcSmem {
-  uint32_t raw, a, b, qinfo, qbv, width, sxn, qbytes, sdot, bars, tbase, err, rcount, total;
+  uint32_t raw, a, b, qinfo, qbv, width, sxn, bars, tbase, err, rcount, total;
 };
 
 __host__ __device__ inline uint32_t tc_take(uint32_t &o, uint32_t bytes, uint32_t align) {
@@ -87,9 +78,6 @@ __host__ __device__ inline TcSmem tc_smem_layout(uint32_t h, const TcShape &s) {
   L.qbv = tc_take(o, s.Bs * s.N * 4, 16);
   L.width = tc_take(o, 2 * 4, 16);
   L.sxn = tc_take(o, kTcAcc * 2 * kTcRows * 4, 16);
-  // the small items' query bytes, and their dot products per slot, half and query
-  L.qbytes = tc_take(o, s.Bs * kTcSmallMax * h, 16);
-  L.sdot = tc_take(o, kTcAcc * 2 * kTcSmallMax * kTcRows * 4, 16);
   L.bars = tc_take(o, kTcBars * 8, 8);
   L.tbase = tc_take(o, 4, 4);
   L.err = tc_take(o, 4, 4);
@@ -122,9 +110,6 @@ int rank_tc_prepare(const uint32_t *cnt, const uint32_t *list_off, uint32_t L, u
 // Process-wide knobs of the pass (0 = default): the largest item width and
 // the cost weight of the CTA split.
 extern std::atomic<uint32_t> g_tc_width, g_tc_beta;
-// Items of at most this many queries are scored on the CUDA cores inside the
-// pass (0 to kTcSmallMax; 0 = every item on the tensor cores).
-extern std::atomic<uint32_t> g_tc_small;
 // Candidate records of the pass into per-query buffers of cap entries
 // (distance bits, row); qfill counts the entries each query was offered.
 int rank_tc_bucket(const uint4 *rec, const uint32_t *rec_n, uint32_t rec_cap, uint32_t ctas,

@@ -730,7 +730,7 @@ struct Plan {
   bool tc;                          // tensor-core ranking pass
   bool coarse_tc;                   // tensor-core coarse product
   TcShape tcs;
-  uint32_t tcitems, cap, seed_rows, ctas, rec_cap, beta, small;
+  uint32_t tcitems, cap, seed_rows, ctas, rec_cap, beta;
   size_t off_fq, off_qhi, off_qlo, off_qn, off_qhn, off_qh0, off_cd, off_probed, off_cnt, off_off,
       off_woff, off_cur, off_work, off_ent, off_slots, off_surv, off_nsurv, off_stats,
       off_tcscratch, off_tcitems, off_tileoff, off_nitems, off_qcount, off_qfill, off_bound,
@@ -778,7 +778,6 @@ int make_plan(const katoann_gpu_index *ix, uint32_t B, uint32_t k, uint32_t p, i
         std::max<size_t>(8192, static_cast<size_t>(B) * pl.S * 32 / pl.ctas));
     // the cost split, unless its 32-bit cost units could overflow
     pl.beta = g_tc_beta.load();
-    pl.small = g_tc_small.load();
     const uint64_t worst = static_cast<uint64_t>(pl.tcitems) * ((ix->max_list + 127) / 128) *
                            (64 + static_cast<uint64_t>(pl.beta) * pl.tcs.N);
     if (worst >= (1ull << 31)) pl.beta = 0;
@@ -1008,7 +1007,6 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
     T.dc = dc;
     T.h = pl.dims;
     T.nprobe = p;
-    T.small = pl.small;
     T.scale = scale;
     if ((rc = rank_tc(T, ix->d_hi, ix->npts, pl.tcs, st))) return rc;
     if ((rc = rank_tc_bucket(rec, rec_n, pl.rec_cap, pl.ctas, qfill, slots, pl.cap, scale, st)))
@@ -1191,18 +1189,15 @@ int autotune(const katoann_gpu_index *ix, const float *queries, uint32_t nq, uin
   cudaEventCreate(&a);
   cudaEventCreate(&b);
   const uint32_t seed0 = g_seed_rows.load(), beta0 = g_tc_beta.load(), width0 = g_tc_width.load();
-  const uint32_t small0 = g_tc_small.load();
   float best = 1e30f;
-  uint32_t bs = seed0, bb = beta0, bw = width0, bsm = small0;
+  uint32_t bs = seed0, bb = beta0, bw = width0;
   int rc = KATO_OK;
   for (uint32_t seed : {512u, 1024u, 2048u})
     for (uint32_t beta : {0u, 1u, 2u, 4u})
-      for (uint32_t width : {0u, 32u})
-        for (uint32_t small : {0u, 4u, 8u}) {
+      for (uint32_t width : {0u, 32u}) {
         g_seed_rows = seed;
         g_tc_beta = beta;
         g_tc_width = width;
-        g_tc_small = small;
         int r = search(ix, queries, nq, k, p, ranking, survivors, max_batch, ws, ws_bytes, ids,
                        dists, budget, st, nullptr);
         if (r == KATO_ENOMEM) continue;  // this setting needs a larger workspace
@@ -1226,13 +1221,11 @@ int autotune(const katoann_gpu_index *ix, const float *queries, uint32_t nq, uin
           bs = seed;
           bb = beta;
           bw = width;
-          bsm = small;
         }
       }
   g_seed_rows = rc ? seed0 : bs;
   g_tc_beta = rc ? beta0 : bb;
   g_tc_width = rc ? width0 : bw;
-  g_tc_small = rc ? small0 : bsm;
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   cudaFree(ids);

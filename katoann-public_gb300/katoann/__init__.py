@@ -38,7 +38,6 @@ def _load():
     gpu.katoann_gpu_timer_read.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
     gpu.katoann_gpu_last_error.restype = C.c_char_p
     gpu.katoann_gpu_copy_to_host.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
-    gpu.katoann_gpu_rank_small.restype = C.c_uint32
     gpu.katoann_gpu_last_launches.restype = C.c_uint32
     lib = C.CDLL(path)
     lib.gpu = gpu
@@ -163,13 +162,6 @@ def build_partition(data, nlist: int = 2048, train_size: int = 256000, kmeans_it
                                         seed, rotation_sample, jacobi_sweeps, _ptr(cen), _ptr(assign),
                                         _ptr(rot), C.byref(rotated), C.byref(head)))
     return cen, assign, (rot if rotated.value else None), int(head.value)
-
-
-def set_rank_small(queries: int) -> None:
-    """Items of at most `queries` queries (0 to 8) are scored on the CUDA
-    cores inside the ranking pass (process-wide; results never change)."""
-    if _lib.gpu.katoann_gpu_set_rank_small(int(queries)) != 0:
-        raise ValueError(_lib.gpu.katoann_gpu_last_error().decode())
 
 
 def normalize_rows(x: np.ndarray) -> np.ndarray:
@@ -386,9 +378,8 @@ class Index:
                  survivors: int = 32, budget: "ProbeModel | None" = None,
                  threshold: float = 0.95) -> dict:
         """Times a search of these queries under every candidate setting of the
-        ranking pass's knobs (seed rows, CTA split weight, item width, the
-        largest item scored on the CUDA cores) and keeps the fastest for the
-        process; results never depend on them."""
+        ranking pass's knobs (seed rows, CTA split weight, item width) and
+        keeps the fastest for the process; results never depend on them."""
         q = np.ascontiguousarray(queries, dtype=np.float32)
         if q.ndim != 2 or q.shape[1] != self.dim:
             raise ValueError("queries must be (n, dim) float32")
@@ -400,7 +391,7 @@ class Index:
                                            budget._h if budget is not None else None,
                                            float(threshold), _ptr(out)))
         return dict(seed_rows=int(out[0]), schedule=int(out[1]), width=int(out[2]),
-                    small=int(_lib.gpu.katoann_gpu_rank_small()), us_per_search=int(out[3]))
+                    us_per_search=int(out[3]))
 
     def search_stats(self) -> dict:
         """Diagnostics of the last search (see katoann_gpu_workspace_stats)."""

@@ -1,5 +1,4 @@
-"""The ranking pass's knobs (seed rows, CTA split weight, item width, the
-small items scored on the CUDA cores) and the
+"""The ranking pass's knobs (seed rows, CTA split weight, item width) and the
 autotuner that picks them: every setting gives the oracle's results bit for
 bit; the autotuner returns one of its candidates and leaves results alone."""
 import ctypes as C
@@ -26,11 +25,6 @@ def test_knob_setters_check_their_ranges():
     assert list(mine)[1:] == [3, 32]
     assert lib.katoann_gpu_set_rank_width(knobs[2]) == 0
     assert lib.katoann_gpu_set_rank_schedule(knobs[1]) == 0
-    lib.katoann_gpu_rank_small.restype = C.c_uint32
-    small = lib.katoann_gpu_rank_small()
-    assert lib.katoann_gpu_set_rank_small(9) == -1
-    assert lib.katoann_gpu_set_rank_small(8) == 0 and lib.katoann_gpu_rank_small() == 8
-    assert lib.katoann_gpu_set_rank_small(small) == 0
 
 
 @pytest.mark.gpu
@@ -44,32 +38,20 @@ def test_every_knob_setting_matches_the_oracle(tmp_path):
     idx.load(prefix)
     ref = oracle.OracleIndex(prefix)
     want = ref.search(queries, k=10, nprobe=12, survivors=32)
-    lib.katoann_gpu_rank_small.restype = C.c_uint32
-    small0 = lib.katoann_gpu_rank_small()
     try:
         for beta in (0, 1, 4, 8):
             for width in (0, 16, 32):
                 for seed in (0, 64, 2048):
-                    for small in (0, 1, 4, 8):  # items of <= small queries on the CUDA cores
-                        assert lib.katoann_gpu_set_rank_schedule(beta) == 0
-                        assert lib.katoann_gpu_set_rank_width(width) == 0
-                        assert lib.katoann_gpu_set_seed_rows(seed) == 0
-                        assert lib.katoann_gpu_set_rank_small(small) == 0
-                        got = idx.search(queries, k=10, nprobe=12, survivors=32)
-                        assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1]), \
-                            (beta, width, seed, small)
-        # the high-byte and exact rankings, and a bound-free search (all rows candidates)
-        for small in (0, 8):
-            assert lib.katoann_gpu_set_rank_small(small) == 0
-            for ranking, surv in (("high", 16), ("prefix", 300)):
-                got = idx.search(queries, k=10, nprobe=12, ranking=ranking, survivors=surv)
-                w2 = ref.search(queries, k=10, nprobe=12, ranking=ranking, survivors=surv)
-                assert np.array_equal(got[0], w2[0]) and np.array_equal(got[1], w2[1]), (small, ranking)
+                    assert lib.katoann_gpu_set_rank_schedule(beta) == 0
+                    assert lib.katoann_gpu_set_rank_width(width) == 0
+                    assert lib.katoann_gpu_set_seed_rows(seed) == 0
+                    got = idx.search(queries, k=10, nprobe=12, survivors=32)
+                    assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1]), \
+                        (beta, width, seed)
     finally:
         lib.katoann_gpu_set_rank_schedule(0)
         lib.katoann_gpu_set_rank_width(0)
         lib.katoann_gpu_set_seed_rows(0)
-        lib.katoann_gpu_set_rank_small(small0)
 
 
 @pytest.mark.gpu
@@ -85,7 +67,7 @@ def test_autotune_keeps_results(tmp_path):
     try:
         t = idx.autotune(queries, k=10, nprobe=12, survivors=32)
         assert t["seed_rows"] in (512, 1024, 2048) and t["schedule"] in (0, 1, 2, 4)
-        assert t["width"] in (0, 32) and t["small"] in (0, 4, 8) and t["us_per_search"] > 0
+        assert t["width"] in (0, 32) and t["us_per_search"] > 0
         got = idx.search(queries, k=10, nprobe=12, survivors=32)
         want = ref.search(queries, k=10, nprobe=12, survivors=32)
         assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
