@@ -346,9 +346,10 @@ class ClockSampler:
 # ------------------------------------------------------------ roofline
 SEED_ROWS = 1024  # rows behind each query's seed bound (the library default for survivors <= 128)
 
-# DRAM bytes per 128-row tile of the tensor-core ranking kernel, from one ncu
-# capture on the 2M x 1024 case (profiles/rank_tc_traffic_2m.md): 536.0 MB over
-# 20,279 tiles. The traffic of a launch scales with the tiles it scores.
+# DRAM bytes per 128-row tile of the tensor-core ranking kernel: one ncu
+# capture (dram__bytes_read.sum + dram__bytes_write.sum) of a 2M x 1024 search
+# read 536.0 MB over 20,279 tiles, about 26.4 KB per tile against the 32 KB of
+# head bytes a full tile holds. The traffic of a launch scales with its tiles.
 RANK_TC_DRAM_BYTES_PER_TILE = 536.0e6 / 20279
 
 

@@ -15,6 +15,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <memory>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -110,6 +111,13 @@ struct BuildResult {
   std::vector<uint32_t> assign;  // per vector: its list
   std::vector<float> rotation;   // dim x dim (row j = basis j); empty without one
   uint32_t head_dims = 0;        // the default prefix dims (src/index.cpp:512)
+};
+
+// A search whose device pipeline gave up on a bounded wait (no counterpart in
+// the reference, which has no device): the kernel returned early and the
+// results are incomplete; the index stays usable.
+struct timeout_error : std::runtime_error {
+  using std::runtime_error::runtime_error;
 };
 
 // min(max(64, round_up(dim / 4, 64)), dim rounded up to 64).

@@ -3,7 +3,8 @@
  * ctypes); it replaces the reference's pybind11 module
  * (python/katoann_module.cpp:34-129) one call for one call. Statuses: 0 ok,
  * -1 invalid argument (std::invalid_argument), -2 runtime error
- * (std::runtime_error, CUDA), -3 logic error (std::logic_error);
+ * (std::runtime_error, CUDA), -3 logic error (std::logic_error), -5 a
+ * bounded wait in a device pipeline ran out (katoann::timeout_error);
  * katoann_last_error() gives the message. Pointers are host memory unless
  * named d_*. */
 #ifndef KATOANN_C_H_

@@ -9,6 +9,8 @@
  *   KATO_ERUNTIME CUDA/runtime error (std::runtime_error)
  *   KATO_ELOGIC  call out of order   (std::logic_error)
  *   KATO_ENOMEM  workspace too small or allocation failed
+ *   KATO_ETIMEOUT a bounded pipeline wait inside a kernel ran out (the
+ *                kernel returned without finishing; results are invalid)
  * katoann_gpu_last_error() gives the message of the calling thread's last
  * failure.
  *
@@ -35,7 +37,8 @@ enum {
   KATO_EINVAL = -1,
   KATO_ERUNTIME = -2,
   KATO_ELOGIC = -3,
-  KATO_ENOMEM = -4
+  KATO_ENOMEM = -4,
+  KATO_ETIMEOUT = -5  /* a bounded wait in a device pipeline ran out */
 };
 
 /* Ranking of SearchParams (include/katoann/index.h:45-49 of the reference). */
@@ -219,6 +222,14 @@ int katoann_gpu_set_rank_width(uint32_t width);
 int katoann_gpu_set_rank_schedule(uint32_t beta);
 /* The current knobs: h_out[3] = {seed rows (0 = default), split weight, item width}. */
 void katoann_gpu_rank_knobs(uint32_t *h_out);
+/* Every mbarrier wait of the tensor-core ranking pass gives up after this
+ * many SM cycles (0 = the default, 4e9, about 2 s at 2 GHz); a CTA that gives
+ * up sets its error flag, lets its copies and MMAs in flight finish, frees
+ * its tensor memory and returns, and is counted in workspace statistic 3.
+ * Process-wide. A limit far below a pipeline step makes searches fail with
+ * KATO_ETIMEOUT (the host library checks the count after each pass); that is
+ * its only use besides the default. */
+int katoann_gpu_set_wait_limit(uint64_t cycles);
 
 /* katoann_gpu_search that also records phase events into `timer` (may be
  * NULL, then identical to katoann_gpu_search). */

@@ -276,6 +276,12 @@ void katoann_gpu_rank_knobs(uint32_t *h_out) {
   h_out[2] = kato::g_tc_width.load();
 }
 
+int katoann_gpu_set_wait_limit(uint64_t cycles) {
+  if (cycles > (1ull << 40)) return kato::invalid("wait limit must be at most 2^40 cycles");
+  kato::g_tc_wait = cycles;
+  return KATO_OK;
+}
+
 int katoann_gpu_set_rank_schedule(uint32_t beta) {
   if (beta > 8) return kato::invalid("rank schedule weight must be at most 8");
   kato::g_tc_beta = beta;

@@ -21,6 +21,9 @@ int guarded(F &&f) {
   } catch (const std::invalid_argument &e) {
     g_error = e.what();
     return -1;
+  } catch (const katoann::timeout_error &e) {
+    g_error = e.what();
+    return -5;
   } catch (const std::logic_error &e) {
     g_error = e.what();
     return -3;

@@ -99,8 +99,24 @@ struct Index::State {
     graphs.clear();
   }
   mutable void *last_stream = nullptr;
+  // per device pass of a host search: the pass's count of CTAs whose bounded
+  // pipeline wait ran out (workspace statistic 3), copied back with the results
+  mutable uint64_t *hwait = nullptr;
+  mutable uint32_t hwait_n = 0;
+  uint64_t *wait_counts(uint32_t passes) const {
+    if (passes > hwait_n) {
+      if (hwait) cudaFreeHost(hwait);
+      hwait = nullptr;
+      hwait_n = 0;
+      cuda_check(cudaMallocHost(reinterpret_cast<void **>(&hwait), passes * sizeof(uint64_t)),
+                 "cudaMallocHost");
+      hwait_n = passes;
+    }
+    return hwait;
+  }
 
   ~State() {
+    if (hwait) cudaFreeHost(hwait);
     drop_graphs();
     if (done) cudaEventDestroy(done);
     if (stream) cudaStreamDestroy(stream);
@@ -633,6 +649,8 @@ void Index::search(const float *queries, uint32_t nq, const SearchParams &p, uin
   if (p.nprobe_used) s.dnp_out.ensure(static_cast<size_t>(b) * 4);
   if (s.last_stream && s.last_stream != s.stream)
     cuda_check(cudaStreamWaitEvent(s.stream, s.done, 0), "cudaStreamWaitEvent");
+  const uint32_t passes = (nq + mb - 1) / mb;
+  uint64_t *waits = s.wait_counts(passes);
   for (uint32_t q0 = 0; q0 < nq; q0 += mb) {
     const uint32_t nb = std::min(mb, nq - q0);
     cuda_check(cudaMemcpyAsync(s.dq.p, queries + static_cast<size_t>(q0) * s.dim,
@@ -664,10 +682,17 @@ void Index::search(const float *queries, uint32_t nq, const SearchParams &p, uin
     cuda_check(cudaMemcpyAsync(dists + static_cast<size_t>(q0) * p.k, s.ddists.p,
                                static_cast<size_t>(nb) * p.k * 4, cudaMemcpyDeviceToHost, s.stream),
                "copy dists");
+    cuda_check(cudaMemcpyAsync(waits + q0 / mb, static_cast<const char *>(s.ws.p) + 3 * sizeof(uint64_t),
+                               sizeof(uint64_t), cudaMemcpyDeviceToHost, s.stream),
+               "copy statistics");
   }
   cuda_check(cudaEventRecord(s.done, s.stream), "cudaEventRecord");
   s.last_stream = s.stream;
   cuda_check(cudaStreamSynchronize(s.stream), "search");
+  for (uint32_t i = 0; i < passes; ++i)
+    if (waits[i])
+      throw timeout_error("search: a bounded pipeline wait in a tensor-core kernel ran out (" +
+                          std::to_string(waits[i]) + " CTAs); the results are incomplete");
 }
 
 void Index::search_device(const float *d_queries, uint32_t nq, const SearchParams &p,

@@ -141,9 +141,9 @@ __device__ __forceinline__ uint32_t mma_width(uint32_t ne) {
 
 // A pipeline wait that also adds the cycles it took to `acc`.
 __device__ __forceinline__ bool timed_wait(uint64_t *b, uint32_t phase, volatile uint32_t *err,
-                                           unsigned long long &acc) {
+                                           unsigned long long &acc, long long limit) {
   const long long t = clock64();
-  const bool ok = tc::mbar_wait_or(b, phase, err);
+  const bool ok = tc::mbar_wait_or(b, phase, err, limit);
   acc += clock64() - t;
   return ok;
 }
@@ -238,8 +238,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         int32_t xs = 0;
         for (uint32_t kc = 0; kc < nkc; ++kc) {
           // warp-uniform waits: a warp arrives once for all its lanes below
-          if (!__all_sync(0xffffffffu, timed_wait(bar.raw_full + rs, rph, err, pw[0]) &&
-                                           timed_wait(bar.a_empty + as, aph ^ 1, err, pw[1]))) {
+          if (!__all_sync(0xffffffffu, timed_wait(bar.raw_full + rs, rph, err, pw[0], A.wait) &&
+                                           timed_wait(bar.a_empty + as, aph ^ 1, err, pw[1], A.wait))) {
             ok = false;
             break;
           }
@@ -280,7 +280,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         if (!ok) break;
         // the row norms of this tile's accumulator slot, once the epilogue
         // has finished with the slot's previous tile
-        if (!__all_sync(0xffffffffu, timed_wait(bar.acc_empty + ab, abph ^ 1, err, pw[1]))) break;
+        if (!__all_sync(0xffffffffu, timed_wait(bar.acc_empty + ab, abph ^ 1, err, pw[1], A.wait))) break;
         sxn[(ab * 2 + hf) * kTcRows + r] = xs;
         __syncwarp();
         if (lane == 0) tc::mbar_arrive(bar.xn_full + ab);
@@ -301,15 +301,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const QInfo *qi = qinfo + ib * N;
         // waits are made warp-uniform: the warp-collective steps below need all lanes
         if (w.first()) {
-          if (!__all_sync(0xffffffffu, timed_wait(bar.b_full + ib, bph, err, pw[0]))) break;
+          if (!__all_sync(0xffffffffu, timed_wait(bar.b_full + ib, bph, err, pw[0], A.wait))) break;
           cph = mma_width<N>(swidth[ib]) / 2;
           c0 = half * cph;
         }
         const uint32_t rin = (w.t - w.start) * kTcRows + row;
         const bool valid = rin < w.cur.nrows;
         const uint32_t grow = w.cur.row0 + rin;
-        if (!__all_sync(0xffffffffu, timed_wait(bar.acc_full + ab, abph, err, pw[1]) &&
-                                         timed_wait(bar.xn_full + ab, abph, err, pw[1])))
+        if (!__all_sync(0xffffffffu, timed_wait(bar.acc_full + ab, abph, err, pw[1], A.wait) &&
+                                         timed_wait(bar.xn_full + ab, abph, err, pw[1], A.wait)))
           break;
         tc::fence_after();
         const int32_t xn = sxn[ab * 2 * kTcRows + row] + sxn[(ab * 2 + 1) * kTcRows + row];
@@ -410,7 +410,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           const int32_t y = static_cast<int32_t>(w.cur.row0 + (w.t - w.start) * kTcRows);
           bool ok = true;
           for (uint32_t kc = 0; kc < nkc; ++kc) {
-            if (!timed_wait(bar.raw_empty + rs, rph ^ 1, err, pw[0])) {
+            if (!timed_wait(bar.raw_empty + rs, rph ^ 1, err, pw[0], A.wait)) {
               ok = false;
               break;
             }
@@ -438,14 +438,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         for (; ok && w.t < t1; ++w.t) {
           w.step();
           if (w.first()) {
-            if (!timed_wait(bar.b_full + ib, bph, err, pw[0])) break;
+            if (!timed_wait(bar.b_full + ib, bph, err, pw[0], A.wait)) break;
             idesc = tc::idesc_f16(kTcRows, mma_width<N>(swidth[ib]));  // the item's queries
           }
-          if (!timed_wait(bar.acc_empty + ab, abph ^ 1, err, pw[1])) break;
+          if (!timed_wait(bar.acc_empty + ab, abph ^ 1, err, pw[1], A.wait)) break;
           tc::fence_after();
           const uint32_t bbase = tc::smem_addr(sm + L.b + ib * btile);
           for (uint32_t kc = 0; kc < nkc; ++kc) {
-            if (!timed_wait(bar.a_full + as, aph, err, pw[2])) {
+            if (!timed_wait(bar.a_full + as, aph, err, pw[2], A.wait)) {
               ok = false;
               break;
             }
@@ -486,7 +486,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       for (; w.t < t1; ++w.t) {
         w.step();
         if (!w.first()) continue;
-        if (!__all_sync(0xffffffffu, timed_wait(bar.b_empty + ib, bph ^ 1, err, pw[0]))) break;
+        if (!__all_sync(0xffffffffu, timed_wait(bar.b_empty + ib, bph ^ 1, err, pw[0], A.wait))) break;
         if (j < N) {
           const uint32_t e0 = A.off[w.cur.list] + w.cur.qfirst;
           const uint32_t ne = min(N, A.off[w.cur.list + 1] - e0);
@@ -1036,6 +1036,7 @@ uint32_t rank_tc_ctas() {
 }
 
 std::atomic<uint32_t> g_tc_width{0}, g_tc_beta{0};
+std::atomic<unsigned long long> g_tc_wait{0};
 
 bool rank_tc_plan(uint32_t h, uint32_t dc, TcShape *s) {
   if (h == 0 || h % 64 || h > 1024 || h > dc || dc % 64) return false;

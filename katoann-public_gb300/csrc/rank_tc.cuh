@@ -34,6 +34,7 @@ struct RankTcArgs {
   unsigned long long *counters;  // [0] 128-row tiles scored, [1] candidates found
   unsigned long long *prof;      // optional: 14 cycle counters of the warp roles
   uint32_t dc, h, nprobe;
+  long long wait;            // cycles a pipeline wait may take before the CTA gives up
   DistScale scale;
 };
 
@@ -110,6 +111,9 @@ int rank_tc_prepare(const uint32_t *cnt, const uint32_t *list_off, uint32_t L, u
 // Process-wide knobs of the pass (0 = default): the largest item width and
 // the cost weight of the CTA split.
 extern std::atomic<uint32_t> g_tc_width, g_tc_beta;
+// The pass's bounded pipeline waits give up after this many cycles (0: the
+// default of 4e9, about 2 s); a CTA that gives up is counted in stats[3].
+extern std::atomic<unsigned long long> g_tc_wait;
 // Candidate records of the pass into per-query buffers of cap entries
 // (distance bits, row); qfill counts the entries each query was offered.
 int rank_tc_bucket(const uint4 *rec, const uint32_t *rec_n, uint32_t rec_cap, uint32_t ctas,

@@ -1007,6 +1007,7 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
     T.dc = dc;
     T.h = pl.dims;
     T.nprobe = p;
+    T.wait = g_tc_wait.load() ? static_cast<long long>(g_tc_wait.load()) : 4000000000ll;
     T.scale = scale;
     if ((rc = rank_tc(T, ix->d_hi, ix->npts, pl.tcs, st))) return rc;
     if ((rc = rank_tc_bucket(rec, rec_n, pl.rec_cap, pl.ctas, qfill, slots, pl.cap, scale, st)))

@@ -38,6 +38,7 @@ def _load():
     gpu.katoann_gpu_timer_read.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
     gpu.katoann_gpu_last_error.restype = C.c_char_p
     gpu.katoann_gpu_copy_to_host.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
+    gpu.katoann_gpu_set_wait_limit.argtypes = [C.c_uint64]
     gpu.katoann_gpu_last_launches.restype = C.c_uint32
     lib = C.CDLL(path)
     lib.gpu = gpu
@@ -122,7 +123,17 @@ def _check(rc: int) -> None:
         raise ValueError(msg)
     if rc == -3:
         raise RuntimeError(f"logic error: {msg}")
+    if rc == -5:
+        raise TimeoutError(msg)
     raise RuntimeError(msg)
+
+
+def set_wait_limit(cycles: int) -> None:
+    """Every pipeline wait of the tensor-core ranking pass gives up after this
+    many SM cycles (0: the default, about 2 s); a search in which one gives up
+    raises TimeoutError. Process-wide."""
+    if _lib.gpu.katoann_gpu_set_wait_limit(int(cycles)) != 0:
+        raise ValueError(_lib.gpu.katoann_gpu_last_error().decode())
 
 
 def amx_available() -> bool:
