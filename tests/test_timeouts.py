@@ -14,7 +14,7 @@ from _util import fixture
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("cycles", [1000, 20000])
+@pytest.mark.parametrize("cycles", [200, 1000])
 def test_short_wait_limit_fails_cleanly_then_search_recovers(cycles):
     import katoann
     spec, z, prefix, queries = fixture("d128")
