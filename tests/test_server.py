@@ -102,3 +102,23 @@ def test_hbm_budget_cuts_batches(tmp_path):
     for a, b in zip(res, res16):
         assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
     _check_alone(idx, queries, ks, res, nprobe=16)
+
+
+@pytest.mark.gpu
+def test_burst_overlaps_batches_and_matches_the_oracle(tmp_path):
+    """1,200 requests submitted at once: the dispatcher launches a batch and
+    forms the next while it runs, so at least two batches are on the device
+    together; every result is the oracle's for that query, bit for bit."""
+    import katoann
+    import oracle
+    queries, idx = _index(tmp_path)
+    ref = oracle.OracleIndex(str(tmp_path / "x"))
+    qs = np.concatenate([queries] * 3)
+    server = katoann.Server(idx, max_batch=64, max_in_flight=3, max_k=10, nprobe=96, survivors=256)
+    tickets = [server.submit(q, 10) for q in qs]
+    res = [server.wait(t) for t in tickets]
+    st = server.stats()
+    assert st["requests"] == len(qs) and st["peak_in_flight"] >= 2, st
+    want_ids, want_d = ref.search(qs, k=10, nprobe=96, survivors=256)
+    for i, r in enumerate(res):
+        assert np.array_equal(r[0], want_ids[i]) and np.array_equal(r[1], want_d[i]), i
