@@ -16,11 +16,11 @@
 //        - a TMA thread loads raw tiles of high bytes (128 rows x 128 bytes,
 //          128-byte swizzle) into a ring of stages;
 //        - two staging warps gather each item's query rows, re-centred to
-//          (byte - 128) as exact fp16, into a double-buffered B tile,
-//          K-major with the 128-byte swizzle, with each query's bound;
+//          (byte - 128) as exact fp16, into a double-buffered B tile in the
+//          canonical K-major layout, with each query's bound;
 //        - eight converter warps (two threads per row) re-centre the raw tiles
-//          to fp16 and store them into tensor memory (the A operand) with
-//          tcgen05.st, and sum each row's centred norm xn';
+//          to fp16 and store them into tensor memory (the A operand, two
+//          stages) with tcgen05.st, and sum each row's centred norm xn';
 //        - one MMA thread issues tcgen05.mma (M = 128 rows, N queries, K = 16)
 //          into double-buffered fp32 TMEM accumulators. Products are at most
 //          128 * 128, so up to 1024 dimensions add up exactly;
@@ -132,22 +132,6 @@ struct TileWalk {
   __device__ bool first() const { return t == t0 || t == start; }
   __device__ bool last() const { return t + 1 == t1 || t + 1 == next; }
 };
-
-// The query tile (the MMA's B operand) is K-major with the 128-byte swizzle:
-// 64-dimension chunks of N rows x 128 bytes, chunk c at c * N * 128; the
-// 16-byte unit v of row j sits at unit v ^ (j % 8) of the row. (The
-// unswizzled layout put every 8-row group of a chunk on the same banks.)
-__device__ __forceinline__ uint32_t bq_off(uint32_t N, uint32_t j, uint32_t dim) {
-  const uint32_t c = dim >> 6, v = (dim & 63) >> 3;
-  return c * N * 128 + j * 128 + ((v ^ (j & 7)) << 4);
-}
-
-// Shared-memory descriptor of a K-major operand in the 128-byte swizzle:
-// rows of 128 bytes, 8-row groups 1024 bytes apart.
-__device__ __forceinline__ uint64_t desc_sw128(uint32_t addr) {
-  return static_cast<uint64_t>((addr & 0x3FFFFu) >> 4) | (1ull << 16) | (64ull << 32) |
-         (1ull << 46) | (2ull << 61);
-}
 
 // The MMA width (queries) an item of ne queries uses: 16, 32 or N.
 template <uint32_t N>
@@ -470,17 +454,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             // A from TMEM (8 columns per 16-dimension step); B's descriptor
             // advances 256 bytes (two core matrices), i.e. 16 encoded, per step
             const uint32_t a0 = tmem + acol + as * (S.inner / 2);
+            const uint64_t bd0 = tc::desc(bbase + kc * S.inner * 16, 128, (h / 8) * 128);
             const uint32_t steps = min(S.inner, h - kc * S.inner) / 16;
             const uint32_t dcol = tmem + ab * N;
 #pragma unroll
             for (uint32_t s = 0; s < 8; ++s)
-              if (s < steps) {
-                // dimensions kc * inner + 16 s: their 64-dimension chunk, then
-                // 32 bytes per 16-dimension step inside it
-                const uint32_t dim = kc * S.inner + 16 * s;
-                const uint64_t bd = desc_sw128(bbase + (dim >> 6) * N * 128 + ((dim & 63) >> 4) * 32);
-                tc::mma_f16_ts(dcol, a0 + 8 * s, bd, idesc, (kc | s) != 0);
-              }
+              if (s < steps) tc::mma_f16_ts(dcol, a0 + 8 * s, bd0 + 16 * s, idesc, (kc | s) != 0);
             tc::commit(bar.a_empty + as);
             pi += clock64() - ti;
             if (++as == kTcAStages) as = 0, aph ^= 1;
@@ -523,8 +502,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
               const uint4 v = __ldg(src + u);
               uint4 lo, hi;
               tc::bytes_to_half16(v, bias, lo, hi);
-              *reinterpret_cast<uint4 *>(b + bq_off(N, j, u * 16)) = lo;
-              *reinterpret_cast<uint4 *>(b + bq_off(N, j, u * 16 + 8)) = hi;
+              *reinterpret_cast<uint4 *>(b + tc::canon_off(j, u * 16, h)) = lo;
+              *reinterpret_cast<uint4 *>(b + tc::canon_off(j, u * 16 + 8, h)) = hi;
               s1 = dp4(v.x, 0x01010101u, dp4(v.y, 0x01010101u, dp4(v.z, 0x01010101u, dp4(v.w, 0x01010101u, s1))));
             }
             // sum (q - 128)^2 = sum q^2 - 256 sum q + 16384 h
@@ -535,8 +514,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           } else {
             const uint4 zero = make_uint4(0, 0, 0, 0);  // fp16 zeros: a centred byte of 128
             for (uint32_t u = 0; u < h / 16; ++u) {
-              *reinterpret_cast<uint4 *>(b + bq_off(N, j, u * 16)) = zero;
-              *reinterpret_cast<uint4 *>(b + bq_off(N, j, u * 16 + 8)) = zero;
+              *reinterpret_cast<uint4 *>(b + tc::canon_off(j, u * 16, h)) = zero;
+              *reinterpret_cast<uint4 *>(b + tc::canon_off(j, u * 16 + 8, h)) = zero;
             }
           }
           qinfo[ib * N + j] = q;

@@ -74,7 +74,7 @@ __host__ __device__ inline TcSmem tc_smem_layout(uint32_t h, const TcShape &s) {
   uint32_t o = 0;
   L.raw = tc_take(o, s.Rs * kTcRows * s.inner, 1024);
   L.a = tc_take(o, 0, 1024);  // the A stages live in tensor memory
-  L.b = tc_take(o, s.Bs * s.N * h * 2, 1024);  // 128-byte swizzle atoms: 1 KiB aligned
+  L.b = tc_take(o, s.Bs * s.N * h * 2, 128);
   L.qinfo = tc_take(o, s.Bs * s.N * kTcQInfo, 16);
   L.qbv = tc_take(o, s.Bs * s.N * 4, 16);
   L.width = tc_take(o, 2 * 4, 16);

@@ -1,10 +1,13 @@
 // 5th-generation tensor core (tcgen05) helpers for sm_103a, as inline PTX.
 //
-// Operands are fp16 tiles, K-major with the 128-byte swizzle, in shared
-// memory (loaded by TMA or written by threads in the same pattern), or the A
-// operand in tensor memory (TMEM: lane = row, two fp16 per 32-bit column).
-// Accumulators are fp32 in TMEM: lane = row of the 128-row tile, column =
-// column of the output.
+// Operands are fp16 tiles in shared memory in the K-major, no-swizzle
+// canonical layout: 8-row x 16-byte core matrices of 128 contiguous bytes;
+// core matrix (row group g, k group j) of a tile that is KT elements wide sits
+// at byte (g * (KT / 8) + j) * 128, row r of it at + 16 * (r % 8). The
+// descriptor's leading byte offset is the distance between core matrices
+// adjacent in K (128) and its stride byte offset the distance between row
+// groups (KT * 16). Accumulators are fp32 in tensor memory (TMEM): lane = row
+// of the 128-row tile, column = column of the output.
 //
 // Exactness: integer-valued fp16 operands with |a|, |b| <= 128 give products
 // of at most 2^14, so up to 1024 of them add up exactly in fp32 (|sum| <= 2^24).
@@ -38,6 +41,15 @@ inline PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Shared-memory matrix descriptor (no swizzle, fixed constant at bit 46).
+__device__ __forceinline__ uint64_t desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = static_cast<uint64_t>((addr & 0x3FFFFu) >> 4);
+  d |= static_cast<uint64_t>((lbo >> 4) & 0x3FFFu) << 16;
+  d |= static_cast<uint64_t>((sbo >> 4) & 0x3FFFu) << 32;
+  d |= 1ull << 46;
+  return d;
 }
 
 // Instruction descriptor of kind::f16: fp16 A and B, K-major, fp32 accumulator.
@@ -215,6 +227,11 @@ __device__ __forceinline__ void tmem_wait_st() {
 }
 __device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// Byte offset of element (r, k) in a tile KT elements wide.
+__host__ __device__ __forceinline__ uint32_t canon_off(uint32_t r, uint32_t k, uint32_t kt) {
+  return ((r >> 3) * (kt >> 3) + (k >> 3)) * 128u + (r & 7u) * 16u + (k & 7u) * 2u;
 }
 
 // 16 unsigned bytes -> 16 fp16 values (byte - bias), exactly: each byte is
