@@ -58,3 +58,9 @@ def test_fixed_grid_rows_ascend():
         row = [p for p, t in g if t == s]
         assert row == sorted(row) and len(row) == len(set(row))
     assert all(p <= 256 for p, _ in bench.fixed_grid(256))
+
+
+def test_rotation_is_fp32_fma_work():
+    bound, work, unit = bench.phase_work("rotate+quantize", B, L, DC, D, P, S, H, 0, 0)
+    assert (bound, unit) == ("fp32", "TFMA/s") and work == pytest.approx(B * D * D / 1e12)
+    assert bench.FP32_TFMA_NOMINAL == pytest.approx(40.27, abs=0.01)
