@@ -442,6 +442,8 @@ def main():
                     max_batch=B)
     torch.cuda.synchronize()
     load_s = time.time() - t1
+    del vectors  # the index holds its codes; the float vectors are not needed any more
+    torch.cuda.empty_cache()
     stream = work_stream.cuda_stream
     ids_d = torch.empty((B, k), dtype=torch.int32, device="cuda")
     dists_d = torch.empty((B, k), dtype=torch.float32, device="cuda")
