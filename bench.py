@@ -116,6 +116,8 @@ def parse_args():
     ap.add_argument("--label-survivors", type=int, default=256,
                     help="survivors of that search (prefix ranking, exact refinement)")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--no-build", action="store_true",
+                    help="skip the timed index build on the device")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default knobs of the ranking pass (profiling runs)")
     ap.add_argument("--probe-epochs", type=int, default=24, help="training epochs of the probe model")
@@ -350,10 +352,11 @@ class ClockSampler:
 SEED_ROWS = 1024  # rows behind each query's seed bound (the library default for survivors <= 128)
 
 # DRAM bytes per 128-row tile of the tensor-core ranking kernel: one ncu
-# capture (dram__bytes_read.sum + dram__bytes_write.sum) of a 2M x 1024 search
-# read 536.0 MB over 20,279 tiles, about 26.4 KB per tile against the 32 KB of
-# head bytes a full tile holds. The traffic of a launch scales with its tiles.
-RANK_TC_DRAM_BYTES_PER_TILE = 536.0e6 / 20279
+# capture (dram__bytes_read.sum + dram__bytes_write.sum, one pass) of this
+# 10M x 1024 search at nprobe 72 and 64 survivors moved 2,632.8 + 24.8 MB over
+# 96,108 tiles, about 27.7 KB per tile (1.09 x the 256 head bytes of each
+# probed row). The traffic of a launch scales with its tiles.
+RANK_TC_DRAM_BYTES_PER_TILE = (2632.8e6 + 24.8e6) / 96108
 
 
 def phase_work(phase: str, B: int, L: int, dc: int, d: int, nprobe: int, S: int, head: int,
@@ -442,8 +445,9 @@ def main():
                     max_batch=B)
     torch.cuda.synchronize()
     load_s = time.time() - t1
-    del vectors  # the index holds its codes; the float vectors are not needed any more
-    torch.cuda.empty_cache()
+    if args.no_build:
+        del vectors  # the index holds its codes; the float vectors are not needed any more
+        torch.cuda.empty_cache()
     stream = work_stream.cuda_stream
     ids_d = torch.empty((B, k), dtype=torch.int32, device="cuda")
     dists_d = torch.empty((B, k), dtype=torch.float32, device="cuda")
@@ -642,6 +646,17 @@ def main():
     e2e_qps = world * B * e2e_steps / e2e_s
     e2e_recall = recall(ih.numpy().view(np.uint32), gt, k)
 
+    # ---- the index build on the device: the same base vectors partitioned by
+    # the library (katoann.build_partition: k-means++ and Lloyd on a training
+    # sample, every vector's list, the PCA rotation), timed, loaded, and
+    # searched at the fixed setting; the timed index above comes from the
+    # setup's k-means so that both arms search the same index
+    build = None
+    if not args.no_build:
+        build = device_build(args, torch, katoann, vectors, order, queries, gt, fixed99, B, k)
+        del vectors
+        torch.cuda.empty_cache()
+
     # ---- serving: Poisson arrivals through the continuous-batching server
     serve = None
     if rank == 0 and world == 1 and not args.no_serving:
@@ -686,7 +701,7 @@ def main():
         traffic = round(RANK_TC_DRAM_BYTES_PER_TILE * search_stats["ranking_tiles"] / 1e9, 3)
     roofline = {"kernel": dom, "bound": bound, "achieved": round(achieved, 2), "peak": peak,
                 "unit": unit, "frac": round(achieved / peak, 4), "traffic": traffic,
-                "traffic_unit": "GB per launch (scaled from the 2M capture by tiles scored)",
+                "traffic_unit": "GB per launch (the 10M capture's bytes per tile x this run's tiles)",
                 "algorithmic": round(work, 3), "algorithmic_rows_from": rows_source,
                 "peak_source": ("nominal: 152 SMs x 128 FP32 lanes x 2.07 GHz" if bound == "fp32" else
                                 peaks["source"] + (" burst bf16" if bound == "tensor" else " copy")),
@@ -728,6 +743,7 @@ def main():
             "recall_0.999": {"fixed": summary(best(0.999, "fixed")),
                              "learned": summary(best(0.999, "learned"))}},
         "autotune": tuned,
+        "index_build": build,
         "probe_model": learned_info,
         "serving": serve,
         "sweep": sweep,
@@ -753,6 +769,40 @@ def main():
         print(json.dumps(out))
     if dist:
         dist.destroy_process_group()
+
+
+def device_build(args, torch, katoann, vectors, order, queries, gt, fixed, B, k):
+    """katoann.build_partition on the device-resident base vectors, then the
+    index of that partition and its recall at the fixed setting."""
+    L = args.nlist
+    torch.cuda.synchronize()
+    t0 = time.time()
+    cen, assign, rot, head = katoann.build_partition(
+        vectors, nlist=L, train_size=min(args.train, vectors.shape[0]), kmeans_iters=args.kmeans_iters,
+        seed=args.seed + 1, rotation_sample=100000)
+    build_s = time.time() - t0
+    a = torch.from_numpy(assign.astype(np.int64)).cuda()
+    pos = torch.argsort(a, stable=True)  # lists in ascending id order
+    del a
+    sizes = np.bincount(assign, minlength=L).astype(np.uint32)
+    idx = katoann.Index()
+    t1 = time.time()
+    moved = vectors[pos]
+    idx.load_arrays(cen, sizes, order[pos].to(torch.int32), moved, rotation=rot, head_dims=args.head,
+                    max_batch=B)
+    torch.cuda.synchronize()
+    load_s = time.time() - t1
+    del moved
+    torch.cuda.empty_cache()
+    ids, _ = idx.search(queries.cpu().numpy(), k=k, nprobe=fixed["nprobe"], survivors=fixed["survivors"])
+    del idx
+    return {"seconds": round(build_s, 1), "load_s": round(load_s, 1), "nlist": L,
+            "train": min(args.train, vectors.shape[0]), "kmeans_iters": args.kmeans_iters,
+            "empty_lists": int((sizes == 0).sum()), "max_list": int(sizes.max()),
+            "rotated": rot is not None, "head_dims": head,
+            "recall_at_fixed_setting": round(recall(ids, gt, k), 5),
+            "setting": {"nprobe": fixed["nprobe"], "survivors": fixed["survivors"]},
+            "api": "katoann.build_partition (device data, no files)"}
 
 
 def serving(katoann, idx, queries, rates, seconds, fixed, learned, seed=0):

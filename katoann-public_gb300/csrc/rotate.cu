@@ -54,6 +54,8 @@ __device__ __forceinline__ void cp_async16(float *dst, const float *src) {
 // kMajor: the staged parts are read from k-major copies xt (d x ldx, rows
 // zero-padded to ldx) and rt (d x ldr, columns zero-padded), 16 bytes per
 // copy; otherwise from the row-major inputs, 4 bytes per copy.
+// Two CTAs per SM (128 registers, a few spills) beat one CTA without spills:
+// 0.45 against 0.66 ms for 4096 x 1024 queries.
 template <bool kMajor>
 __global__ void __launch_bounds__(256, 2) rotate_lanes_kernel(const float *__restrict__ in,
                                                               uint32_t nrows, uint32_t d,
@@ -113,18 +115,23 @@ __global__ void __launch_bounds__(256, 2) rotate_lanes_kernel(const float *__res
     }
     __syncthreads();
     const uint32_t kend = min(static_cast<uint32_t>(kRotK), d16 - k0);
-    for (uint32_t c = 0; c < kend; c += 16) {
-      const float *xk = xs[buf] + (c + l) * kRotStride, *rk = rs[buf] + (c + l) * kRotStride;
-      const float4 x0 = *reinterpret_cast<const float4 *>(xk + rb);
-      const float4 x1 = *reinterpret_cast<const float4 *>(xk + rb + 4);
-      const float4 r0 = *reinterpret_cast<const float4 *>(rk + cb);
-      const float4 r1 = *reinterpret_cast<const float4 *>(rk + cb + 4);
-      const float xv[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
-      const float rv[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
+    // this lane's dimension of each 16-dimension step: fixed offsets from one
+    // base per chunk, the four steps unrolled (kend is a multiple of 16)
+    const float *xl = xs[buf] + l * kRotStride + rb, *rl = rs[buf] + l * kRotStride + cb;
 #pragma unroll
-      for (int a = 0; a < 8; ++a)
+    for (uint32_t c = 0; c < kRotK; c += 16) {
+      if (c < kend) {
+        const float4 x0 = *reinterpret_cast<const float4 *>(xl + c * kRotStride);
+        const float4 x1 = *reinterpret_cast<const float4 *>(xl + c * kRotStride + 4);
+        const float4 r0 = *reinterpret_cast<const float4 *>(rl + c * kRotStride);
+        const float4 r1 = *reinterpret_cast<const float4 *>(rl + c * kRotStride + 4);
+        const float xv[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+        const float rv[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
 #pragma unroll
-        for (int b = 0; b < 8; ++b) acc[a][b] = __fmaf_rn(xv[a], rv[b], acc[a][b]);
+        for (int a = 0; a < 8; ++a)
+#pragma unroll
+          for (int b = 0; b < 8; ++b) acc[a][b] = __fmaf_rn(xv[a], rv[b], acc[a][b]);
+      }
     }
     __syncthreads();  // the buffer is refilled by the next iteration's copies
   }

@@ -30,9 +30,9 @@ def test_other_phases():
 
 
 def test_traffic_per_tile_is_the_capture():
-    # 536.0 MB over 20,279 tiles in the 2M x 1024 capture: 26.4 KB per tile
-    assert bench.RANK_TC_DRAM_BYTES_PER_TILE == pytest.approx(536.0e6 / 20279)
-    assert 26_000 < bench.RANK_TC_DRAM_BYTES_PER_TILE < 27_000
+    # 2,657.6 MB over 96,108 tiles in the 10M x 1024 capture: 27.7 KB per tile
+    assert bench.RANK_TC_DRAM_BYTES_PER_TILE == pytest.approx(2657.6e6 / 96108)
+    assert 27_000 < bench.RANK_TC_DRAM_BYTES_PER_TILE < 28_000
 
 
 def test_workloads_and_metric_names():
