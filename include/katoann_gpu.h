@@ -208,9 +208,11 @@ uint32_t katoann_gpu_last_launches(void);
 int katoann_gpu_set_candidate_cap(uint32_t cap);
 
 /* Rows of each query's nearest lists that give it a bound before the
- * tensor-core ranking pass (0 = the default, max(1024, 8 x survivors); at
- * most 4096; process-wide). A tighter bound means fewer candidates to merge,
- * a looser one less work up front. Results do not depend on it. */
+ * tensor-core ranking pass (0 = the default, max(2048, 16 x survivors); at
+ * most 4096; process-wide). Beyond 3 x survivors rows, a sketch over their
+ * first 32 head bytes picks the 3 x survivors that are scored in full. More
+ * rows mean a tighter bound (fewer candidates to merge) for more work up
+ * front. Results do not depend on it. */
 int katoann_gpu_set_seed_rows(uint32_t rows);
 
 /* Knobs of the tensor-core ranking pass (process-wide; results never depend
@@ -391,7 +393,7 @@ int katoann_gpu_probe_grads(const katoann_gpu_probe_model *model, const float *d
                             float *d_gb1, float *d_gw2, float *d_gb2, float *d_gw3, float *d_gb3);
 
 /* The autotuner: times one search of these queries (the workspace sized for
- * it) under every candidate setting - seed rows {512, 1024, 2048}, split
+ * it) under every candidate setting - seed rows {1024, 2048, 4096}, split
  * weight {0, 1, 2, 4}, item width {default, 32} - and keeps the fastest
  * (settings that need a larger workspace are skipped). h_out[4] = {seed
  * rows, split weight, item width, microseconds per search}. Synchronous. */

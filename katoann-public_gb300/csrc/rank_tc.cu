@@ -578,7 +578,7 @@ __device__ __forceinline__ uint32_t row_dot(const uint8_t *row, const uint32_t *
 }
 
 // Dot products of a query (its h bytes as words in shared memory) with rows
-// r0 .. r0 + n - 1 of a byte plane, lanes split along each row: a group of
+// row(0) .. row(n - 1) of a byte plane, lanes split along each row: a group of
 // G = min(32, h / 16) lanes reads a row as one coalesced run of 16-byte
 // loads and sums over the group by shuffles. A warp takes 32 rows at a time
 // (G steps, all loads of the batch in flight together) and hands row
@@ -589,9 +589,9 @@ __device__ __forceinline__ uint32_t row_dot(const uint8_t *row, const uint32_t *
 // loaded at the start of the batch by the lane that later calls
 // f(i, dot, pre(i)), so that it arrives with the rows instead of after them.
 
-template <uint32_t G, typename F, typename Pre>
+template <uint32_t G, typename F, typename Pre, typename RowAt>
 __device__ __forceinline__ void rows_split(const uint8_t *__restrict__ x, uint32_t dc, uint32_t h,
-                                           const uint32_t *qw, uint32_t r0, uint32_t n, Pre pre,
+                                           const uint32_t *qw, RowAt row, uint32_t n, Pre pre,
                                            F f) {
   constexpr uint32_t RPW = 32 / G;  // rows per step
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -607,7 +607,7 @@ __device__ __forceinline__ void rows_split(const uint8_t *__restrict__ x, uint32
 #pragma unroll
       for (uint32_t it = 0; it < (G <= 16 ? G : 1); ++it) {
         const uint32_t i = base + it * RPW + sub;
-        v[it] = i < n ? __ldg(reinterpret_cast<const uint4 *>(x + static_cast<size_t>(r0 + i) * dc) + gl)
+        v[it] = i < n ? __ldg(reinterpret_cast<const uint4 *>(x + static_cast<size_t>(row(i)) * dc) + gl)
                       : make_uint4(0, 0, 0, 0);
       }
 #pragma unroll
@@ -623,7 +623,7 @@ __device__ __forceinline__ void rows_split(const uint8_t *__restrict__ x, uint32
         const uint32_t i = base + it * RPW + sub;
         uint32_t dot = 0;
         if (i < n) {
-          const uint4 *rv = reinterpret_cast<const uint4 *>(x + static_cast<size_t>(r0 + i) * dc);
+          const uint4 *rv = reinterpret_cast<const uint4 *>(x + static_cast<size_t>(row(i)) * dc);
           for (uint32_t c = 0; c < cpl; ++c) {
             const uint32_t u = gl + c * G;
             const uint4 vv = __ldg(rv + u);
@@ -640,23 +640,39 @@ __device__ __forceinline__ void rows_split(const uint8_t *__restrict__ x, uint32
   }
 }
 
+// rows_split with the group size for h.
+template <typename F, typename Pre, typename RowAt>
+__device__ __forceinline__ void for_rows_at(const uint8_t *__restrict__ x, uint32_t dc, uint32_t h,
+                                            const uint32_t *qw, RowAt row, uint32_t n, F f, Pre pre) {
+  const uint32_t g = min(32u, h / 16);
+  if (g == 16) rows_split<16>(x, dc, h, qw, row, n, pre, f);
+  else if (g == 32) rows_split<32>(x, dc, h, qw, row, n, pre, f);
+  else if (g == 8) rows_split<8>(x, dc, h, qw, row, n, pre, f);
+  else rows_split<4>(x, dc, h, qw, row, n, pre, f);
+}
+
+// The same over the contiguous rows r0 .. r0 + n - 1.
 template <typename F, typename Pre>
 __device__ __forceinline__ void for_rows_split(const uint8_t *__restrict__ x, uint32_t dc, uint32_t h,
                                                const uint32_t *qw, uint32_t r0, uint32_t n, F f,
                                                Pre pre) {
-  const uint32_t g = min(32u, h / 16);
-  if (g == 16) rows_split<16>(x, dc, h, qw, r0, n, pre, f);
-  else if (g == 32) rows_split<32>(x, dc, h, qw, r0, n, pre, f);
-  else if (g == 8) rows_split<8>(x, dc, h, qw, r0, n, pre, f);
-  else rows_split<4>(x, dc, h, qw, r0, n, pre, f);
+  for_rows_at(x, dc, h, qw, [r0](uint32_t i) { return r0 + i; }, n, f, pre);
 }
 
 // ------------------------------------------------------------- seed bounds
-// One CTA per query: l2 of the first `want` rows of its probed lists (probe
-// order, nearest list first), the S-th smallest by 8-bit radix digits, then
-// bound = L + (L >> 22) + 1: the distance value is monotone in l2 and two l2
-// that far apart never round to the same float, so every row whose distance
-// can tie the S-th best is still inside. Fewer than S rows: no bound.
+// One CTA per query. It looks at the first `want` rows of the query's probed
+// lists (probe order, nearest list first). When there are more than `full` of
+// them, a sketch picks the ones to score: the squared distance over the first
+// 32 head dimensions (the leading rotated dimensions, which carry most of the
+// variance), of which the `full` smallest are scored over all h dimensions.
+// The bound is the S-th smallest scored l2, widened to L + (L >> 22) + 1: the
+// distance value is monotone in l2 and two l2 that far apart never round to
+// the same float, so every row whose distance can tie the S-th best is still
+// inside. Any S of a query's candidates bound its S-th best from above, so
+// the rows the sketch picks change no result, only how tight the bound is
+// and how many bytes it costs: 2,048 sketched rows (32 bytes each) and 3S
+// scored rows read 2.3 times fewer bytes than 1,024 scored rows of 256 bytes
+// and leave fewer candidates. Fewer than S rows: no bound.
 // The queries grouped by their nearest list: a counting sort by one CTA, so
 // that seed CTAs reading the same list's rows run together and share them
 // through L2. order[i] = the query the i-th seed CTA takes.
@@ -679,55 +695,108 @@ __global__ void __launch_bounds__(1024) seed_order_kernel(const uint32_t *__rest
     order[atomicAdd(&lh[probed[static_cast<size_t>(q) * p]], 1u)] = q;
 }
 
+constexpr uint32_t kSketchBytes = 32;  // head bytes of a row the sketch reads
+
+__device__ __forceinline__ uint32_t sq_diff4(uint32_t a, uint32_t b, uint32_t acc) {
+  const uint32_t d = __vabsdiffu4(a, b);  // |a - b| per byte
+  return dp4(d, d, acc);
+}
+
 __global__ void __launch_bounds__(256, 3) rank_seed_kernel(
     const uint8_t *__restrict__ xhi, const int64_t *__restrict__ xnorm,
     const uint8_t *__restrict__ qhi, const int64_t *__restrict__ qnorm,
     const uint32_t *__restrict__ probed, const uint32_t *__restrict__ qprobes,
     const uint32_t *__restrict__ list_off, const uint32_t *__restrict__ order, uint32_t p,
-    uint32_t dc, uint32_t h, uint32_t S, uint32_t want, int32_t *__restrict__ bound) {
-  __shared__ int32_t l2s[kSeedCap];
-  __shared__ uint32_t qw[2048 / 4];
-  __shared__ uint32_t hist[256], sel[2], wsum[8];
+    uint32_t dc, uint32_t h, uint32_t S, uint32_t want, uint32_t full, int32_t *__restrict__ bound) {
+  // rowof: the rows looked at; val: their sketch keys. After the pick the
+  // scored rows are in val and their l2 go to rowof.
+  __shared__ uint32_t rowof[kSeedCap], val[kSeedCap];
+  __shared__ __align__(16) uint32_t qw[2048 / 4];
+  __shared__ uint32_t hist[256], sel[2], wsum[8], npick;
   const uint32_t q = order ? order[blockIdx.x] : blockIdx.x, tid = threadIdx.x;
   for (uint32_t i = tid; i < h / 4; i += blockDim.x)
     qw[i] = reinterpret_cast<const uint32_t *>(qhi + static_cast<size_t>(q) * dc)[i];
-  __syncthreads();
-  const int64_t qn = qnorm[q];
   const uint32_t pq = qprobes ? qprobes[q] : p;  // the query's own budget
   uint32_t count = 0;
   for (uint32_t r = 0; r < pq && count < want; ++r) {
     const uint32_t c = probed[static_cast<size_t>(q) * p + r];
-    const uint32_t r0 = list_off[c], n = min(list_off[c + 1] - r0, kSeedCap - count);
-    for_rows_split(
-        xhi, dc, h, qw, r0, n,
-        [&](uint32_t i, uint32_t dot, int64_t xn) {
-          l2s[count + i] = static_cast<int32_t>(qn + xn - 2 * static_cast<int64_t>(dot));
-        },
-        [&](uint32_t i) { return xnorm[r0 + i]; });
+    const uint32_t r0 = list_off[c], n = min(list_off[c + 1] - r0, want - count);
+    for (uint32_t i = tid; i < n; i += blockDim.x) rowof[count + i] = r0 + i;
     count += n;
   }
+  if (tid == 0) npick = 0;
   __syncthreads();
   if (count < S) {
     if (tid == 0) bound[q] = 0x7FFFFFFF;
     return;
   }
-  uint32_t prefix = 0, rank = S - 1;
-  for (int shift = 24; shift >= 0; shift -= 8) {
-    for (uint32_t i = tid; i < 256; i += blockDim.x) hist[i] = 0;
-    __syncthreads();
-    const uint32_t hm = shift == 24 ? 0u : (0xFFFFFFFFu << (shift + 8));
-    for (uint32_t i = tid; i < count; i += blockDim.x) {
-      const uint32_t v = static_cast<uint32_t>(l2s[i]);
-      if ((v & hm) == prefix) atomicAdd(&hist[(v >> shift) & 0xFFu], 1u);
+  // radix selection of the rank-th smallest of v[0 .. n) by 8-bit digits
+  auto select = [&](const uint32_t *v, uint32_t n, uint32_t rank) {
+    uint32_t prefix = 0;
+    for (int shift = 24; shift >= 0; shift -= 8) {
+      for (uint32_t i = tid; i < 256; i += blockDim.x) hist[i] = 0;
+      __syncthreads();
+      const uint32_t hm = shift == 24 ? 0u : (0xFFFFFFFFu << (shift + 8));
+      for (uint32_t i = tid; i < n; i += blockDim.x)
+        if ((v[i] & hm) == prefix) atomicAdd(&hist[(v[i] >> shift) & 0xFFu], 1u);
+      __syncthreads();
+      block_pick_digit(hist, rank, sel, wsum);
+      rank -= sel[1];
+      prefix |= sel[0] << shift;
+      __syncthreads();
+    }
+    return prefix;
+  };
+  const uint32_t *rows = rowof;
+  uint32_t *l2s = val, n = count;
+  if (count > full) {
+    // keys (sketch distance, at most 20 bits) << 12 | i: distinct, so
+    // exactly `full` of them are <= the full-th smallest
+    const uint32_t parts = min(kSketchBytes, h) / 16;  // lanes per row, 16 bytes each
+    const uint32_t part = tid % parts, per = blockDim.x / parts;
+    const uint4 qv = reinterpret_cast<const uint4 *>(qw)[part];
+    for (uint32_t base = 0; base < count; base += 4 * per) {
+      uint4 v[4];
+#pragma unroll
+      for (uint32_t j = 0; j < 4; ++j) {
+        const uint32_t i = base + j * per + tid / parts;
+        v[j] = i < count ? __ldg(reinterpret_cast<const uint4 *>(
+                               xhi + static_cast<size_t>(rowof[i]) * dc) + part)
+                         : make_uint4(0, 0, 0, 0);
+      }
+#pragma unroll
+      for (uint32_t j = 0; j < 4; ++j) {
+        uint32_t d2 = sq_diff4(v[j].x, qv.x, sq_diff4(v[j].y, qv.y,
+                      sq_diff4(v[j].z, qv.z, sq_diff4(v[j].w, qv.w, 0))));
+        if (parts == 2) d2 += __shfl_xor_sync(0xffffffffu, d2, 1);
+        const uint32_t i = base + j * per + tid / parts;
+        if (part == 0 && i < count) val[i] = (min(d2, 0xFFFFFu) << 12) | i;
+      }
     }
     __syncthreads();
-    block_pick_digit(hist, rank, sel, wsum);
-    rank -= sel[1];
-    prefix |= sel[0] << shift;
+    const uint32_t kth = select(val, count, full - 1);
+    uint32_t mine = 0;  // bit j: key tid + 256 j is picked (count <= 16 x 256)
+    for (uint32_t j = 0, i = tid; i < count; ++j, i += blockDim.x)
+      if (val[i] <= kth) mine |= 1u << j;
     __syncthreads();
+    for (uint32_t j = 0, i = tid; i < count; ++j, i += blockDim.x)
+      if (mine >> j & 1u) val[atomicAdd(&npick, 1u)] = rowof[i];
+    __syncthreads();
+    rows = val;
+    l2s = rowof;
+    n = full;
   }
+  const int64_t qn = qnorm[q];
+  for_rows_at(
+      xhi, dc, h, qw, [&](uint32_t i) { return rows[i]; }, n,
+      [&](uint32_t i, uint32_t dot, int64_t xn) {
+        l2s[i] = static_cast<uint32_t>(qn + xn - 2 * static_cast<int64_t>(dot));
+      },
+      [&](uint32_t i) { return xnorm[rows[i]]; });
+  __syncthreads();
+  const uint32_t L2 = select(l2s, n, S - 1);
   if (tid == 0) {
-    const int32_t v = static_cast<int32_t>(prefix);
+    const int32_t v = static_cast<int32_t>(L2);
     bound[q] = v + (v >> 22) + 1;
   }
 }
@@ -1117,8 +1186,11 @@ int rank_seed(const uint8_t *xhi, const int64_t *xnorm, const uint8_t *qhi, cons
     KATO_LAUNCHED("seed_order_kernel");
     ord = order;
   }
+  // rows the sketch picks to score in full: 3S (fewer loosen the bound, more
+  // cost bytes)
+  const uint32_t want = std::min(std::max(rows, S), kSeedCap);
   rank_seed_kernel<<<B, 256, 0, st>>>(xhi, xnorm, qhi, qnorm, probed, qprobes, list_off, ord, p, dc,
-                                      h, S, std::min(std::max(rows, S), kSeedCap), bound);
+                                      h, S, want, std::min(want, 3 * S), bound);
   KATO_LAUNCHED("rank_seed_kernel");
   return KATO_OK;
 }

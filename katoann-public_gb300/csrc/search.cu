@@ -27,7 +27,7 @@ namespace kato {
 thread_local uint32_t g_launches = 0;  // kernel launches of the last search pass
 // Entries per query of the tensor-core ranking pass's candidate buffer.
 std::atomic<uint32_t> g_candidate_cap{32768};
-// Rows a query's seed bound looks at (0: max(1024, 8 survivors)).
+// Rows a query's seed bound looks at (0: max(2048, 16 survivors)).
 std::atomic<uint32_t> g_seed_rows{0};
 
 namespace {
@@ -769,7 +769,7 @@ int make_plan(const katoann_gpu_index *ix, uint32_t B, uint32_t k, uint32_t p, i
     pl.select = true;
     pl.SC = pl.S;
     const uint32_t sr = g_seed_rows.load();
-    pl.seed_rows = sr ? std::max(sr, pl.S) : std::max(1024u, 8 * pl.S);
+    pl.seed_rows = sr ? std::max(sr, pl.S) : std::max(2048u, 16 * pl.S);
     pl.tcitems = static_cast<uint32_t>(bp / pl.tcs.N + std::min<size_t>(L, bp) + 1);
     // candidate records per CTA: room for 32 S per query of the batch, spread
     // over the CTAs (a CTA that runs out flags the queries it drops)
@@ -1193,7 +1193,7 @@ int autotune(const katoann_gpu_index *ix, const float *queries, uint32_t nq, uin
   float best = 1e30f;
   uint32_t bs = seed0, bb = beta0, bw = width0;
   int rc = KATO_OK;
-  for (uint32_t seed : {512u, 1024u, 2048u})
+  for (uint32_t seed : {1024u, 2048u, 4096u})
     for (uint32_t beta : {0u, 1u, 2u, 4u})
       for (uint32_t width : {0u, 32u}) {
         g_seed_rows = seed;

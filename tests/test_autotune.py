@@ -41,7 +41,7 @@ def test_every_knob_setting_matches_the_oracle(tmp_path):
     try:
         for beta in (0, 1, 4, 8):
             for width in (0, 16, 32):
-                for seed in (0, 64, 2048):
+                for seed in (0, 64, 2048, 4096):
                     assert lib.katoann_gpu_set_rank_schedule(beta) == 0
                     assert lib.katoann_gpu_set_rank_width(width) == 0
                     assert lib.katoann_gpu_set_seed_rows(seed) == 0
@@ -66,7 +66,7 @@ def test_autotune_keeps_results(tmp_path):
     ref = oracle.OracleIndex(prefix)
     try:
         t = idx.autotune(queries, k=10, nprobe=12, survivors=32)
-        assert t["seed_rows"] in (512, 1024, 2048) and t["schedule"] in (0, 1, 2, 4)
+        assert t["seed_rows"] in (1024, 2048, 4096) and t["schedule"] in (0, 1, 2, 4)
         assert t["width"] in (0, 32) and t["us_per_search"] > 0
         got = idx.search(queries, k=10, nprobe=12, survivors=32)
         want = ref.search(queries, k=10, nprobe=12, survivors=32)

@@ -25,8 +25,10 @@ def test_other_phases():
         B * S * (2 * DC + 12) / 1e9)
     assert bench.phase_work("coarse select", B, L, DC, D, P, S, H, 0, 0)[1] == pytest.approx(
         B * L * 4 / 1e9)
+    # 2,048 sketched rows of 32 bytes and 3S = 192 rows of 256 bytes per query
     assert bench.phase_work("seed bounds", B, L, DC, D, P, S, H, 0, 0)[1] == pytest.approx(
-        B * bench.SEED_ROWS * H / 1e9)
+        B * (2048 * 32 + 3 * S * H) / 1e9)
+    assert bench.seed_bytes(B, 128, S, H) == B * 128 * H  # few rows: all in full
 
 
 def test_traffic_per_tile_is_the_capture():
