@@ -349,7 +349,18 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------ roofline
-SEED_ROWS = 1024  # rows behind each query's seed bound (the library default for survivors <= 128)
+SEED_ROWS = 2048  # rows behind each query's seed bound (the library default for survivors <= 128)
+SKETCH_BYTES = 32  # head bytes of a row the seed's sketch reads
+
+
+def seed_bytes(B: int, rows: int, S: int, head: int) -> float:
+    """Bytes the seed bounds read: every looked-at row's first SKETCH_BYTES
+    head bytes and the 3S rows the sketch picks in full; with at most 3S rows
+    every row in full."""
+    full = min(rows, 3 * S)
+    if rows > full:
+        return float(B) * (rows * min(SKETCH_BYTES, head) + full * head)
+    return float(B) * rows * head
 
 # DRAM bytes per 128-row tile of the tensor-core ranking kernel: one ncu
 # capture (dram__bytes_read.sum + dram__bytes_write.sum, one pass) of this
@@ -372,8 +383,9 @@ def phase_work(phase: str, B: int, L: int, dc: int, d: int, nprobe: int, S: int,
         # summed from the same bytes; ids are only read for the survivors)
         return "hbm", probed_lists_rows * head / 1e9, "GB/s"
     if phase == "seed bounds":
-        # the first SEED_ROWS rows of each query's nearest lists
-        return "hbm", B * SEED_ROWS * head / 1e9, "GB/s"
+        # the sketch over the first SEED_ROWS rows of each query's nearest
+        # lists, and the rows it picks
+        return "hbm", seed_bytes(B, SEED_ROWS, S, head) / 1e9, "GB/s"
     if phase == "refine":
         return "hbm", B * S * (2 * dc + 8 + 4) / 1e9, "GB/s"
     if phase == "rotate+quantize":
@@ -788,8 +800,10 @@ def device_build(args, torch, katoann, vectors, order, queries, gt, fixed, B, k)
     idx = katoann.Index()
     t1 = time.time()
     moved = vectors[pos]
-    idx.load_arrays(cen, sizes, order[pos].to(torch.int32), moved, rotation=rot, head_dims=args.head,
-                    max_batch=B)
+    # device vectors: every array goes in as a CUDA tensor
+    idx.load_arrays(torch.from_numpy(cen).cuda(), sizes, order[pos].to(torch.int32), moved,
+                    rotation=None if rot is None else torch.from_numpy(rot).cuda(),
+                    head_dims=args.head, max_batch=B)
     torch.cuda.synchronize()
     load_s = time.time() - t1
     del moved
@@ -807,9 +821,9 @@ def device_build(args, torch, katoann, vectors, order, queries, gt, fixed, B, k)
 
 def serving(katoann, idx, queries, rates, seconds, fixed, learned, seed=0):
     """Poisson arrivals at each rate, k drawn from {10, 100} per request, served
-    by katoann.Server (continuous batching, 3 batches in flight) from the
-    library's native client; latency from the scheduled arrival to
-    completion. `fixed` / `learned` are the search settings (learned: model,
+    by katoann.Server (continuous batching, 3 batches in flight, each a replay
+    of a captured search graph) from the library's native client; latency
+    from the scheduled arrival to completion. `fixed` / `learned` are the search settings (learned: model,
     threshold, cap)."""
     out = []
     q = queries.cpu().numpy()
@@ -818,16 +832,20 @@ def serving(katoann, idx, queries, rates, seconds, fixed, learned, seed=0):
             continue
         server = katoann.Server(idx, max_batch=4096, max_in_flight=3, max_k=100,
                                 nprobe=cfg["nprobe"], survivors=cfg["survivors"],
-                                budget=cfg.get("model"), threshold=cfg.get("threshold", 0.95))
+                                budget=cfg.get("model"), threshold=cfg.get("threshold", 0.95),
+                                warm_k=(10, 100))
         for _ in range(2):  # warm-up: a full batch of each k
             for r in [server.submit(q[i], k) for k in (10, 100) for i in range(len(q))]:
                 server.wait(r)
         for rate in rates:
             n = max(2000, int(rate * seconds))
             r = server.load(q, rate, n, kmix=(10, 100), seed=seed + int(rate))
+            st = server.stats()
             out.append({"nprobe_path": name, "rate": rate, "requests": n,
                         **{key: (round(v, 3) if isinstance(v, float) else v)
-                           for key, v in r.items()}})
+                           for key, v in r.items()},
+                        "graph_batches": st["graph_batches"], "graphs": st["graphs"],
+                        "batches_so_far": st["batches"]})
         del server
     return out
 

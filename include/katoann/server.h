@@ -33,6 +33,15 @@ struct ServerOptions {
   const ProbeModel *budget = nullptr;  // learned per-query nprobe (null: fixed)
   float budget_threshold = 0.95f;
   double max_wait_ms = 0;         // a partial batch waits this long for more requests
+  // Replay captured CUDA graphs: each slot owns a full batch's device memory
+  // and keeps one captured search per (k, batch size rounded up to a power of
+  // two), captured on first use; a batch's queries are padded to that size
+  // with copies of its first query. Enqueuing a batch is then one graph
+  // launch and four copies. Needs an HBM budget of max_in_flight full batches
+  // (the default); with less, batches are carved from the pool and launched
+  // kernel by kernel.
+  bool graphs = true;
+  std::vector<uint32_t> warm_k;   // k whose graphs are captured for every slot and size up front
 };
 
 struct ServerResult {
@@ -50,6 +59,8 @@ struct ServerStats {
   // where a batch's time goes, at most (since construction or reset_peaks):
   double max_enqueue_ms = 0;      // host: staging the queries and enqueuing copies and kernels
   double max_batch_gpu_ms = 0;    // device: the batch's copies and search, on its stream
+  uint64_t graph_batches = 0;     // batches run as a graph replay
+  uint32_t graphs = 0;            // graphs captured
 };
 
 struct LoadReport {

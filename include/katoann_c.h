@@ -139,11 +139,14 @@ int katoann_probe_predict(const void *model, const float *z, uint32_t n, float t
 /* ------------------------------------------- continuous-batching server
  * katoann::Server (include/katoann/server.h); supersedes the serial loop of
  * the reference's `katoann load` (tools/katoann.cpp:304-321). hbm_budget 0:
- * room for max_in_flight full batches; model NULL: fixed nprobe. */
+ * room for max_in_flight full batches; model NULL: fixed nprobe. graphs != 0:
+ * replay captured searches (ServerOptions::graphs), those of the n_warm k in
+ * warm_k captured up front. */
 int katoann_server_new(void *index, uint32_t max_batch, uint32_t max_in_flight,
                        uint64_t hbm_budget, uint32_t max_k, uint32_t nprobe, int ranking,
                        uint32_t survivors, const void *model, float threshold,
-                       double max_wait_ms, void **server);
+                       double max_wait_ms, int graphs, const uint32_t *warm_k, uint32_t n_warm,
+                       void **server);
 void katoann_server_free(void *server);
 /* Queues one query (dim floats) with its k; *id receives the request id. */
 int katoann_server_submit(void *server, const float *query, uint32_t k, uint64_t *id);
@@ -155,8 +158,8 @@ int katoann_server_wait(void *server, uint64_t id, uint32_t *ids, float *dists,
 int katoann_server_poll(void *server, uint64_t id, uint32_t *ids, float *dists,
                         uint32_t *nprobe, double *latency_ms, int *done);
 int katoann_server_drain(void *server);
-/* stats[7] = {requests, batches, peak_in_flight, peak_hbm_bytes, mean_batch x 1000,
- * max_enqueue_ms x 1000, max_batch_gpu_ms x 1000} */
+/* stats[9] = {requests, batches, peak_in_flight, peak_hbm_bytes, mean_batch x 1000,
+ * max_enqueue_ms x 1000, max_batch_gpu_ms x 1000, graph_batches, graphs} */
 int katoann_server_stats(void *server, uint64_t *stats);
 /* katoann::run_load: n Poisson arrivals at `rate` from a native client, queries
  * round-robin from queries (nq x dim), k uniform over kmix. report[13] =

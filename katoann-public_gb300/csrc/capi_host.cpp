@@ -230,7 +230,8 @@ const void *katoann_index_device_view(void *index) { return I(index)->device_vie
 int katoann_server_new(void *index, uint32_t max_batch, uint32_t max_in_flight,
                        uint64_t hbm_budget, uint32_t max_k, uint32_t nprobe, int ranking,
                        uint32_t survivors, const void *model, float threshold,
-                       double max_wait_ms, void **server) {
+                       double max_wait_ms, int graphs, const uint32_t *warm_k, uint32_t n_warm,
+                       void **server) {
   return guarded([&] {
     katoann::ServerOptions o;
     o.max_batch = max_batch;
@@ -243,6 +244,8 @@ int katoann_server_new(void *index, uint32_t max_batch, uint32_t max_in_flight,
     o.budget = M(model);
     o.budget_threshold = threshold;
     o.max_wait_ms = max_wait_ms;
+    o.graphs = graphs != 0;
+    if (warm_k) o.warm_k.assign(warm_k, warm_k + n_warm);
     *server = new katoann::Server(*I(index), o);
   });
 }
@@ -309,6 +312,8 @@ int katoann_server_stats(void *server, uint64_t *stats) {
     stats[4] = static_cast<uint64_t>(s.mean_batch * 1000.0);
     stats[5] = static_cast<uint64_t>(s.max_enqueue_ms * 1000.0);
     stats[6] = static_cast<uint64_t>(s.max_batch_gpu_ms * 1000.0);
+    stats[7] = s.graph_batches;
+    stats[8] = s.graphs;
   });
 }
 

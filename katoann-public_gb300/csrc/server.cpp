@@ -8,6 +8,8 @@
 // batches in launch order, hands the results to their requests and returns
 // the memory and the slot. A batch that does not fit in the free pool waits
 // for completions; with nothing in flight it is cut to the size that fits.
+// In graph mode every slot owns a full batch's memory instead, and a batch
+// replays the slot's captured search for its k and padded size.
 #include "katoann/server.h"
 
 #include <cuda_runtime.h>
@@ -119,6 +121,18 @@ struct Slot {
   float *hd = nullptr;
   uint32_t *hnp = nullptr;   // pinned: max_batch
   bool busy = false;
+  size_t base = SIZE_MAX;    // graph mode: the slot's own block of the pool
+  std::map<uint64_t, void *> graph;  // (k << 32 | padded size) -> captured search
+};
+
+// Device pointers of one batch of n queries at k within its memory block.
+struct Layout {
+  unsigned char *ws;
+  size_t ws_bytes;
+  float *dq;
+  uint32_t *dids;
+  float *dd;
+  uint32_t *dnp;
 };
 
 struct Batch {
@@ -128,6 +142,7 @@ struct Batch {
   std::vector<Request> reqs;
   std::string err;           // a launch that failed
   double enqueue_ms = 0;     // host time of launch()
+  bool graph = false;        // replayed a captured search
 };
 
 }  // namespace
@@ -152,12 +167,65 @@ struct Server::Impl {
   double max_enqueue_ms = 0, max_batch_gpu_ms = 0;
   bool stop = false;
   std::thread dispatcher, completer;
+  bool graphs = false;        // graph mode (fixed slot memory, captured searches)
+  size_t slot_bytes = 0;      // a slot's block in graph mode
+  uint64_t graph_batches = 0;
+  uint32_t graphs_captured = 0;  // written by the thread that captures, under mu
 
   size_t batch_bytes(uint32_t n, uint32_t k) const {
     const size_t ws = katoann_gpu_search_workspace(view, n, k, depth, rk, opt.survivors);
     if (ws == 0) return 0;
     return align256(ws) + align256(size_t(n) * dim * 4) + 2 * align256(size_t(n) * k * 4) +
            align256(size_t(n) * 4);
+  }
+
+  Layout layout(unsigned char *p, uint32_t n, uint32_t k) const {
+    Layout L;
+    L.ws = p;
+    L.ws_bytes = align256(katoann_gpu_search_workspace(view, n, k, depth, rk, opt.survivors));
+    L.dq = reinterpret_cast<float *>(p + L.ws_bytes);
+    L.dids = reinterpret_cast<uint32_t *>(p + L.ws_bytes + align256(size_t(n) * dim * 4));
+    L.dd = reinterpret_cast<float *>(reinterpret_cast<unsigned char *>(L.dids) +
+                                     align256(size_t(n) * k * 4));
+    L.dnp = reinterpret_cast<uint32_t *>(reinterpret_cast<unsigned char *>(L.dd) +
+                                         align256(size_t(n) * k * 4));
+    return L;
+  }
+
+  // graph mode: the size a batch of n runs at, the next power of two (at
+  // most max_batch)
+  uint32_t padded(uint32_t n) const {
+    uint32_t b = 1;
+    while (b < n) b <<= 1;
+    return std::min(b, max_batch);
+  }
+
+  // The slot's captured search for (k, nb), captured now if it is not yet;
+  // null with *err set on failure. Only the thread that owns the slot (the
+  // dispatcher, or the constructor before it starts) calls this.
+  void *graph_for(Slot &s, uint32_t k, uint32_t nb, std::string *err) {
+    const uint64_t key = (uint64_t(k) << 32) | nb;
+    auto it = s.graph.find(key);
+    if (it != s.graph.end()) return it->second;
+    if (batch_bytes(nb, k) > slot_bytes) {
+      *err = "server: a batch of " + std::to_string(nb) + " at k " + std::to_string(k) +
+             " needs more device memory than a slot holds";
+      return nullptr;
+    }
+    const Layout L = layout(pool.at(s.base), nb, k);
+    void *g = nullptr;
+    if (katoann_gpu_search_capture(view, L.dq, nb, k, opt.nprobe, rk, opt.survivors, nb, nullptr,
+                                   use_model ? &model : nullptr, L.ws, L.ws_bytes, L.dids, L.dd,
+                                   L.dnp, reinterpret_cast<katoann_stream_t>(s.stream), &g)) {
+      *err = std::string("search graph: ") + katoann_gpu_last_error();
+      return nullptr;
+    }
+    s.graph.emplace(key, g);
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      ++graphs_captured;
+    }
+    return g;
   }
 
   // the oldest waiting request's class, or 0
@@ -186,38 +254,37 @@ struct Server::Impl {
       ~Timed() { b.enqueue_ms = std::chrono::duration<double, std::milli>(Clock::now() - h0).count(); }
     } timed{b, h0};
     Slot &s = *b.slot;
-    const uint32_t n = b.n, k = b.k;
+    const uint32_t n = b.n, k = b.k, nb = graphs ? padded(n) : n;
     for (uint32_t i = 0; i < n; ++i)
       std::memcpy(s.hq + size_t(i) * dim, b.reqs[i].q.data(), size_t(dim) * 4);
-    unsigned char *p = pool.at(b.off);
-    const size_t ws = align256(katoann_gpu_search_workspace(view, n, k, depth, rk, opt.survivors));
-    float *dq = reinterpret_cast<float *>(p + ws);
-    uint32_t *dids = reinterpret_cast<uint32_t *>(p + ws + align256(size_t(n) * dim * 4));
-    float *dd = reinterpret_cast<float *>(reinterpret_cast<unsigned char *>(dids) +
-                                          align256(size_t(n) * k * 4));
-    uint32_t *dnp = reinterpret_cast<uint32_t *>(reinterpret_cast<unsigned char *>(dd) +
-                                                 align256(size_t(n) * k * 4));
+    for (uint32_t i = n; i < nb; ++i)  // padding: the first query again
+      std::memcpy(s.hq + size_t(i) * dim, s.hq, size_t(dim) * 4);
+    const Layout L = layout(pool.at(graphs ? s.base : b.off), nb, k);
     const auto st = reinterpret_cast<katoann_stream_t>(s.stream);
+    void *g = nullptr;
+    if (graphs && !(g = graph_for(s, k, nb, &b.err))) return;
     cudaError_t e = cudaEventRecord(s.start, s.stream);
     if (e != cudaSuccess) {
       b.err = std::string("cudaEventRecord: ") + cudaGetErrorString(e);
       return;
     }
-    e = cudaMemcpyAsync(dq, s.hq, size_t(n) * dim * 4, cudaMemcpyHostToDevice, s.stream);
+    e = cudaMemcpyAsync(L.dq, s.hq, size_t(nb) * dim * 4, cudaMemcpyHostToDevice, s.stream);
     if (e != cudaSuccess) {
       b.err = std::string("copy queries: ") + cudaGetErrorString(e);
       return;
     }
-    const int rc = katoann_gpu_search_budget(view, dq, n, k, opt.nprobe, rk, opt.survivors, n,
-                                             nullptr, use_model ? &model : nullptr, p, ws, dids,
-                                             dd, dnp, st, nullptr);
+    const int rc = g ? katoann_gpu_graph_launch(g, st)
+                     : katoann_gpu_search_budget(view, L.dq, n, k, opt.nprobe, rk, opt.survivors, n,
+                                                 nullptr, use_model ? &model : nullptr, L.ws,
+                                                 L.ws_bytes, L.dids, L.dd, L.dnp, st, nullptr);
     if (rc) {
       b.err = katoann_gpu_last_error();
       return;
     }
-    cudaMemcpyAsync(s.hids, dids, size_t(n) * k * 4, cudaMemcpyDeviceToHost, s.stream);
-    cudaMemcpyAsync(s.hd, dd, size_t(n) * k * 4, cudaMemcpyDeviceToHost, s.stream);
-    cudaMemcpyAsync(s.hnp, dnp, size_t(n) * 4, cudaMemcpyDeviceToHost, s.stream);
+    b.graph = g != nullptr;
+    cudaMemcpyAsync(s.hids, L.dids, size_t(n) * k * 4, cudaMemcpyDeviceToHost, s.stream);
+    cudaMemcpyAsync(s.hd, L.dd, size_t(n) * k * 4, cudaMemcpyDeviceToHost, s.stream);
+    cudaMemcpyAsync(s.hnp, L.dnp, size_t(n) * 4, cudaMemcpyDeviceToHost, s.stream);
     e = cudaEventRecord(s.event, s.stream);
     if (e != cudaSuccess) b.err = std::string("cudaEventRecord: ") + cudaGetErrorString(e);
   }
@@ -239,8 +306,8 @@ struct Server::Impl {
         }
       }
       uint32_t n = static_cast<uint32_t>(std::min<size_t>(q.size(), max_batch));
-      size_t bytes = batch_bytes(n, k);
-      size_t off = pool.take(bytes);
+      size_t bytes = graphs ? 0 : batch_bytes(n, k);
+      size_t off = graphs ? free_slot()->base : pool.take(bytes);
       if (off == SIZE_MAX) {
         if (in_flight > 0) {  // wait for memory to come back
           cv_dispatch.wait(lk);
@@ -268,7 +335,7 @@ struct Server::Impl {
         bytes = batch_bytes(n, k);
         off = pool.take(bytes);
       }
-      Batch b{free_slot(), k, n, off, bytes, {}, {}};
+      Batch b{free_slot(), k, n, off, bytes, {}, {}, 0, false};
       b.slot->busy = true;
       b.reqs.reserve(n);
       for (uint32_t i = 0; i < n; ++i) {
@@ -284,6 +351,7 @@ struct Server::Impl {
       launch(b);  // no lock held while the host copies and enqueues
       lk.lock();
       max_enqueue_ms = std::max(max_enqueue_ms, b.enqueue_ms);
+      graph_batches += b.graph ? 1 : 0;
       launched.push_back(std::move(b));
       cv_complete.notify_one();
     }
@@ -326,7 +394,7 @@ struct Server::Impl {
         en.err = err;
         en.res = std::move(res[i]);
       }
-      pool.give(b.off, b.bytes);
+      if (b.bytes) pool.give(b.off, b.bytes);
       max_batch_gpu_ms = std::max(max_batch_gpu_ms, static_cast<double>(gpu_ms));
       b.slot->busy = false;
       --in_flight;
@@ -364,8 +432,10 @@ Server::Server(const Index &index, const ServerOptions &opt) : m_(new Impl) {
   }
   const size_t full = m.batch_bytes(m.max_batch, opt.max_k);
   if (full == 0) throw std::invalid_argument(katoann_gpu_last_error());
-  const size_t budget = opt.hbm_budget ? opt.hbm_budget : full * opt.max_in_flight;
+  const size_t budget = opt.hbm_budget ? opt.hbm_budget : align256(full) * opt.max_in_flight;
   m.pool.init(budget);
+  m.graphs = opt.graphs && budget >= align256(full) * opt.max_in_flight;
+  m.slot_bytes = full;
   m.slots.resize(opt.max_in_flight);
   for (Slot &s : m.slots) {
     cuda_check(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking), "server stream");
@@ -375,7 +445,18 @@ Server::Server(const Index &index, const ServerOptions &opt) : m_(new Impl) {
     cuda_check(cudaMallocHost(&s.hids, size_t(m.max_batch) * opt.max_k * 4), "server pinned ids");
     cuda_check(cudaMallocHost(&s.hd, size_t(m.max_batch) * opt.max_k * 4), "server pinned dists");
     cuda_check(cudaMallocHost(&s.hnp, size_t(m.max_batch) * 4), "server pinned nprobe");
+    if (m.graphs) s.base = m.pool.take(full);  // the slot's for good
   }
+  if (m.graphs)
+    for (const uint32_t k : opt.warm_k) {
+      if (k == 0 || k > opt.max_k) throw std::invalid_argument("server: warm k must be 1 to max_k");
+      for (Slot &s : m.slots)
+        for (uint32_t nb = 1;; nb = std::min(2 * nb, m.max_batch)) {
+          std::string err;
+          if (!m.graph_for(s, k, nb, &err)) throw std::runtime_error(err);
+          if (nb == m.max_batch) break;
+        }
+    }
   m.dispatcher = std::thread([&m] { m.dispatch_loop(); });
   m.completer = std::thread([&m] { m.complete_loop(); });
 }
@@ -391,6 +472,7 @@ Server::~Server() {
   m.cv_complete.notify_all();
   if (m.completer.joinable()) m.completer.join();
   for (Slot &s : m.slots) {
+    for (auto &g : s.graph) katoann_gpu_graph_destroy(g.second);
     if (s.event) cudaEventDestroy(s.event);
     if (s.start) cudaEventDestroy(s.start);
     if (s.stream) cudaStreamDestroy(s.stream);
@@ -525,6 +607,8 @@ ServerStats Server::stats() const {
   s.mean_batch = m.nbatches ? double(m.batched) / double(m.nbatches) : 0;
   s.max_enqueue_ms = m.max_enqueue_ms;
   s.max_batch_gpu_ms = m.max_batch_gpu_ms;
+  s.graph_batches = m.graph_batches;
+  s.graphs = m.graphs_captured;
   return s;
 }
 

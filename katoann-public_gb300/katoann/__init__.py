@@ -82,7 +82,8 @@ def _load():
     lib.katoann_probe_weights.argtypes = [P, P, P, P, P, P, P, P, P]
     lib.katoann_probe_features.argtypes = [P, P, U32, U32, P]
     lib.katoann_probe_predict.argtypes = [P, P, U32, F, U32, P, P]
-    lib.katoann_server_new.argtypes = [P, U32, U32, U64, U32, U32, I32, U32, P, F, D, C.POINTER(P)]
+    lib.katoann_server_new.argtypes = [P, U32, U32, U64, U32, U32, I32, U32, P, F, D, I32, P, U32,
+                                       C.POINTER(P)]
     lib.katoann_server_free.argtypes = [P]
     lib.katoann_server_submit.argtypes = [P, P, U32, C.POINTER(U64)]
     lib.katoann_server_wait.argtypes = [P, U64, P, P, P, P]
@@ -646,17 +647,19 @@ class Server:
                  hbm_budget: int = 0, max_k: int = 128, nprobe: int = 64,
                  ranking: str = "prefix", survivors: int = 32,
                  budget: "ProbeModel | None" = None, threshold: float = 0.95,
-                 max_wait_ms: float = 0.0):
+                 max_wait_ms: float = 0.0, graphs: bool = True, warm_k=()):
         self._index = index  # the server reads the index's device arrays
         self._budget = budget
         self.dim = index.dim
         self.normalized = index.normalized
         self._k = {}
         h = C.c_void_p()
+        warm = np.ascontiguousarray(warm_k, dtype=np.uint32)
         _check(_lib.katoann_server_new(index._h, max_batch, max_in_flight, hbm_budget, max_k,
                                        nprobe, _RANKING[ranking], survivors,
                                        budget._h if budget is not None else None, threshold,
-                                       max_wait_ms, C.byref(h)))
+                                       max_wait_ms, int(graphs), _ptr(warm) if warm.size else None,
+                                       warm.size, C.byref(h)))
         self._h = h.value
 
     def __del__(self):
@@ -711,8 +714,9 @@ class Server:
         return out
 
     def stats(self) -> dict:
-        s = np.zeros(7, np.uint64)
+        s = np.zeros(9, np.uint64)
         _check(_lib.katoann_server_stats(self._h, _ptr(s)))
         return dict(requests=int(s[0]), batches=int(s[1]), peak_in_flight=int(s[2]),
                     peak_hbm_bytes=int(s[3]), mean_batch=float(s[4]) / 1000.0,
-                    max_enqueue_ms=float(s[5]) / 1000.0, max_batch_gpu_ms=float(s[6]) / 1000.0)
+                    max_enqueue_ms=float(s[5]) / 1000.0, max_batch_gpu_ms=float(s[6]) / 1000.0,
+                    graph_batches=int(s[7]), graphs=int(s[8]))

@@ -71,13 +71,19 @@ def test_results_in_the_mix_equal_alone(tmp_path, learned):
         model = katoann.ProbeModel.train(idx, train, ladder=(2, 4, 8, 16, 32), depth=32,
                                          label_nprobe=96, survivors=32, epochs=10, batch=256)
     ks = np.random.default_rng(3).choice([10, 100], len(queries))
+    # learned: the graphs of k = 10 captured up front (3 slots x sizes 1 .. 64)
     server = katoann.Server(idx, max_batch=64, max_in_flight=3, max_k=100, nprobe=32,
-                            survivors=32, budget=model, threshold=0.9)
+                            survivors=32, budget=model, threshold=0.9,
+                            warm_k=(10,) if learned else ())
+    if learned:
+        assert server.stats()["graphs"] == 3 * 7
     res = _serve(server, queries, ks)
     stats = server.stats()
     assert stats["requests"] == len(queries) and stats["batches"] >= len(queries) / 64
     assert stats["peak_in_flight"] >= 1
     assert stats["max_batch_gpu_ms"] > 0 and stats["max_enqueue_ms"] > 0
+    # every batch replayed a captured search, its queries padded to a power of two
+    assert stats["graph_batches"] == stats["batches"] and stats["graphs"] >= 2
     assert all(r[3] > 0 for r in res)
     _check_alone(idx, queries, ks, res, nprobe=32, survivors=32, budget=model, threshold=0.9)
 
@@ -92,12 +98,13 @@ def test_hbm_budget_cuts_batches(tmp_path):
     res16 = _serve(probe, queries, ks, threads=1)
     budget = probe.stats()["peak_hbm_bytes"]
     del probe
-    # a server allowed 4096-query batches, but with only that much memory
+    # a server allowed 4096-query batches, but with only that much memory:
+    # too little for a slot of its own per batch, so no graphs either
     small = katoann.Server(idx, max_batch=4096, max_in_flight=2, max_k=10, nprobe=16,
                            hbm_budget=budget)
     res = _serve(small, queries, ks, threads=2)
     st = small.stats()
-    assert st["peak_hbm_bytes"] <= budget
+    assert st["peak_hbm_bytes"] <= budget and st["graph_batches"] == 0
     assert st["batches"] >= len(queries) // 16 and st["mean_batch"] <= 16
     for a, b in zip(res, res16):
         assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
@@ -105,7 +112,8 @@ def test_hbm_budget_cuts_batches(tmp_path):
 
 
 @pytest.mark.gpu
-def test_burst_overlaps_batches_and_matches_the_oracle(tmp_path):
+@pytest.mark.parametrize("graphs", [True, False])
+def test_burst_overlaps_batches_and_matches_the_oracle(tmp_path, graphs):
     """1,200 requests submitted at once: the dispatcher launches a batch and
     forms the next while it runs, so at least two batches are on the device
     together; every result is the oracle's for that query, bit for bit."""
@@ -114,7 +122,8 @@ def test_burst_overlaps_batches_and_matches_the_oracle(tmp_path):
     queries, idx = _index(tmp_path)
     ref = oracle.OracleIndex(str(tmp_path / "x"))
     qs = np.concatenate([queries] * 3)
-    server = katoann.Server(idx, max_batch=64, max_in_flight=3, max_k=10, nprobe=96, survivors=256)
+    server = katoann.Server(idx, max_batch=64, max_in_flight=3, max_k=10, nprobe=96, survivors=256,
+                            graphs=graphs)
     tickets = [server.submit(q, 10) for q in qs]
     res = [server.wait(t) for t in tickets]
     st = server.stats()
