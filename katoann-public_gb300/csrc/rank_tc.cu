@@ -664,7 +664,8 @@ __device__ __forceinline__ void for_rows_split(const uint8_t *__restrict__ x, ui
 // lists (probe order, nearest list first). When there are more than `full` of
 // them, a sketch picks the ones to score: the squared distance over the first
 // 32 head dimensions (the leading rotated dimensions, which carry most of the
-// variance), of which the `full` smallest are scored over all h dimensions.
+// variance), of which the `full` smallest, and any others in the last one's
+// bin of sketch distance / 16, are scored over all h dimensions.
 // The bound is the S-th smallest scored l2, widened to L + (L >> 22) + 1: the
 // distance value is monotone in l2 and two l2 that far apart never round to
 // the same float, so every row whose distance can tie the S-th best is still
@@ -730,10 +731,12 @@ __global__ void __launch_bounds__(256, 3) rank_seed_kernel(
     if (tid == 0) bound[q] = 0x7FFFFFFF;
     return;
   }
-  // radix selection of the rank-th smallest of v[0 .. n) by 8-bit digits
-  auto select = [&](const uint32_t *v, uint32_t n, uint32_t rank) {
+  // radix selection of the rank-th smallest of v[0 .. n) by 8-bit digits,
+  // from the digit at bit `start` down to the one at bit `stop` (the lower
+  // bits of the result stay 0; digits above `start` must be 0 in every value)
+  auto select = [&](const uint32_t *v, uint32_t n, uint32_t rank, int start, int stop) {
     uint32_t prefix = 0;
-    for (int shift = 24; shift >= 0; shift -= 8) {
+    for (int shift = start; shift >= stop; shift -= 8) {
       for (uint32_t i = tid; i < 256; i += blockDim.x) hist[i] = 0;
       __syncthreads();
       const uint32_t hm = shift == 24 ? 0u : (0xFFFFFFFFu << (shift + 8));
@@ -750,8 +753,10 @@ __global__ void __launch_bounds__(256, 3) rank_seed_kernel(
   const uint32_t *rows = rowof;
   uint32_t *l2s = val, n = count;
   if (count > full) {
-    // keys (sketch distance, at most 20 bits) << 12 | i: distinct, so
-    // exactly `full` of them are <= the full-th smallest
+    // keys (sketch distance, at most 20 bits) << 12 | i. Two digits find the
+    // 16-bit bin (sketch distance >> 4) of the full-th smallest key; every
+    // row in or below that bin is scored: at least `full`, a few more when
+    // the bin holds several
     const uint32_t parts = min(kSketchBytes, h) / 16;  // lanes per row, 16 bytes each
     const uint32_t part = tid % parts, per = blockDim.x / parts;
     const uint4 qv = reinterpret_cast<const uint4 *>(qw)[part];
@@ -774,7 +779,7 @@ __global__ void __launch_bounds__(256, 3) rank_seed_kernel(
       }
     }
     __syncthreads();
-    const uint32_t kth = select(val, count, full - 1);
+    const uint32_t kth = select(val, count, full - 1, 24, 16) | 0xFFFFu;
     uint32_t mine = 0;  // bit j: key tid + 256 j is picked (count <= 16 x 256)
     for (uint32_t j = 0, i = tid; i < count; ++j, i += blockDim.x)
       if (val[i] <= kth) mine |= 1u << j;
@@ -784,7 +789,7 @@ __global__ void __launch_bounds__(256, 3) rank_seed_kernel(
     __syncthreads();
     rows = val;
     l2s = rowof;
-    n = full;
+    n = npick;
   }
   const int64_t qn = qnorm[q];
   for_rows_at(
@@ -794,7 +799,8 @@ __global__ void __launch_bounds__(256, 3) rank_seed_kernel(
       },
       [&](uint32_t i) { return xnorm[rows[i]]; });
   __syncthreads();
-  const uint32_t L2 = select(l2s, n, S - 1);
+  // l2 < 255^2 h: below 2^24 (no top digit) for h up to 258
+  const uint32_t L2 = select(l2s, n, S - 1, h * 65025u < (1u << 24) ? 16 : 24, 0);
   if (tid == 0) {
     const int32_t v = static_cast<int32_t>(L2);
     bound[q] = v + (v >> 22) + 1;
