@@ -96,6 +96,21 @@ def test_rotation_matches_reference_arithmetic(torch, d):
         assert np.array_equal(out.cpu().numpy(), oracle.rotate_with(x, r)), nrows
 
 
+@pytest.mark.parametrize("d", [64, 1024])
+def test_rotation_into_an_unaligned_buffer(torch, d):
+    """Rows of 16-dimension multiples are stored four outputs at a time when
+    the destination is 16-byte aligned; an output pointer one float off takes
+    the scalar stores and gives the same bits."""
+    rng = np.random.default_rng(d + 1)
+    x = rng.standard_normal((40, d)).astype(np.float32)
+    r = rng.standard_normal((d, d)).astype(np.float32) / np.float32(np.sqrt(d))
+    xd, rd = torch.from_numpy(x).cuda(), torch.from_numpy(r).cuda()
+    buf = torch.zeros(40 * d + 1, dtype=torch.float32, device="cuda")
+    check(gpu().katoann_gpu_rotate_rows(dptr(xd), 40, d, dptr(rd), buf.data_ptr() + 4, None))
+    got = buf[1:].cpu().numpy().reshape(40, d)
+    assert np.array_equal(got, oracle.rotate_with(x, r)) and buf[0].item() == 0.0
+
+
 def test_rotation_kmajor_layout(torch):
     """katoann_gpu_rotation_kmajor: entry [k][j] = rot[j][k] for k < d & ~15,
     j < d & ~3, rows padded with zeros to a multiple of 32 (both the 16-byte
