@@ -34,9 +34,10 @@ struct ServerOptions {
   float budget_threshold = 0.95f;
   double max_wait_ms = 0;         // a partial batch waits this long for more requests
   // Replay captured CUDA graphs: each slot owns a full batch's device memory
-  // and keeps one captured search per (k, batch size rounded up to a power of
-  // two), captured on first use; a batch's queries are padded to that size
-  // with copies of its first query. Enqueuing a batch is then one graph
+  // and keeps one captured search per (k, padded batch size: the next power
+  // of two up to 16, above that the next multiple of an eighth of the size's
+  // octave), captured on first use; a batch's queries are padded to that
+  // size with its own queries again. Enqueuing a batch is then one graph
   // launch and four copies. Needs an HBM budget of max_in_flight full batches
   // (the default); with less, batches are carved from the pool and launched
   // kernel by kernel.

@@ -192,11 +192,18 @@ struct Server::Impl {
     return L;
   }
 
-  // graph mode: the size a batch of n runs at, the next power of two (at
-  // most max_batch)
+  // graph mode: the size a batch of n runs at. Up to 16, the next power of
+  // two; above, the next multiple of an eighth of n's octave (at most 12.5%
+  // padding); never above max_batch.
   uint32_t padded(uint32_t n) const {
     uint32_t b = 1;
-    while (b < n) b <<= 1;
+    while (b < n && b < 16) b <<= 1;
+    if (n > 16) {
+      uint32_t oct = 16;  // oct < n <= 2 oct
+      while (2 * oct < n) oct <<= 1;
+      const uint32_t step = oct / 8;
+      b = (n + step - 1) / step * step;
+    }
     return std::min(b, max_batch);
   }
 
@@ -257,8 +264,11 @@ struct Server::Impl {
     const uint32_t n = b.n, k = b.k, nb = graphs ? padded(n) : n;
     for (uint32_t i = 0; i < n; ++i)
       std::memcpy(s.hq + size_t(i) * dim, b.reqs[i].q.data(), size_t(dim) * 4);
-    for (uint32_t i = n; i < nb; ++i)  // padding: the first query again
-      std::memcpy(s.hq + size_t(i) * dim, s.hq, size_t(dim) * 4);
+    // padding: the batch's own queries again, in turn, so that no query is
+    // repeated more than once (thousands of copies of one query would crowd
+    // its lists and the candidate records of the CTAs that scan them)
+    for (uint32_t i = n; i < nb; ++i)
+      std::memcpy(s.hq + size_t(i) * dim, s.hq + size_t(i % n) * dim, size_t(dim) * 4);
     const Layout L = layout(pool.at(graphs ? s.base : b.off), nb, k);
     const auto st = reinterpret_cast<katoann_stream_t>(s.stream);
     void *g = nullptr;
@@ -451,10 +461,12 @@ Server::Server(const Index &index, const ServerOptions &opt) : m_(new Impl) {
     for (const uint32_t k : opt.warm_k) {
       if (k == 0 || k > opt.max_k) throw std::invalid_argument("server: warm k must be 1 to max_k");
       for (Slot &s : m.slots)
-        for (uint32_t nb = 1;; nb = std::min(2 * nb, m.max_batch)) {
+        for (uint32_t n = 1, last = 0; n <= m.max_batch; ++n) {
+          const uint32_t nb = m.padded(n);
+          if (nb == last) continue;
+          last = nb;
           std::string err;
           if (!m.graph_for(s, k, nb, &err)) throw std::runtime_error(err);
-          if (nb == m.max_batch) break;
         }
     }
   m.dispatcher = std::thread([&m] { m.dispatch_loop(); });

@@ -50,6 +50,20 @@ def _serve(server, queries, ks, threads=3, seed=0):
     return [server.wait(r) for r in ids]
 
 
+def _padded(n, max_batch):
+    """The batch size the server's graphs run a batch of n at."""
+    b = 1
+    while b < n and b < 16:
+        b <<= 1
+    if n > 16:
+        octave = 16
+        while 2 * octave < n:
+            octave <<= 1
+        step = octave // 8
+        b = -(-n // step) * step
+    return min(b, max_batch)
+
+
 def _check_alone(idx, queries, ks, results, **kw):
     for k in np.unique(ks):
         sel = np.nonzero(ks == k)[0]
@@ -71,12 +85,13 @@ def test_results_in_the_mix_equal_alone(tmp_path, learned):
         model = katoann.ProbeModel.train(idx, train, ladder=(2, 4, 8, 16, 32), depth=32,
                                          label_nprobe=96, survivors=32, epochs=10, batch=256)
     ks = np.random.default_rng(3).choice([10, 100], len(queries))
-    # learned: the graphs of k = 10 captured up front (3 slots x sizes 1 .. 64)
+    # learned: the graphs of k = 10 captured up front (3 slots x the padded
+    # sizes up to 64: 1, 2, 4, 8, 16, 18, 20, .., 32, 36, 40, .., 64)
     server = katoann.Server(idx, max_batch=64, max_in_flight=3, max_k=100, nprobe=32,
                             survivors=32, budget=model, threshold=0.9,
                             warm_k=(10,) if learned else ())
     if learned:
-        assert server.stats()["graphs"] == 3 * 7
+        assert server.stats()["graphs"] == 3 * len({_padded(n, 64) for n in range(1, 65)}) == 3 * 21
     res = _serve(server, queries, ks)
     stats = server.stats()
     assert stats["requests"] == len(queries) and stats["batches"] >= len(queries) / 64
