@@ -364,10 +364,10 @@ def seed_bytes(B: int, rows: int, S: int, head: int) -> float:
 
 # DRAM bytes per 128-row tile of the tensor-core ranking kernel: one ncu
 # capture (dram__bytes_read.sum + dram__bytes_write.sum, one pass) of this
-# 10M x 1024 search at nprobe 72 and 64 survivors moved 2,632.8 + 24.8 MB over
-# 96,108 tiles, about 27.7 KB per tile (1.09 x the 256 head bytes of each
+# 10M x 1024 search at nprobe 72 and 64 survivors moved 2,632.4 + 22.3 MB over
+# 96,108 tiles, about 27.6 KB per tile (1.09 x the 256 head bytes of each
 # probed row). The traffic of a launch scales with its tiles.
-RANK_TC_DRAM_BYTES_PER_TILE = (2632.8e6 + 24.8e6) / 96108
+RANK_TC_DRAM_BYTES_PER_TILE = (2632.4e6 + 22.3e6) / 96108
 
 
 def phase_work(phase: str, B: int, L: int, dc: int, d: int, nprobe: int, S: int, head: int,
