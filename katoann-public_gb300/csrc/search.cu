@@ -503,7 +503,7 @@ __global__ void __launch_bounds__(kThreads) merge_kernel(
 // reference's top-k heap: the first k enter, later ones replace the largest
 // (distance, id) when their distance is strictly smaller (:1113-1124); output
 // ascending by (distance, id), padded (emit_topk, :384-398).
-__global__ void __launch_bounds__(kThreads) refine_kernel(
+__global__ void __launch_bounds__(kThreads, 4) refine_kernel(
     const uint8_t *__restrict__ qhi, const uint8_t *__restrict__ qlo,
     const int64_t *__restrict__ qnorm, const uint8_t *__restrict__ xhi,
     const uint8_t *__restrict__ xlo, const int64_t *__restrict__ xnorm,
@@ -529,47 +529,31 @@ __global__ void __launch_bounds__(kThreads) refine_kernel(
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t nwarps = blockDim.x / 32;
   const int64_t qn = qnorm[q];
-  // two survivors per warp step, every row load issued before the products
-  for (uint32_t s0 = warp; s0 < ns; s0 += 2 * nwarps) {
-    const uint32_t s1 = s0 + nwarps;
-    const bool two = s1 < ns;
+  // one survivor per warp step, its row loads issued before the products (a
+  // smaller register set than two survivors per step: four CTAs per SM)
+  for (uint32_t s0 = warp; s0 < ns; s0 += nwarps) {
     const uint32_t r0 = srow[s0];
-    const uint32_t r1 = two ? srow[s1] : r0;
-    uint32_t id0 = 0, id1 = 0;
-    int64_t xn0 = 0, xn1 = 0;
+    uint32_t id0 = 0;
+    int64_t xn0 = 0;
     if (lane == 0) {
       id0 = ids[r0];
       xn0 = xnorm[r0];
-      id1 = ids[r1];
-      xn1 = xnorm[r1];
     }
     const uint4 *h0 = reinterpret_cast<const uint4 *>(xhi + static_cast<size_t>(r0) * dc);
     const uint4 *l0 = reinterpret_cast<const uint4 *>(xlo + static_cast<size_t>(r0) * dc);
-    const uint4 *h1 = reinterpret_cast<const uint4 *>(xhi + static_cast<size_t>(r1) * dc);
-    const uint4 *l1 = reinterpret_cast<const uint4 *>(xlo + static_cast<size_t>(r1) * dc);
-    uint32_t hh0 = 0, mx0 = 0, ll0 = 0, hh1 = 0, mx1 = 0, ll1 = 0;
+    uint32_t hh0 = 0, mx0 = 0, ll0 = 0;
 #pragma unroll 2
     for (uint32_t u = lane; u < n16; u += 32) {
       const uint4 bh0 = h0[u], bl0 = l0[u];
-      uint4 bh1 = make_uint4(0, 0, 0, 0), bl1 = bh1;
-      if (two) {
-        bh1 = h1[u];
-        bl1 = l1[u];
-      }
       const uint4 ah = sq[u], al = sq[n16 + u];
       const uint32_t a_h[4] = {ah.x, ah.y, ah.z, ah.w}, a_l[4] = {al.x, al.y, al.z, al.w};
       const uint32_t b_h0[4] = {bh0.x, bh0.y, bh0.z, bh0.w}, b_l0[4] = {bl0.x, bl0.y, bl0.z, bl0.w};
-      const uint32_t b_h1[4] = {bh1.x, bh1.y, bh1.z, bh1.w}, b_l1[4] = {bl1.x, bl1.y, bl1.z, bl1.w};
 #pragma unroll
       for (int w = 0; w < 4; ++w) {
         hh0 = dp4(a_h[w], b_h0[w], hh0);
         mx0 = dp4(a_h[w], b_l0[w], mx0);
         mx0 = dp4(a_l[w], b_h0[w], mx0);
         ll0 = dp4(a_l[w], b_l0[w], ll0);
-        hh1 = dp4(a_h[w], b_h1[w], hh1);
-        mx1 = dp4(a_h[w], b_l1[w], mx1);
-        mx1 = dp4(a_l[w], b_h1[w], mx1);
-        ll1 = dp4(a_l[w], b_l1[w], ll1);
       }
     }
 #pragma unroll
@@ -577,21 +561,12 @@ __global__ void __launch_bounds__(kThreads) refine_kernel(
       hh0 += __shfl_xor_sync(0xffffffffu, hh0, o);
       mx0 += __shfl_xor_sync(0xffffffffu, mx0, o);
       ll0 += __shfl_xor_sync(0xffffffffu, ll0, o);
-      hh1 += __shfl_xor_sync(0xffffffffu, hh1, o);
-      mx1 += __shfl_xor_sync(0xffffffffu, mx1, o);
-      ll1 += __shfl_xor_sync(0xffffffffu, ll1, o);
     }
     if (lane == 0) {
       const int64_t dot0 = static_cast<int64_t>((static_cast<uint64_t>(hh0) << 16) +
                                                 (static_cast<uint64_t>(mx0) << 8) + ll0);
       ex[s0] = dist_value(qn + xn0 - 2 * dot0, scale);
       eid[s0] = id0;
-      if (two) {
-        const int64_t dot1 = static_cast<int64_t>((static_cast<uint64_t>(hh1) << 16) +
-                                                  (static_cast<uint64_t>(mx1) << 8) + ll1);
-        ex[s1] = dist_value(qn + xn1 - 2 * dot1, scale);
-        eid[s1] = id1;
-      }
     }
   }
   __syncthreads();
