@@ -187,6 +187,12 @@ void katoann_gpu_timer_destroy(void *timer);
 /* Sums the phase durations (ms) of all passes recorded since the last read
  * into h_ms[0..KATO_PHASES) and their count into *passes; synchronous. */
 int katoann_gpu_timer_read(void *timer, float *h_ms, uint32_t *passes);
+/* The timer also brackets single kernels with events: 0 the query rotation
+ * (its transposes and rotate_lanes_kernel), 1 coarse_tc_kernel, 2
+ * rank_tc_kernel. Their summed ms and launch counts over the passes of the
+ * last katoann_gpu_timer_read (a kernel a pass did not run is not counted). */
+#define KATO_TIMED_KERNELS 3
+void katoann_gpu_timer_kernels(void *timer, float *h_ms, uint32_t *h_launches);
 
 /* Tensor-core form of a plane pair: d_hi16 / d_lo16 = (byte - 128) as fp16
  * bits, rows x dc each, and d_term[r] = norm[r] - 256 (65792 s_h + 257 s_l)

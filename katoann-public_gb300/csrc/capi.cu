@@ -116,6 +116,7 @@ extern std::atomic<uint32_t> g_candidate_cap;
 extern std::atomic<uint32_t> g_seed_rows;
 void timer_destroy(void *t);
 int timer_read(void *t, float *ms, uint32_t *passes);
+void timer_kernels(void *t, float *ms, uint32_t *launches);
 size_t search_workspace(const katoann_gpu_index *ix, uint32_t max_batch, uint32_t k, uint32_t p,
                         int ranking, uint32_t survivors);
 
@@ -370,6 +371,10 @@ int katoann_gpu_set_candidate_cap(uint32_t cap) {
 }
 
 void katoann_gpu_timer_destroy(void *timer) { kato::timer_destroy(timer); }
+
+void katoann_gpu_timer_kernels(void *timer, float *h_ms, uint32_t *h_launches) {
+  kato::timer_kernels(timer, h_ms, h_launches);
+}
 
 int katoann_gpu_timer_read(void *timer, float *h_ms, uint32_t *passes) {
   if (!timer) return kato::invalid("null timer");

@@ -688,14 +688,28 @@ int select_topp_ex(const float *dists, uint32_t nq, uint32_t n, uint32_t p, uint
                    uint32_t *probed, unsigned long long *tie_count, const uint32_t *only,
                    uint32_t only_above, cudaStream_t st);
 
+// Per pass: the KATO_PHASES + 1 phase boundaries, then a start and an end
+// event around each timed kernel (KATO_TIMED_KERNELS: the query rotation,
+// coarse_tc_kernel, rank_tc_kernel).
+constexpr uint32_t kTimerStride = KATO_PHASES + 1 + 2 * KATO_TIMED_KERNELS;
+
 struct PhaseTimer {
-  std::vector<cudaEvent_t> ev;  // (KATO_PHASES + 1) per pass
+  std::vector<cudaEvent_t> ev;  // kTimerStride per pass
+  std::vector<uint8_t> kdone;   // per pass: the kernels whose two events were recorded
   uint32_t max_passes = 0, used = 0;
+  float kms[KATO_TIMED_KERNELS] = {};      // of the passes the last read summed
+  uint32_t kn[KATO_TIMED_KERNELS] = {};
 };
 
 static void mark(PhaseTimer *t, uint32_t phase, cudaStream_t st) {
   if (!t || t->used >= t->max_passes) return;
-  cudaEventRecord(t->ev[t->used * (KATO_PHASES + 1) + phase], st);
+  cudaEventRecord(t->ev[t->used * kTimerStride + phase], st);
+}
+
+static void kmark(PhaseTimer *t, uint32_t kernel, bool end, cudaStream_t st) {
+  if (!t || t->used >= t->max_passes) return;
+  cudaEventRecord(t->ev[t->used * kTimerStride + KATO_PHASES + 1 + 2 * kernel + end], st);
+  if (end) t->kdone[t->used] |= static_cast<uint8_t>(1u << kernel);
 }
 
 struct Plan {
@@ -830,9 +844,11 @@ int coarse_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
   // 1. rotation and quantization of the queries (src/index.cpp:895-899, :917-943)
   const float *src = queries;
   if (ix->rotated) {
+    kmark(tm, 0, false, st);
     if ((rc = rotate_rows_kmajor(queries, nq, ix->dim, ix->d_rotation, ix->d_rotation_t,
                                  ws + pl.off_rot, fq, st)))
       return rc;
+    kmark(tm, 0, true, st);
     src = fq;
   }
   if ((rc = quantize_rows(src, nq, ix->dim, dc, ix->lo, ix->inv_step, ix->head_dims, qhi, qlo, qn,
@@ -853,11 +869,13 @@ int coarse_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
     __half *ql16 = reinterpret_cast<__half *>(ws + pl.off_ql16);
     int64_t *qterm = reinterpret_cast<int64_t *>(ws + pl.off_qterm);
     if ((rc = centre_planes(qhi, qlo, qn, nq, dc, qh16, ql16, qterm, st))) return rc;
+    kmark(tm, 1, false, st);
     if ((rc = coarse_tc(reinterpret_cast<const __half *>(ix->d_chi16),
                         reinterpret_cast<const __half *>(ix->d_clo16), ix->d_cterm, L, qh16, ql16,
                         qterm, nq, dc, ix->step_sq, cd, reinterpret_cast<uint32_t *>(stats + 3),
                         stats + 32, st)))
       return rc;
+    kmark(tm, 1, true, st);
     ++g_launches;
   } else if ((rc = sq16_tiles(qhi, qlo, ix->d_chi, ix->d_clo, qn, ix->d_cnorm, ix->step_sq, nq, L,
                               dc, dc, dc, cd, true, st))) {
@@ -984,7 +1002,9 @@ int search_pass(const katoann_gpu_index *ix, const Plan &pl, const float *querie
     T.nprobe = p;
     T.wait = g_tc_wait.load() ? static_cast<long long>(g_tc_wait.load()) : 4000000000ll;
     T.scale = scale;
+    kmark(tm, 2, false, st);
     if ((rc = rank_tc(T, ix->d_hi, ix->npts, pl.tcs, st))) return rc;
+    kmark(tm, 2, true, st);
     if ((rc = rank_tc_bucket(rec, rec_n, pl.rec_cap, pl.ctas, qfill, slots, pl.cap, scale, st)))
       return rc;
     const RescanBufs rb{reinterpret_cast<uint32_t *>(ws + pl.off_rlist),
@@ -1268,7 +1288,8 @@ void graph_destroy(void *h) {
 void *timer_create(uint32_t max_passes) {
   auto *t = new PhaseTimer();
   t->max_passes = max_passes;
-  t->ev.resize(static_cast<size_t>(max_passes) * (KATO_PHASES + 1));
+  t->ev.resize(static_cast<size_t>(max_passes) * kTimerStride);
+  t->kdone.assign(max_passes, 0);
   for (auto &e : t->ev)
     if (cudaEventCreate(&e) != cudaSuccess) {
       delete t;
@@ -1288,16 +1309,37 @@ int timer_read(void *p, float *ms, uint32_t *passes) {
   auto *t = static_cast<PhaseTimer *>(p);
   for (int i = 0; i < KATO_PHASES; ++i) ms[i] = 0.0f;
   *passes = t->used;
+  for (int k = 0; k < KATO_TIMED_KERNELS; ++k) t->kms[k] = 0.0f, t->kn[k] = 0;
   if (t->used == 0) return KATO_OK;
-  KATO_CUDA(cudaEventSynchronize(t->ev[t->used * (KATO_PHASES + 1) - 1]));
-  for (uint32_t u = 0; u < t->used; ++u)
+  // the last phase event of the last pass follows every other event in it
+  KATO_CUDA(cudaEventSynchronize(t->ev[(t->used - 1) * kTimerStride + KATO_PHASES]));
+  for (uint32_t u = 0; u < t->used; ++u) {
+    const cudaEvent_t *e = t->ev.data() + static_cast<size_t>(u) * kTimerStride;
     for (int i = 0; i < KATO_PHASES; ++i) {
       float x = 0;
-      const cudaEvent_t a = t->ev[u * (KATO_PHASES + 1) + i], b = t->ev[u * (KATO_PHASES + 1) + i + 1];
-      if (cudaEventElapsedTime(&x, a, b) == cudaSuccess) ms[i] += x;
+      if (cudaEventElapsedTime(&x, e[i], e[i + 1]) == cudaSuccess) ms[i] += x;
     }
+    for (int k = 0; k < KATO_TIMED_KERNELS; ++k) {
+      float x = 0;
+      if ((t->kdone[u] >> k & 1u) &&
+          cudaEventElapsedTime(&x, e[KATO_PHASES + 1 + 2 * k], e[KATO_PHASES + 2 + 2 * k]) ==
+              cudaSuccess) {
+        t->kms[k] += x;
+        ++t->kn[k];
+      }
+    }
+    t->kdone[u] = 0;
+  }
   t->used = 0;
   return KATO_OK;
+}
+
+void timer_kernels(void *p, float *ms, uint32_t *launches) {
+  const auto *t = static_cast<const PhaseTimer *>(p);
+  for (int k = 0; k < KATO_TIMED_KERNELS; ++k) {
+    ms[k] = t->kms[k];
+    launches[k] = t->kn[k];
+  }
 }
 
 size_t search_workspace(const katoann_gpu_index *ix, uint32_t max_batch, uint32_t k, uint32_t p,

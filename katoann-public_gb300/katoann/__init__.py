@@ -36,6 +36,8 @@ def _load():
     gpu.katoann_gpu_timer_create.restype = C.c_void_p
     gpu.katoann_gpu_timer_destroy.argtypes = [C.c_void_p]
     gpu.katoann_gpu_timer_read.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    gpu.katoann_gpu_timer_kernels.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    gpu.katoann_gpu_timer_kernels.restype = None
     gpu.katoann_gpu_last_error.restype = C.c_char_p
     gpu.katoann_gpu_copy_to_host.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
     gpu.katoann_gpu_set_wait_limit.argtypes = [C.c_uint64]
@@ -190,6 +192,7 @@ def dist_value(l2: int, step_sq: float) -> float:
 
 PHASES = ("rotate+quantize", "coarse product", "coarse select", "probe budget", "inversion",
           "seed bounds", "ranking pass", "survivor merge", "refine")
+TIMED_KERNELS = ("rotation", "coarse_tc_kernel", "rank_tc_kernel")  # the phase timer's kernel events
 
 
 class PhaseTimer:
@@ -208,6 +211,14 @@ class PhaseTimer:
         if rc:
             raise RuntimeError(_lib.gpu.katoann_gpu_last_error().decode())
         return dict(zip(PHASES, map(float, ms))), int(n[0])
+
+    def kernels(self) -> dict:
+        """Summed ms and launch count of the single kernels the timer
+        brackets, over the passes of the last read()."""
+        ms = np.zeros(len(TIMED_KERNELS), np.float32)
+        n = np.zeros(len(TIMED_KERNELS), np.uint32)
+        _lib.gpu.katoann_gpu_timer_kernels(C.c_void_p(self.handle), _ptr(ms), _ptr(n))
+        return {k: (float(a), int(b)) for k, a, b in zip(TIMED_KERNELS, ms, n)}
 
     def __del__(self):
         h = getattr(self, "handle", None)

@@ -90,3 +90,27 @@ def test_graph_search_refuses_a_timer(small):
     st = torch.cuda.Stream()
     with pytest.raises(ValueError, match="phase events"):
         idx.search_device(q, ids, dists, nprobe=4, stream=st.cuda_stream, timer=timer, graph=True)
+
+
+def test_phase_timer_brackets_the_top_kernels(small):
+    """Two timed searches: every phase and each of the three bracketed kernels
+    is counted once per pass, and a kernel takes no longer than its phase."""
+    torch = pytest.importorskip("torch")
+    import katoann
+    _, queries, idx = small
+    q = torch.from_numpy(queries).cuda()
+    ids = torch.empty((len(queries), 10), dtype=torch.int32, device="cuda")
+    dists = torch.empty((len(queries), 10), dtype=torch.float32, device="cuda")
+    timer = katoann.PhaseTimer(4)
+    st = torch.cuda.Stream()
+    for _ in range(2):
+        idx.search_device(q, ids, dists, nprobe=4, survivors=32, stream=st.cuda_stream, timer=timer)
+    phases, passes = timer.read()
+    kern = timer.kernels()
+    assert passes == 2 and set(kern) == set(katoann.TIMED_KERNELS)
+    for name, phase in (("rotation", "rotate+quantize"), ("coarse_tc_kernel", "coarse product"),
+                        ("rank_tc_kernel", "ranking pass")):
+        ms, n = kern[name]
+        assert n == 2 and 0 < ms <= phases[phase] + 1e-3, (name, kern, phases)
+    # a read with no passes since clears the kernel sums too
+    assert timer.read()[1] == 0 and all(n == 0 for _, n in timer.kernels().values())
