@@ -1091,9 +1091,11 @@ __global__ void __launch_bounds__(512) tc_bucket_kernel(const uint4 *__restrict_
                                                         uint32_t rec_cap, uint32_t *__restrict__ qfill,
                                                         uint2 *__restrict__ qbuf, uint32_t cap,
                                                         DistScale scale) {
+  // gridDim.y CTAs share each ranking CTA's list, so that enough records
+  // (each a global atomic and a scattered store) are in flight per SM
   const uint4 *r = rec + static_cast<size_t>(blockIdx.x) * rec_cap;
   const uint32_t n = rec_n[blockIdx.x];
-  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+  for (uint32_t i = blockIdx.y * blockDim.x + threadIdx.x; i < n; i += gridDim.y * blockDim.x) {
     const uint4 e = r[i];
     const uint32_t at = atomicAdd(qfill + e.x, 1u);
     if (at < cap)
@@ -1172,7 +1174,7 @@ int rank_tc(const RankTcArgs &A, const uint8_t *xhi, uint32_t npts, const TcShap
 
 int rank_tc_bucket(const uint4 *rec, const uint32_t *rec_n, uint32_t rec_cap, uint32_t ctas,
                    uint32_t *qfill, uint2 *qbuf, uint32_t cap, DistScale scale, cudaStream_t st) {
-  tc_bucket_kernel<<<ctas, 512, 0, st>>>(rec, rec_n, rec_cap, qfill, qbuf, cap, scale);
+  tc_bucket_kernel<<<dim3(ctas, 4), 512, 0, st>>>(rec, rec_n, rec_cap, qfill, qbuf, cap, scale);
   KATO_LAUNCHED("tc_bucket_kernel");
   return KATO_OK;
 }
