@@ -273,6 +273,7 @@ __global__ void quantize_rows_kernel(const float *__restrict__ x, uint32_t nrows
   const uint32_t lane = threadIdx.x & 31;
   const uint64_t warp = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
+  const QuantScale qs = quant_scale(lo, inv_step);
   for (uint64_t row = warp; row < nrows; row += nwarps) {
     const float *xr = x + row * d;
     uint8_t *hr = hi + row * dc;
@@ -280,7 +281,7 @@ __global__ void quantize_rows_kernel(const float *__restrict__ x, uint32_t nrows
     uint64_t s = 0, sh = 0, s0 = 0;
     for (uint32_t k = lane; k < dc; k += 32) {
       uint32_t v = 0;
-      if (k < d) v = quantize1(xr[k], lo, inv_step);
+      if (k < d) v = quantize1(xr[k], qs);
       const uint32_t vh = v >> 8;
       hr[k] = static_cast<uint8_t>(vh);
       lr[k] = static_cast<uint8_t>(v & 0xFFu);

@@ -96,6 +96,55 @@ def test_rotation_matches_reference_arithmetic(torch, d):
         assert np.array_equal(out.cpu().numpy(), oracle.rotate_with(x, r)), nrows
 
 
+def _lround_clamped(x, lo, inv_step):
+    """The reference's code of a value: (double(x) - lo) * inv_step in double,
+    rounded half away from zero, clamped to [0, 65535]."""
+    t = (x.astype(np.float64) - np.float64(lo)) * np.float64(inv_step)
+    f = np.floor(t)
+    return np.clip(f + (t - f >= 0.5), 0, 65535).astype(np.int64)
+
+
+@pytest.mark.parametrize("lo,inv_step", [(-0.3712, 65535.0 / 0.8093),  # a generic index scale
+                                         (0.0, 4096.0),                # exact halves: the double path
+                                         (-1.0, 32767.5)])
+def test_quantization_at_rounding_ties(torch, lo, inv_step):
+    """The single-precision quantizer against the reference's double arithmetic
+    at and around half-integers (the float neighbours of each tie), at integers,
+    at the clamps and on random values."""
+    lo = float(np.float32(lo))
+    rng = np.random.default_rng(11)
+    k = np.concatenate([np.arange(0, 40), rng.integers(0, 65535, 3000), np.arange(65495, 65536)])
+    ties = (np.float64(lo) + (k + 0.5) / inv_step).astype(np.float32)
+    near = [ties]
+    for step in (1, 2, 3):
+        near.append(np.nextafter(near[-1], np.float32(np.inf)))
+    down = [ties]
+    for step in (1, 2, 3):
+        down.append(np.nextafter(down[-1], np.float32(-np.inf)))
+    ints = (np.float64(lo) + k / inv_step).astype(np.float32)
+    span = 65535.0 / inv_step
+    rand = rng.uniform(lo - 0.2 * span, lo + 1.2 * span, 20000).astype(np.float32)
+    edge = np.array([lo, np.nextafter(np.float32(lo), np.float32(-1)), lo + span, -1e30, 1e30, 0.0],
+                    np.float32)
+    x = np.concatenate(near + down[1:] + [ints, rand, edge])
+    d = 64
+    x = np.concatenate([x, np.zeros((-len(x)) % d, np.float32)]).reshape(-1, d)
+    n = x.shape[0]
+    xd = torch.from_numpy(x).cuda()
+    hi = torch.zeros((n, d), dtype=torch.uint8, device="cuda")
+    lp = torch.zeros((n, d), dtype=torch.uint8, device="cuda")
+    nrm = torch.zeros(n, dtype=torch.int64, device="cuda")
+    hn = torch.zeros(n, dtype=torch.int64, device="cuda")
+    check(gpu().katoann_gpu_quantize_rows(dptr(xd), n, d, d, lo, inv_step, 0, dptr(hi), dptr(lp),
+                                          dptr(nrm), dptr(hn), None, None))
+    got = hi.cpu().numpy().astype(np.int64) * 256 + lp.cpu().numpy()
+    want = _lround_clamped(x, lo, inv_step)
+    bad = np.argwhere(got != want)
+    assert len(bad) == 0, (len(bad), [(x[i, j], got[i, j], want[i, j]) for i, j in bad[:5]])
+    assert np.array_equal(nrm.cpu().numpy(), (want * want).sum(1))
+    assert np.array_equal(hn.cpu().numpy(), ((want >> 8) ** 2).sum(1))
+
+
 @pytest.mark.parametrize("d", [64, 1024])
 def test_rotation_into_an_unaligned_buffer(torch, d):
     """Rows of 16-dimension multiples are stored four outputs at a time when
