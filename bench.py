@@ -646,21 +646,27 @@ def main():
     ih = torch.empty((B, k), dtype=torch.int32).pin_memory()
     dh = torch.empty((B, k), dtype=torch.float32).pin_memory()
 
-    def host_search():
+    def host_search(graph):
         idx.search_into(qh.data_ptr(), B, ih.data_ptr(), dh.data_ptr(), k=k, nprobe=cfg["nprobe"],
-                        survivors=S, budget=cfg.get("model"), threshold=cfg.get("threshold", 0.95))
+                        survivors=S, budget=cfg.get("model"), threshold=cfg.get("threshold", 0.95),
+                        graph=graph)
 
-    for _ in range(3):
-        host_search()
+    # end to end through the host API, each step copying its queries in and
+    # its results out: with the kernels replayed as a captured graph (the
+    # line's e2e), and launched one by one (e2e_launches)
     e2e_steps = max(10, min(args.steps, 100))
-    if dist:
-        dist.barrier()
-    t2 = time.perf_counter()
-    for _ in range(e2e_steps):
-        host_search()
-    e2e_s = max_over_ranks(dist, time.perf_counter() - t2)
-    e2e_qps = world * B * e2e_steps / e2e_s
-    e2e_recall = recall(ih.numpy().view(np.uint32), gt, k)
+    e2e_runs = {}
+    for graph in (False, True):
+        for _ in range(3):
+            host_search(graph)
+        if dist:
+            dist.barrier()
+        t2 = time.perf_counter()
+        for _ in range(e2e_steps):
+            host_search(graph)
+        e2e_s = max_over_ranks(dist, time.perf_counter() - t2)
+        e2e_runs[graph] = (world * B * e2e_steps / e2e_s, recall(ih.numpy().view(np.uint32), gt, k))
+    e2e_qps, e2e_recall = e2e_runs[True]
 
     # ---- the index build on the device: the same base vectors partitioned by
     # the library (katoann.build_partition: k-means++ and Lloyd on a training
@@ -780,7 +786,9 @@ def main():
                          "api": "katoann.Index.search_device(graph=True)"},
         "e2e": {"value": round(e2e_qps, 1), "unit": "queries/s", "recall": round(e2e_recall, 5),
                 "h2d_bytes_per_step": B * d * 4, "d2h_bytes_per_step": B * k * 8,
-                "api": "katoann.Index.search_into (pinned host buffers)"},
+                "api": "katoann.Index.search_into(graph=True) (pinned host buffers)",
+                "launched_one_by_one": {"value": round(e2e_runs[False][0], 1),
+                                        "recall": round(e2e_runs[False][1], 5)}},
         "gpu_launches": launches_per_search * args.steps,
         "clocks": clk,
         "cpu_baseline": cpu,

@@ -84,9 +84,11 @@ struct SearchParams {
   float budget_threshold = 0.95f;
   const uint32_t *nprobe_per_query = nullptr;
   uint32_t *nprobe_used = nullptr;
-  // search_device only: run the call as a CUDA graph, captured the first time
-  // these pointers and parameters are seen (the index keeps the last 16) and
-  // replayed in one launch after that.
+  // Run the search's kernels as a CUDA graph, captured the first time these
+  // pointers and parameters are seen (the index keeps the last 16) and
+  // replayed in one launch after that. search_device captures the whole
+  // call; search captures each pass on the index's own device buffers and
+  // keeps the copies of the queries and results outside the graph.
   bool graph = false;
 };
 

@@ -80,11 +80,12 @@ int katoann_index_search_device(void *index, const float *d_queries, uint32_t nq
 /* Index.search with a per-query nprobe (SearchParams::budget /
  * nprobe_per_query / nprobe_used; no counterpart in the reference): model is
  * a katoann_probe_* handle or NULL, nprobe_in (nq values, capped at nprobe)
- * or NULL, nprobe_out (nq values) or NULL. */
+ * or NULL, nprobe_out (nq values) or NULL; graph != 0 replays each pass's
+ * kernels as a captured CUDA graph (SearchParams::graph). */
 int katoann_index_search_budget(void *index, const float *queries, uint32_t nq, uint32_t k,
                                 uint32_t nprobe, int ranking, uint32_t survivors, int selection,
                                 const void *model, float threshold, const uint32_t *nprobe_in,
-                                uint32_t *nprobe_out, uint32_t *ids, float *dists);
+                                uint32_t *nprobe_out, uint32_t *ids, float *dists, int graph);
 
 /* katoann_index_search_device with the per-query nprobe of
  * katoann_index_search_budget (d_nprobe_in / d_nprobe_out: device memory);

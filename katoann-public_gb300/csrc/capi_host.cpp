@@ -320,13 +320,14 @@ int katoann_server_stats(void *server, uint64_t *stats) {
 int katoann_index_search_budget(void *index, const float *queries, uint32_t nq, uint32_t k,
                                 uint32_t nprobe, int ranking, uint32_t survivors, int selection,
                                 const void *model, float threshold, const uint32_t *nprobe_in,
-                                uint32_t *nprobe_out, uint32_t *ids, float *dists) {
+                                uint32_t *nprobe_out, uint32_t *ids, float *dists, int graph) {
   return guarded([&] {
     katoann::SearchParams p = params(k, nprobe, ranking, survivors, selection);
     p.budget = M(model);
     p.budget_threshold = threshold;
     p.nprobe_per_query = nprobe_in;
     p.nprobe_used = nprobe_out;
+    p.graph = graph != 0;
     I(index)->search(queries, nq, p, ids, dists);
   });
 }

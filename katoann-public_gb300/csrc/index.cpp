@@ -98,6 +98,38 @@ struct Index::State {
     for (auto &g : graphs) katoann_gpu_graph_destroy(g.handle);
     graphs.clear();
   }
+  // The captured search of these device buffers and parameters (every
+  // pointer and size the capture bakes in; model: the device probe model or
+  // null), captured now if it is not yet. At most 16 are kept, the least
+  // recently used dropped first. The caller holds mu.
+  void *graph_of(const float *d_queries, uint32_t nq, const SearchParams &p, int rk,
+                 const katoann_gpu_probe_model *model, uint32_t *d_ids, float *d_dists,
+                 const uint32_t *d_npin, uint32_t *d_npout, cudaStream_t st) const {
+    const std::vector<uint64_t> key = {
+        reinterpret_cast<uint64_t>(d_queries), nq, reinterpret_cast<uint64_t>(d_ids),
+        reinterpret_cast<uint64_t>(d_dists), p.k, p.nprobe, static_cast<uint64_t>(rk),
+        p.survivors, reinterpret_cast<uint64_t>(d_npin), reinterpret_cast<uint64_t>(d_npout),
+        model ? reinterpret_cast<uint64_t>(model->d_w1) : 0,
+        model ? (uint64_t(model->nclass) << 32 | model->depth) : 0,
+        model ? static_cast<uint64_t>(std::llround(double(p.budget_threshold) * 1e9)) : 0,
+        reinterpret_cast<uint64_t>(st), reinterpret_cast<uint64_t>(ws.p), ws.n};
+    for (size_t i = 0; i < graphs.size(); ++i)
+      if (graphs[i].key == key) {
+        void *h = graphs[i].handle;
+        std::rotate(graphs.begin() + i, graphs.begin() + i + 1, graphs.end());
+        return h;
+      }
+    void *h = nullptr;
+    gpu_check(katoann_gpu_search_capture(&view, d_queries, nq, p.k, p.nprobe, rk, p.survivors,
+                                         max_batch, d_npin, model, ws.p, ws.n, d_ids, d_dists,
+                                         d_npout, reinterpret_cast<katoann_stream_t>(st), &h));
+    if (graphs.size() >= 16) {
+      katoann_gpu_graph_destroy(graphs.front().handle);
+      graphs.erase(graphs.begin());
+    }
+    graphs.push_back({key, h});
+    return h;
+  }
   mutable void *last_stream = nullptr;
   // per device pass of a host search: the pass's count of CTAs whose bounded
   // pipeline wait ran out (workspace statistic 3), copied back with the results
@@ -630,6 +662,7 @@ BudgetPlan budget_plan(const SearchParams &p, uint32_t nlist) {
 
 }  // namespace
 
+
 void Index::search(const float *queries, uint32_t nq, const SearchParams &p, uint32_t *ids,
                    float *dists) const {
   if (nq == 0) return;
@@ -641,7 +674,11 @@ void Index::search(const float *queries, uint32_t nq, const SearchParams &p, uin
   const int rk = ranking_code(p.ranking);
   const size_t need = katoann_gpu_search_workspace(&s.view, b, p.k, bp.depth, rk, p.survivors);
   if (need == 0) gpu_check(KATO_EINVAL);
-  s.ws.ensure(need);
+  if (need > s.ws.n) {
+    cuda_check(cudaStreamSynchronize(s.stream), "workspace resize");
+    s.drop_graphs();  // they hold the old workspace
+    s.ws.ensure(need);
+  }
   s.dq.ensure(static_cast<size_t>(b) * s.dim * 4);
   s.dids.ensure(static_cast<size_t>(b) * p.k * 4);
   s.ddists.ensure(static_cast<size_t>(b) * p.k * 4);
@@ -656,7 +693,23 @@ void Index::search(const float *queries, uint32_t nq, const SearchParams &p, uin
     cuda_check(cudaMemcpyAsync(s.dq.p, queries + static_cast<size_t>(q0) * s.dim,
                                static_cast<size_t>(nb) * s.dim * 4, cudaMemcpyHostToDevice, s.stream),
                "copy queries");
-    if (bp.active || p.nprobe_used) {
+    if (p.graph) {
+      // the kernels as one captured graph of the index's own buffers; the
+      // copies in and out stay outside it
+      if (p.nprobe_per_query)
+        cuda_check(cudaMemcpyAsync(s.dnp_in.p, p.nprobe_per_query + q0, static_cast<size_t>(nb) * 4,
+                                   cudaMemcpyHostToDevice, s.stream),
+                   "copy budgets");
+      void *h = s.graph_of(s.dq.as<float>(), nb, p, rk, bp.use_model ? &bp.model : nullptr,
+                           s.dids.as<uint32_t>(), s.ddists.as<float>(),
+                           p.nprobe_per_query ? s.dnp_in.as<uint32_t>() : nullptr,
+                           p.nprobe_used ? s.dnp_out.as<uint32_t>() : nullptr, s.stream);
+      gpu_check(katoann_gpu_graph_launch(h, reinterpret_cast<katoann_stream_t>(s.stream)));
+      if (p.nprobe_used)
+        cuda_check(cudaMemcpyAsync(p.nprobe_used + q0, s.dnp_out.p, static_cast<size_t>(nb) * 4,
+                                   cudaMemcpyDeviceToHost, s.stream),
+                   "copy budgets");
+    } else if (bp.active || p.nprobe_used) {
       if (p.nprobe_per_query)
         cuda_check(cudaMemcpyAsync(s.dnp_in.p, p.nprobe_per_query + q0, static_cast<size_t>(nb) * 4,
                                    cudaMemcpyHostToDevice, s.stream),
@@ -716,34 +769,8 @@ void Index::search_device(const float *d_queries, uint32_t nq, const SearchParam
     cuda_check(cudaStreamWaitEvent(st, s.done, 0), "cudaStreamWaitEvent");
   if (p.graph) {
     if (timer) throw std::invalid_argument("a graph search records no phase events");
-    // the call's identity: every pointer and size it captures
-    const std::vector<uint64_t> key = {
-        reinterpret_cast<uint64_t>(d_queries), nq, reinterpret_cast<uint64_t>(d_ids),
-        reinterpret_cast<uint64_t>(d_dists), p.k, p.nprobe, static_cast<uint64_t>(rk),
-        p.survivors, reinterpret_cast<uint64_t>(p.nprobe_per_query),
-        reinterpret_cast<uint64_t>(p.nprobe_used),
-        bp.use_model ? reinterpret_cast<uint64_t>(bp.model.d_w1) : 0,
-        bp.use_model ? (uint64_t(bp.model.nclass) << 32 | bp.model.depth) : 0,
-        bp.use_model ? static_cast<uint64_t>(std::llround(double(p.budget_threshold) * 1e9)) : 0,
-        reinterpret_cast<uint64_t>(st), reinterpret_cast<uint64_t>(s.ws.p)};
-    void *h = nullptr;
-    for (size_t i = 0; i < s.graphs.size(); ++i)
-      if (s.graphs[i].key == key) {
-        h = s.graphs[i].handle;
-        std::rotate(s.graphs.begin() + i, s.graphs.begin() + i + 1, s.graphs.end());
-        break;
-      }
-    if (!h) {
-      gpu_check(katoann_gpu_search_capture(
-          &s.view, d_queries, nq, p.k, p.nprobe, rk, p.survivors, s.max_batch,
-          p.nprobe_per_query, bp.use_model ? &bp.model : nullptr, s.ws.p, s.ws.n, d_ids, d_dists,
-          p.nprobe_used, reinterpret_cast<katoann_stream_t>(st), &h));
-      if (s.graphs.size() >= 16) {
-        katoann_gpu_graph_destroy(s.graphs.front().handle);
-        s.graphs.erase(s.graphs.begin());
-      }
-      s.graphs.push_back({key, h});
-    }
+    void *h = s.graph_of(d_queries, nq, p, rk, bp.use_model ? &bp.model : nullptr, d_ids, d_dists,
+                         p.nprobe_per_query, p.nprobe_used, st);
     gpu_check(katoann_gpu_graph_launch(h, reinterpret_cast<katoann_stream_t>(st)));
   } else if (bp.active || p.nprobe_used)
     gpu_check(katoann_gpu_search_budget(&s.view, d_queries, nq, p.k, p.nprobe, rk, p.survivors,

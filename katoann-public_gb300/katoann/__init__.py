@@ -70,7 +70,8 @@ def _load():
     lib.katoann_dist_value.argtypes = [C.c_int64, D]
     lib.katoann_dist_value.restype = C.c_float
     F = C.c_float
-    lib.katoann_index_search_budget.argtypes = [P, P, U32, U32, U32, I32, U32, I32, P, F, P, P, P, P]
+    lib.katoann_index_search_budget.argtypes = [P, P, U32, U32, U32, I32, U32, I32, P, F, P, P, P, P,
+                                                I32]
     lib.katoann_index_search_device_budget.argtypes = [P, P, U32, U32, U32, I32, U32, I32, P, F, P,
                                                        P, P, P, P, P, I32]
     lib.katoann_probe_train.argtypes = [P, P, U32, P, U32, U32, U32, U32, I32, U32, I32, U32, U32,
@@ -316,10 +317,12 @@ class Index:
 
     def search(self, queries, k: int = 10, nprobe: int = 64, ranking: str = "prefix",
                survivors: int = 32, selection: str = "threshold", budget: "ProbeModel | None" = None,
-               threshold: float = 0.95, nprobe_per_query=None, return_nprobe: bool = False):
+               threshold: float = 0.95, nprobe_per_query=None, return_nprobe: bool = False,
+               graph: bool = False):
         """Search all queries together; returns (ids uint32 [nq, k], squared
         L2 distances float32 [nq, k]), nearest first. Queries are normalized
-        when the index was built with normalized=True.
+        when the index was built with normalized=True. graph=True replays the
+        kernels of each pass as a captured CUDA graph (SearchParams::graph).
 
         Additions: a per-query nprobe, capped at `nprobe`: given
         (nprobe_per_query, nq values) or chosen by a ProbeModel (`budget`, at
@@ -337,7 +340,7 @@ class Index:
         nq = q.shape[0]
         ids = np.zeros((nq, k), np.uint32)
         dists = np.zeros((nq, k), np.float32)
-        if budget is None and nprobe_per_query is None and not return_nprobe:
+        if budget is None and nprobe_per_query is None and not return_nprobe and not graph:
             _check(_lib.katoann_index_search(self._h, _ptr(q), nq, k, nprobe, _RANKING[ranking],
                                              survivors, _SELECTION[selection], _ptr(ids),
                                              _ptr(dists)))
@@ -351,15 +354,16 @@ class Index:
         _check(_lib.katoann_index_search_budget(
             self._h, _ptr(q), nq, k, nprobe, _RANKING[ranking], survivors, _SELECTION[selection],
             budget._h if budget is not None else None, float(threshold),
-            _ptr(npq) if npq is not None else None, _ptr(used), _ptr(ids), _ptr(dists)))
+            _ptr(npq) if npq is not None else None, _ptr(used), _ptr(ids), _ptr(dists), int(graph)))
         return (ids, dists, used) if return_nprobe else (ids, dists)
 
     def search_into(self, q_ptr: int, nq: int, ids_ptr: int, dists_ptr: int, k: int = 10,
                     nprobe: int = 64, ranking: str = "prefix", survivors: int = 32,
                     selection: str = "threshold", budget: "ProbeModel | None" = None,
-                    threshold: float = 0.95, nprobe_out_ptr: int = 0) -> None:
-        """search() on raw host pointers (e.g. pinned buffers); no normalisation."""
-        if budget is None and not nprobe_out_ptr:
+                    threshold: float = 0.95, nprobe_out_ptr: int = 0, graph: bool = False) -> None:
+        """search() on raw host pointers (e.g. pinned buffers); no normalisation.
+        graph=True replays each pass's kernels as a captured CUDA graph."""
+        if budget is None and not nprobe_out_ptr and not graph:
             _check(_lib.katoann_index_search(self._h, C.c_void_p(q_ptr), nq, k, nprobe,
                                              _RANKING[ranking], survivors, _SELECTION[selection],
                                              C.c_void_p(ids_ptr), C.c_void_p(dists_ptr)))
@@ -368,7 +372,7 @@ class Index:
             self._h, C.c_void_p(q_ptr), nq, k, nprobe, _RANKING[ranking], survivors,
             _SELECTION[selection], budget._h if budget is not None else None, float(threshold),
             None, C.c_void_p(nprobe_out_ptr) if nprobe_out_ptr else None, C.c_void_p(ids_ptr),
-            C.c_void_p(dists_ptr)))
+            C.c_void_p(dists_ptr), int(graph)))
 
     def search_device(self, queries, ids, dists, k: int = 10, nprobe: int = 64,
                       ranking: str = "prefix", survivors: int = 32, selection: str = "threshold",

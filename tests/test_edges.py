@@ -114,3 +114,33 @@ def test_phase_timer_brackets_the_top_kernels(small):
         assert n == 2 and 0 < ms <= phases[phase] + 1e-3, (name, kern, phases)
     # a read with no passes since clears the kernel sums too
     assert timer.read()[1] == 0 and all(n == 0 for _, n in timer.kernels().values())
+
+
+def test_host_search_replayed_as_a_graph(small):
+    """Index.search with graph=True (each pass's kernels a captured graph of
+    the index's own buffers, the copies outside it) gives the plain search's
+    results and the oracle's: repeated calls, another k, a batch split into
+    passes of 16 queries, and per-query budgets."""
+    import katoann
+    prefix, queries, idx = small
+    ref = oracle.OracleIndex(prefix)
+    for k, nprobe in ((10, 4), (5, 6), (10, 4)):
+        got = idx.search(queries, k=k, nprobe=nprobe, survivors=32, graph=True)
+        plain = idx.search(queries, k=k, nprobe=nprobe, survivors=32)
+        want = ref.search(queries, k=k, nprobe=nprobe, survivors=32)
+        for a, b, c in zip(got, plain, want):
+            assert np.array_equal(a, b) and np.array_equal(a, c), (k, nprobe)
+    passes = katoann.Index()
+    passes.load(prefix, max_batch=16)
+    for _ in range(2):
+        ids, dists = passes.search(queries, k=10, nprobe=4, survivors=32, graph=True)
+        want = ref.search(queries, k=10, nprobe=4, survivors=32)
+        assert np.array_equal(ids, want[0]) and np.array_equal(dists, want[1])
+    npq = (np.arange(len(queries)) % 5 + 1).astype(np.uint32)
+    ids, dists, used = idx.search(queries, k=10, nprobe=6, survivors=32, nprobe_per_query=npq,
+                                  return_nprobe=True, graph=True)
+    assert np.array_equal(used, npq)
+    for p in np.unique(npq):
+        sel = np.nonzero(npq == p)[0]
+        want = ref.search(queries[sel], k=10, nprobe=int(p), survivors=32)
+        assert np.array_equal(ids[sel], want[0]) and np.array_equal(dists[sel], want[1]), p
